@@ -1,0 +1,269 @@
+/*
+ * axisym_gb300.h - C ABI of the GB300 (sm_103a) implementation of the
+ * PyAxisymFlow per-timestep grid hot path.
+ *
+ * Conventions
+ *   - Every field is a dense row-major (nr, nz) array in device memory:
+ *     axis 0 is r (grid_size_r rows), axis 1 is z (grid_size_z, contiguous),
+ *     exactly the numpy layout the reference kernels take.
+ *   - "_f64" entry points compute in double, "_f32" in float.
+ *   - Every call is asynchronous on `stream` (a cudaStream_t; NULL = legacy
+ *     default stream) unless its comment says it synchronises.
+ *   - Every call returns an axi_status; axi_last_error() describes the last
+ *     failure on the calling thread. Nothing allocates device memory unless
+ *     its comment says so: scratch is passed in by the caller.
+ *   - Citations name the reference function each entry replaces
+ *     (file:line, relative to the PyAxisymFlow project root).
+ */
+#ifndef AXISYM_GB300_H
+#define AXISYM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  AXI_OK = 0,
+  AXI_ERR_INVALID = 1,        /* bad size, null pointer or parameter */
+  AXI_ERR_CUDA = 2,           /* launch or runtime failure */
+  AXI_ERR_NOT_CONVERGED = 3,  /* iteration cap reached (least-squares front marching) */
+  AXI_ERR_NONFINITE = 4,      /* a NaN/Inf was detected in a reduction */
+  AXI_ERR_RANGE = 5           /* a stencil would read outside the grid */
+} axi_status;
+
+/* Library version (major * 10000 + minor * 100 + patch). */
+int axi_version(void);
+/* Message of the last failing call on this thread ("" if none). */
+const char* axi_last_error(void);
+
+/* ---------------------------------------------------------------------
+ * Velocity from the Stokes stream function.
+ * kernels/compute_velocity_from_psi.py:4-17 compute_velocity_from_psi_unb(u_z, u_r, psi, R, dx)
+ * ------------------------------------------------------------------ */
+int axi_velocity_from_psi_unb_f64(double* u_z, double* u_r, const double* psi, const double* R,
+                                  int nr, int nz, double dx, void* stream);
+int axi_velocity_from_psi_unb_f32(float* u_z, float* u_r, const float* psi, const float* R,
+                                  int nr, int nz, float dx, void* stream);
+/* kernels/compute_velocity_from_psi.py:20-34 (_periodic): exchanges `ghost` periodic
+ * z-ghost columns of psi in place first (kernels/periodic_boundary_ghost_comm.py:9-13). */
+int axi_velocity_from_psi_periodic_f64(double* u_z, double* u_r, double* psi, const double* R,
+                                       int nr, int nz, double dx, int ghost, void* stream);
+int axi_velocity_from_psi_periodic_f32(float* u_z, float* u_r, float* psi, const float* R,
+                                       int nr, int nz, float dx, int ghost, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Vorticity from velocity on the interior [1:-1, 1:-1].
+ * kernels/compute_vorticity_from_velocity.py:4-13 (_unb) and :16-28 (_periodic,
+ * which first exchanges the ghosts of u_r and u_z in place).
+ * ------------------------------------------------------------------ */
+int axi_vorticity_from_velocity_unb_f64(double* vort, const double* u_z, const double* u_r,
+                                        int nr, int nz, double dx, void* stream);
+int axi_vorticity_from_velocity_unb_f32(float* vort, const float* u_z, const float* u_r,
+                                        int nr, int nz, float dx, void* stream);
+int axi_vorticity_from_velocity_periodic_f64(double* vort, double* u_z, double* u_r,
+                                             int nr, int nz, double dx, int ghost, void* stream);
+int axi_vorticity_from_velocity_periodic_f32(float* vort, float* u_z, float* u_r,
+                                             int nr, int nz, float dx, int ghost, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Implicit Brinkman penalisation, elementwise over n cells.
+ * kernels/brinkmann_penalize.py:4-16
+ * brinkmann_penalize(lam, dt, char_func, U_z, U_r, grid_u_z, grid_u_r, penalized_u_z, penalized_u_r)
+ * ------------------------------------------------------------------ */
+int axi_brinkmann_penalize_f64(double lam, double dt, const double* char_func, double U_z,
+                               double U_r, const double* grid_u_z, const double* grid_u_r,
+                               double* penalized_u_z, double* penalized_u_r, int64_t n,
+                               void* stream);
+int axi_brinkmann_penalize_f32(float lam, float dt, const float* char_func, float U_z, float U_r,
+                               const float* grid_u_z, const float* grid_u_r, float* penalized_u_z,
+                               float* penalized_u_r, int64_t n, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Smoothed Heaviside of a level set, elementwise over n cells (reads H).
+ * kernels/smooth_Heaviside.py:5-14 smooth_Heaviside(H, phi, blend_w)
+ * ------------------------------------------------------------------ */
+int axi_smooth_heaviside_f64(double* H, const double* phi, double blend_w, int64_t n,
+                             void* stream);
+int axi_smooth_heaviside_f32(float* H, const float* phi, float blend_w, int64_t n, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Sine taper of boundary vorticity.
+ * kernels/kill_boundary_vorticity_sine.py:4-14 (_z, uses Z) and :17-27 (_r, uses R).
+ * The reference's literal "1 - Z" / "1 - R" (unit domain length) is kept.
+ * ------------------------------------------------------------------ */
+int axi_kill_boundary_vorticity_sine_z_f64(double* vort, const double* Z, int nr, int nz,
+                                           int width, double dx, void* stream);
+int axi_kill_boundary_vorticity_sine_z_f32(float* vort, const float* Z, int nr, int nz,
+                                           int width, float dx, void* stream);
+int axi_kill_boundary_vorticity_sine_r_f64(double* vort, const double* R, int nr, int nz,
+                                           int width, double dx, void* stream);
+int axi_kill_boundary_vorticity_sine_r_f32(float* vort, const float* R, int nr, int nz,
+                                           int width, float dx, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Explicit two-stage diffusion of vorticity.
+ * kernels/diffusion_RK2.py:4-44 diffusion_RK2_unb(vorticity, temp_vorticity, R, nu, dt, dx)
+ * and :47-89 (_periodic: ghost exchange of vorticity, then of temp_vorticity).
+ * temp_vorticity is both scratch and output, as in the reference.
+ * ------------------------------------------------------------------ */
+int axi_diffusion_rk2_unb_f64(double* vort, double* temp_vort, const double* R, int nr, int nz,
+                              double nu, double dt, double dx, void* stream);
+int axi_diffusion_rk2_unb_f32(float* vort, float* temp_vort, const float* R, int nr, int nz,
+                              float nu, float dt, float dx, void* stream);
+int axi_diffusion_rk2_periodic_f64(double* vort, double* temp_vort, const double* R, int nr,
+                                   int nz, double nu, double dt, double dx, int ghost,
+                                   void* stream);
+int axi_diffusion_rk2_periodic_f32(float* vort, float* temp_vort, const float* R, int nr, int nz,
+                                   float nu, float dt, float dx, int ghost, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Periodic z-ghost exchange, in place.
+ * kernels/periodic_boundary_ghost_comm.py:4-15 (plain) and :18-33 (eta: +/- shift
+ * of z_max - 2*ghost*dx).
+ * ------------------------------------------------------------------ */
+int axi_periodic_ghost_comm_f64(double* field, int nr, int nz, int ghost, void* stream);
+int axi_periodic_ghost_comm_f32(float* field, int nr, int nz, int ghost, void* stream);
+int axi_periodic_ghost_comm_eta_f64(double* field, int nr, int nz, int ghost, double z_max,
+                                    double dx, void* stream);
+int axi_periodic_ghost_comm_eta_f32(float* field, int nr, int nz, int ghost, float z_max,
+                                    float dx, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Body force integrals, accumulated in double whatever the field type.
+ * kernels/compute_forces.py:4-17 compute_force_on_body(...) -> (F_pen, F_un)
+ * kernels/force_projection.py:5-15 force_projection(...) -> (U_z, U_r)
+ * `out` is device memory for 2 doubles. `partials` is device scratch of
+ * axi_reduction_scratch_doubles(n) doubles. The reduction order is fixed, so
+ * repeated calls give identical bits.
+ * ------------------------------------------------------------------ */
+int64_t axi_reduction_scratch_doubles(int64_t n);
+int axi_compute_force_on_body_f64(const double* R, const double* char_func, double rho_f,
+                                  double brink_lam, const double* u_z, double U_z_cm_part,
+                                  double part_vol, double dt, double diff, int64_t n,
+                                  double* partials, double* out, void* stream);
+int axi_compute_force_on_body_f32(const float* R, const float* char_func, double rho_f,
+                                  double brink_lam, const float* u_z, double U_z_cm_part,
+                                  double part_vol, double dt, double diff, int64_t n,
+                                  double* partials, double* out, void* stream);
+int axi_force_projection_f64(double rho_s, const double* char_func, const double* u_z,
+                             const double* u_r, const double* R, int64_t n, double* partials,
+                             double* out, void* stream);
+int axi_force_projection_f32(double rho_s, const float* char_func, const float* u_z,
+                             const float* u_r, const float* R, int64_t n, double* partials,
+                             double* out, void* stream);
+
+/* ---------------------------------------------------------------------
+ * ENO3 Euler-forward advection with the axis mirror done by index reflection
+ * (no doubled buffers). `scratch` is one (nr, nz) field per advected field.
+ * kernels/advect_vorticity_via_eno3.py:8-44 (vorticity odd, u_z even, u_r odd;
+ *   conservative flux pyst_kernels/advection_flux.py:9-163, step
+ *   pyst_kernels/advection_timestep.py:37-54), :47-91 (_periodic: ghost
+ *   exchange of u_z, u_r, vorticity first).
+ * elasto_kernels/advect_refmap_via_eno3.py:8-54 (eta1 even, eta2 odd, the
+ *   non-conservative flux advection_flux.py:166-332), :57-115 (_periodic:
+ *   u_z, u_r, eta2 plain exchange; eta1 shifted exchange with z_max).
+ * ------------------------------------------------------------------ */
+int axi_advect_vorticity_eno3_f64(double* vort, const double* u_z, const double* u_r,
+                                  double* scratch, int nr, int nz, double dt_by_dx,
+                                  void* stream);
+int axi_advect_vorticity_eno3_f32(float* vort, const float* u_z, const float* u_r,
+                                  float* scratch, int nr, int nz, float dt_by_dx, void* stream);
+int axi_advect_vorticity_eno3_periodic_f64(double* vort, double* u_z, double* u_r,
+                                           double* scratch, int nr, int nz, double dt_by_dx,
+                                           int ghost, void* stream);
+int axi_advect_vorticity_eno3_periodic_f32(float* vort, float* u_z, float* u_r, float* scratch,
+                                           int nr, int nz, float dt_by_dx, int ghost,
+                                           void* stream);
+int axi_advect_refmap_eno3_f64(double* eta1, double* eta2, const double* u_z, const double* u_r,
+                               double* scratch2, int nr, int nz, double dt_by_dx, void* stream);
+int axi_advect_refmap_eno3_f32(float* eta1, float* eta2, const float* u_z, const float* u_r,
+                               float* scratch2, int nr, int nz, float dt_by_dx, void* stream);
+int axi_advect_refmap_eno3_periodic_f64(double* eta1, double* eta2, double* u_z, double* u_r,
+                                        double* scratch2, int nr, int nz, double dt_by_dx,
+                                        int ghost, double z_max, double dx, void* stream);
+int axi_advect_refmap_eno3_periodic_f32(float* eta1, float* eta2, float* u_z, float* u_r,
+                                        float* scratch2, int nr, int nz, float dt_by_dx,
+                                        int ghost, float z_max, float dx, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Neo-Hookean solid stress and its curl into vorticity.
+ * elasto_kernels/solid_sigma.py:4-29 solid_sigma(s11, s12, s22, G, dx, eta_1, eta_2,
+ *   eta_1z, eta_1r, eta_2z, eta_2r): the gradient arrays are outputs written where
+ *   the reference writes them; stress uses whatever they hold elsewhere.
+ * elasto_kernels/div_tau.py:4-34 update_vorticity_from_solid_stress(vorticity, tau_z,
+ *   tau_r, tau11, tau12, tau22, R, dt, dx)
+ * ------------------------------------------------------------------ */
+int axi_solid_sigma_f64(double* s11, double* s12, double* s22, double G, double dx,
+                        const double* eta1, const double* eta2, double* eta1z, double* eta1r,
+                        double* eta2z, double* eta2r, int nr, int nz, void* stream);
+int axi_solid_sigma_f32(float* s11, float* s12, float* s22, float G, float dx, const float* eta1,
+                        const float* eta2, float* eta1z, float* eta1r, float* eta2z,
+                        float* eta2r, int nr, int nz, void* stream);
+int axi_update_vorticity_from_solid_stress_f64(double* vort, double* tau_z, double* tau_r,
+                                               const double* tau11, const double* tau12,
+                                               const double* tau22, const double* R, int nr,
+                                               int nz, double dt, double dx, void* stream);
+int axi_update_vorticity_from_solid_stress_f32(float* vort, float* tau_z, float* tau_r,
+                                               const float* tau11, const float* tau12,
+                                               const float* tau22, const float* R, int nr,
+                                               int nz, float dt, float dx, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Least-squares front-marching extrapolation of (eta_x, eta_y), first order.
+ * core/src/extrapolate_using_least_squares.hpp:450-467 (impl :142-446) as bound by
+ * core/src/extrapolate_using_least_squares_bind.cpp:88-91
+ * extrapolate_using_least_squares_till_first_order(current_flag, target_flag, eta_x,
+ * eta_y, grid_x, grid_y), int16 flags, double fields, all (n0, n1) row-major.
+ * current_flag is updated in place. `work` is device scratch of
+ * axi_lsq_work_bytes(n0, n1) bytes. Runs at most max_sweeps sweeps
+ * (AXI_ERR_NOT_CONVERGED past it); a 3x3 window leaving the grid gives
+ * AXI_ERR_RANGE (the reference reads out of bounds there). Synchronises the
+ * stream to return the status; *sweeps_out (host) receives the sweep count.
+ * ------------------------------------------------------------------ */
+int64_t axi_lsq_work_bytes(int n0, int n1);
+int axi_extrapolate_lsq_first_order_f64(int16_t* current_flag, const int16_t* target_flag,
+                                        double* eta_x, double* eta_y, const double* grid_x,
+                                        const double* grid_y, int n0, int n1, int max_sweeps,
+                                        void* work, int* sweeps_out, void* stream);
+/* elasto_kernels/extrapolate_eta_using_least_squares_unb.py:7-30 with
+ * elasto_kernels/extrapolate_using_least_squares.py:33-38 folded in: builds the
+ * axis-mirrored (2*nr, nz) level set, masked eta and flags (phi < 0, phi <
+ * extrap_zone) from the upper-half fields, extrapolates, and copies back.
+ * inside_solid is a byte mask (numpy bool). The doubled buffers are caller
+ * scratch of 2*nr*nz doubles each; flags of 2*nr*nz int16 each. grid_y must
+ * hold 2*nr coordinates (the reference passes z). */
+int axi_extrapolate_eta_with_least_squares_f64(
+    const uint8_t* inside_solid, const double* ball_phi, double* eta1, double* eta2,
+    double* ball_phi_double, double* eta1_double, double* eta2_double, int16_t* current_flag,
+    int16_t* target_flag, double extrap_zone, int nr, int nz, const double* grid_x,
+    const double* grid_y, int max_sweeps, void* work, int* sweeps_out, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Fast-diagonalisation spectral transform (Stokes / potential solve,
+ * implicit diffusion step):
+ *   out = Er * ((Er_inv_w * in * EzinvT) .* inv_eig) * EzT
+ * kernels/FastDiagonalisationStokesSolver.py:130-156 (Er_inv_w = E_r^-1 diag(r)),
+ * kernels/FastDiagonalisationPotentialSolver.py:119-145 and
+ * kernels/implicit_diffusion_solver.py:108-143 (Er_inv_w = E_r^-1).
+ * Er, Er_inv_w: (nr, nr); EzinvT, EzT: (nz, nz); inv_eig: (nr, nz), all
+ * row-major double in device memory, from the host eigendecomposition.
+ * `in` and `out` are (nr, nz) with row strides ld_in / ld_out >= nz (the
+ * periodic examples solve on the ghost-free slice field[:, g:-g]).
+ * work: device scratch of 2*nr*nz doubles. `out` may alias `in`.
+ * ------------------------------------------------------------------ */
+int axi_fd_transform_f64(double* out, int ld_out, const double* in, int ld_in,
+                         const double* Er_inv_w, const double* EzinvT, const double* inv_eig,
+                         const double* Er, const double* EzT, double* work, int nr, int nz,
+                         void* stream);
+/* Row-major double GEMM C = A(M,K) * B(K,N) (.* S(M,N) if S != NULL), row
+ * strides ldc, lda, ldb; S is dense (row stride N). */
+int axi_dgemm_f64(double* C, int ldc, const double* A, int lda, const double* B, int ldb,
+                  const double* S, int M, int N, int K, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AXISYM_GB300_H */

@@ -378,6 +378,7 @@ def advection_timestep_euler_forward_eno3(field, velocity, dt_by_dx, conservativ
     def sh(arr, d0, d1):
         return arr[g + d0: n0 - g + d0, g + d1: n1 - g + d1]
 
+    inner = flux[s0, s1]
     if conservative:
         xf = _eno3_face_conservative(sh(f, 0, -1), sh(f, 0, 0), sh(f, 0, 1), sh(f, 0, 2),
                                      sh(ux, 0, -1), sh(ux, 0, 0), sh(ux, 0, 1), sh(ux, 0, 2))
@@ -387,22 +388,26 @@ def advection_timestep_euler_forward_eno3(field, velocity, dt_by_dx, conservativ
                                      sh(uy, -1, 0), sh(uy, 0, 0), sh(uy, 1, 0), sh(uy, 2, 0))
         yb = _eno3_face_conservative(sh(f, -2, 0), sh(f, -1, 0), sh(f, 0, 0), sh(f, 1, 0),
                                      sh(uy, -2, 0), sh(uy, -1, 0), sh(uy, 0, 0), sh(uy, 1, 0))
+        inner[...] = inner + a * xf
+        inner[...] = inner - a * xb
+        inner[...] = inner + a * yf
+        inner[...] = inner - a * yb
     else:
+        # advection_flux.py:189-202: advection_flux + inv_dx * (face) * velocity[0, 0]
         u0x = sh(ux, 0, 0)
         u0y = sh(uy, 0, 0)
         xf = _eno3_face_non_conservative(sh(f, 0, -1), sh(f, 0, 0), sh(f, 0, 1), sh(f, 0, 2),
-                                         u0x, sh(ux, 0, 1)) * u0x
+                                         u0x, sh(ux, 0, 1))
         xb = _eno3_face_non_conservative(sh(f, 0, -2), sh(f, 0, -1), sh(f, 0, 0), sh(f, 0, 1),
-                                         sh(ux, 0, -1), u0x) * u0x
+                                         sh(ux, 0, -1), u0x)
         yf = _eno3_face_non_conservative(sh(f, -1, 0), sh(f, 0, 0), sh(f, 1, 0), sh(f, 2, 0),
-                                         u0y, sh(uy, 1, 0)) * u0y
+                                         u0y, sh(uy, 1, 0))
         yb = _eno3_face_non_conservative(sh(f, -2, 0), sh(f, -1, 0), sh(f, 0, 0), sh(f, 1, 0),
-                                         sh(uy, -1, 0), u0y) * u0y
-    inner = flux[s0, s1]
-    inner[...] = inner + a * xf
-    inner[...] = inner - a * xb
-    inner[...] = inner + a * yf
-    inner[...] = inner - a * yb
+                                         sh(uy, -1, 0), u0y)
+        inner[...] = inner + (a * xf) * u0x
+        inner[...] = inner - (a * xb) * u0x
+        inner[...] = inner + (a * yf) * u0y
+        inner[...] = inner - (a * yb) * u0y
     field[...] = field + flux
 
 

@@ -1,0 +1,82 @@
+// Shared helpers of the sm_103a kernels behind the C ABI in include/axisym_gb300.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/axisym_gb300.h"
+
+namespace axi {
+
+// Per-thread message of the last failing entry point (read by axi_last_error).
+void set_error(const char* fmt, ...);
+void clear_error();
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline int ceil_div(long long a, long long b) { return static_cast<int>((a + b - 1) / b); }
+
+// Turns a launch error into AXI_ERR_CUDA with a message naming the kernel.
+inline int launch_status(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("%s: CUDA launch failed: %s", what, cudaGetErrorString(e));
+    return AXI_ERR_CUDA;
+  }
+  return AXI_OK;
+}
+
+inline int check_grid(const char* what, int nr, int nz, int min_nr = 3, int min_nz = 3) {
+  if (nr < min_nr || nz < min_nz) {
+    set_error("%s: grid %d x %d is smaller than %d x %d", what, nr, nz, min_nr, min_nz);
+    return AXI_ERR_INVALID;
+  }
+  return AXI_OK;
+}
+
+inline int check_ptr(const char* what, const void* p, const char* name) {
+  if (p == nullptr) {
+    set_error("%s: %s is null", what, name);
+    return AXI_ERR_INVALID;
+  }
+  return AXI_OK;
+}
+
+// Number of SMs on the current device (cached per device).
+int sm_count();
+
+}  // namespace axi
+
+#define AXI_TRY(expr)            \
+  do {                           \
+    int _st = (expr);            \
+    if (_st != AXI_OK) return _st; \
+  } while (0)
+
+// Rounded arithmetic that the compiler may not contract into FMA: used where
+// results must match the reference's numpy evaluation bit for bit.
+template <typename T> __device__ __forceinline__ T rn_mul(T a, T b);
+template <typename T> __device__ __forceinline__ T rn_add(T a, T b);
+template <typename T> __device__ __forceinline__ T rn_sub(T a, T b);
+template <typename T> __device__ __forceinline__ T rn_div(T a, T b);
+template <> __device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+template <> __device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(a, b); }
+template <> __device__ __forceinline__ double rn_sub(double a, double b) { return __dsub_rn(a, b); }
+template <> __device__ __forceinline__ double rn_div(double a, double b) { return __ddiv_rn(a, b); }
+template <> __device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+template <> __device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
+template <> __device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+template <> __device__ __forceinline__ float rn_div(float a, float b) { return __fdiv_rn(a, b); }
+
+// Host-side product of two scalars (kept separate so no contraction applies).
+template <typename T> inline T rn_host_mul(T a, T b) { return a * b; }
+
+template <typename T> __device__ __forceinline__ T dev_sin(T x);
+template <> __device__ __forceinline__ double dev_sin(double x) { return sin(x); }
+template <> __device__ __forceinline__ float dev_sin(float x) { return sinf(x); }
+
+template <typename T> struct Pi;
+template <> struct Pi<double> { static constexpr double v = 3.141592653589793; };
+template <> struct Pi<float> { static constexpr float v = 3.14159265f; };
