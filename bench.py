@@ -1,0 +1,337 @@
+"""Benchmark of the per-timestep hot path on GB300 (one JSON line on stdout).
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                [--workload ensemble64|sphere512] [--precision f32|f64]
+
+A "step" advances every case of the workload by one timestep (the loop body
+of examples/FlowPastSphere/flow_past_sphere.py:107-188). value = cell-updates
+per second over the whole job (all ranks): cells of all cases x steps / time.
+
+Workloads (synthetic, seeded; there is no dataset):
+  ensemble64  64 rigid-sphere cases, nz in {256, 512, 768, 1024}, nr = nz / 2,
+              z in [0, 2], r in [0, 1], Re log-uniform in [10, 1000], sphere
+              radius uniform in [0.04, 0.12], seed 4
+  sphere512   one 512 x 256 rigid sphere, Re 100, radius 0.0625 at z = 0.5
+
+--impl reference times the reference's CPU path restated by the oracle
+(numpy FP64, all host cores for BLAS) on a bounded sample of the same
+workload; it never touches the GPU.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "cell-updates/s on 1 GB300, batched FP32 vs plain FP64 at <=1e-5 L2; p50/p99 lat"
+UNIT = "cell-updates/s"
+PHASES = ("kill", "transform", "vel_max", "penalise", "adv_diff1", "diff2")
+# Algorithmic fields moved per cell by each stencil phase (reads + writes):
+# vel_max psi; penalise psi chi omega -> u_z u_r omega; adv_diff1 omega u_z
+# u_r -> w_adv w_tmp; diff2 w_adv w_tmp -> omega.
+PHASE_FIELDS = {"vel_max": 1, "penalise": 6, "adv_diff1": 5, "diff2": 3}
+
+
+def ensemble_cases(workload, seed=4):
+    from pyaxisymflow_gb300.engine import RigidBodyCase
+    if workload == "sphere512":
+        return [RigidBodyCase()]
+    rng = np.random.default_rng(seed)
+    cases = []
+    for k in range(64):
+        nz = int(rng.choice([256, 512, 768, 1024]))
+        Re = float(np.exp(rng.uniform(np.log(10.0), np.log(1000.0))))
+        radius = float(rng.uniform(0.04, 0.12))
+        cases.append(RigidBodyCase(nz=nz, nr=nz // 2, dx=2.0 / nz, r_sphere=radius, Re=Re,
+                                   z_cm=0.5, seed=1000 + k))
+    return cases
+
+
+def peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return p.get("hbm_gbs", 6800.0), p.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._thread = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.gpu}",
+                                      f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._thread.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        self._thread.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if len(s) > 5 + k and s[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_oracle_rate(cases, steps):
+    """Oracle (numpy FP64) cell-updates/s on the host for `cases`, `steps` steps each."""
+    from oracle import kernels as K
+    from oracle import simulation as sim
+    runs = []
+    for c in cases:
+        oc = sim.RigidSphereCase(nz=c.nz, nr=c.nr, dx=c.dx, z_cm=c.z_cm, r_sphere=c.r_sphere,
+                                 U0=c.U0, Re=c.Re, lam=c.lam, cfl=c.cfl, kill_width=c.kill_width,
+                                 ramp=c.ramp, noise=c.noise, seed=c.seed)
+        st, coords = sim.rigid_sphere_init(oc, K)
+        solver = K.FastDiagonalisationStokesSolver(oc.nr, oc.nz, oc.dx)
+        adv = K.gen_advect_vorticity_via_eno3(oc.dx, oc.nr, oc.nz)
+        runs.append((oc, st, coords, solver, adv))
+    cells = 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for oc, st, coords, solver, adv in runs:
+            sim.rigid_sphere_step(oc, st, coords, solver, adv, K)
+            cells += oc.nr * oc.nz
+    dt = time.perf_counter() - t0
+    return cells / dt, dt, cells
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    cases = ensemble_cases(args.workload)
+    sample = cases[:4] if len(cases) > 4 else cases
+    from oracle import kernels as K  # noqa: F401  (import cost outside timing)
+    rates = []
+    for _ in range(args.warmup):
+        cpu_oracle_rate(sample, 1)
+    for _ in range(args.steps):
+        r, _, _ = cpu_oracle_rate(sample, 1)
+        rates.append(r)
+    value = float(np.median(rates))
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    desc = (f"{len(sample)} of the {len(cases)} cases "
+            f"({', '.join(f'{c.nz}x{c.nr}' for c in sample)}), 1 timestep each per step, "
+            "numpy FP64 oracle (BLAS threads = all cores, elementwise single-threaded)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(1000.0 * sum(c.nr * c.nz for c in sample) / value),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": args.workload, "sample": desc},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, world, rank, local):
+    import torch
+    from pyaxisymflow_gb300 import _native
+    from pyaxisymflow_gb300.engine import ST_CD, ST_DT, RigidEnsemble
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _native.lib()
+    cases = ensemble_cases(args.workload)
+    ens = RigidEnsemble(cases, precision=args.precision, device=dev)
+    cells = ens.cells()
+    stream = torch.cuda.current_stream(dev)
+    ens.capture(1)
+    for _ in range(args.warmup):
+        ens.replay()
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    # ---- timed region: K graph replays, device time by CUDA events ------------
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            ens.replay()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier(world)
+    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(world, ms)
+    ms_per_step = ms / args.steps
+    value = cells * world / (ms_per_step / 1000.0)
+    status = ens.status()
+    # ---- per-phase device times (same stream, same step sequence) -------------
+    ph_ms = {p: 0.0 for p in PHASES}
+    nph = max(3, min(args.steps, 10))
+    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            for _ in PHASES] for _ in range(nph)]
+    for s in range(nph):
+        for k, p in enumerate(PHASES):
+            evs[s][k][0].record(stream)
+            ens.phase(k)
+            evs[s][k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    for s in range(nph):
+        for k, p in enumerate(PHASES):
+            ph_ms[p] += evs[s][k][0].elapsed_time(evs[s][k][1]) / nph
+    # ---- end to end through the public API with host buffers ------------------
+    host_w = [torch.empty(c.nr * c.nz, dtype=ens.dtype, pin_memory=True) for c in cases]
+    for k in range(len(cases)):
+        host_w[k].copy_(ens.fields[k]["omega"].reshape(-1))
+    host_state = torch.empty(ens.state.shape, dtype=torch.float64, pin_memory=True)
+    torch.cuda.synchronize(dev)
+    field_bytes = sum(h.numel() * h.element_size() for h in host_w)
+    h2d = field_bytes
+    d2h = field_bytes + host_state.numel() * 8
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        # host-resident vorticity in, one step, vorticity and (dt, Cd) back out
+        for k in range(len(cases)):
+            ens.fields[k]["omega"].view(-1).copy_(host_w[k], non_blocking=True)
+        ens.step(1)
+        for k in range(len(cases)):
+            host_w[k].copy_(ens.fields[k]["omega"].view(-1), non_blocking=True)
+        host_state.copy_(ens.state, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        _ = float(host_state[0, ST_CD]) + float(host_state[0, ST_DT])
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_s = max_over_ranks(world, e2e_s)
+    e2e_value = cells * world / e2e_s
+    # ---- roofline of the dominant kernel ---------------------------------------
+    hbm, bf16, src = peaks()
+    dom = max(ph_ms, key=ph_ms.get)
+    esize = 8 if args.precision == "f64" else 4
+    if dom == "transform":
+        flops = sum(4.0 * c.nr * c.nz * (c.nr + c.nz) for c in cases)
+        achieved = flops / (ph_ms[dom] / 1000.0) / 1e12
+        if args.precision == "f64":
+            roof = {"bound": "fp64", "achieved": achieved, "peak": 1.05, "unit": "TFLOP/s",
+                    "peak_source": "DMMA/DFMA throughput probe on this pool's GB300"}
+        else:
+            roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                    "peak_source": f"{src} bf16"}
+    else:
+        nbytes = sum(PHASE_FIELDS[dom] * esize * c.nr * c.nz for c in cases)
+        achieved = nbytes / (ph_ms[dom] / 1000.0) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "peak_source": f"{src} hbm"}
+    roof["kernel"] = dom
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["traffic"] = None
+    stencil_bytes = sum(15 * esize * c.nr * c.nz for c in cases)
+    stencil_ms = sum(ph_ms[p] for p in PHASE_FIELDS)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
+        "data": "synthetic",
+        "config": {"workload": args.workload, "cases": len(cases), "cells_per_step": cells,
+                   "precision": args.precision, "l2": "working set > L2 (129 MB)",
+                   "parallelism": f"case-parallel replicas x{world}"},
+        "roofline": roof,
+        "phase_ms": ph_ms,
+        "stencil_hbm_gbs": stencil_bytes / (stencil_ms / 1000.0) / 1e9,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": None,
+        "clocks": clocks.summary(),
+        "status_ok": bool(np.all(status == 0)),
+    }
+    n_launch = 1 + 4 * len(cases) + 4
+    line["gpu_launches"] = n_launch * args.steps
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sample = cases[:2]
+        rate, secs, _ = cpu_oracle_rate(sample, 2)
+        cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else 1
+        line["cpu_baseline"] = {
+            "value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"cases {', '.join(f'{c.nz}x{c.nr}' for c in sample)}, 2 timesteps each, "
+                      f"numpy FP64 oracle, {secs:.1f} s"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="ensemble64", choices=["ensemble64", "sphere512"])
+    ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gb300(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

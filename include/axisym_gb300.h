@@ -262,6 +262,81 @@ int axi_fd_transform_f64(double* out, int ld_out, const double* in, int ld_in,
 int axi_dgemm_f64(double* C, int ldc, const double* A, int lda, const double* B, int ldb,
                   const double* S, int M, int N, int K, void* stream);
 
+/* ---------------------------------------------------------------------
+ * Fused per-timestep engine for flows past rigid bodies, many cases per launch.
+ * One step = the loop body of examples/FlowPastSphere/flow_past_sphere.py:107-188
+ * (kill_boundary_vorticity_sine_z/_r, FastDiagonalisationStokesSolver.solve,
+ * compute_velocity_from_psi_unb, free stream ramp, CFL dt,
+ * brinkmann_penalize + compute_vorticity_from_velocity_unb, drag,
+ * advect_vorticity_via_eno3, diffusion_RK2_unb) for every case of a plan.
+ * dt, the drag coefficient and the simulated time stay on the device (state
+ * block), so steps never synchronise with the host and can be captured in a
+ * CUDA graph. Non-finite velocity or drag sets bit AXI_ERR_NONFINITE in the
+ * AXI_ST_STATUS word of the case.
+ * ------------------------------------------------------------------ */
+/* Words of the per-case device state block (doubles). */
+enum {
+  AXI_ST_T = 0,        /* simulated time */
+  AXI_ST_DT = 1,       /* last time step */
+  AXI_ST_CD = 2,       /* last drag coefficient */
+  AXI_ST_STEPS = 3,    /* steps taken */
+  AXI_ST_UMAX = 4,     /* bits of max(|u_z| + |u_r|) of the current step (uint64) */
+  AXI_ST_COUNT = 5,    /* reduction counter of the current step (uint32 in the low word) */
+  AXI_ST_STATUS = 6,   /* sticky axi_status bits (uint32 in the low word) */
+  AXI_ST_FORCE = 7,    /* last body force sum (FP64) */
+  AXI_ST_WORDS = 8
+};
+
+/* One flow-past-rigid-body case. Fields are (nr, nz) row-major in the engine
+ * precision (double for _f64, float for _f32); r, z, rinv2dx, rinv2 are
+ * double vectors of length nr / nz / nr / nr. */
+typedef struct axi_case {
+  int32_t nr, nz;
+  int32_t kill_width;
+  int32_t stencil_tile0; /* first stencil tile of this case in the plan */
+  double dx, nu, lam, U0, t_ramp, cfl, U_body, cd_scale, dt_diff, eps;
+  void* omega;
+  void* psi;
+  void* u_z;
+  void* u_r;
+  void* chi;
+  void* w_adv;   /* scratch: advected vorticity */
+  void* w_tmp;   /* scratch: RK2 stage */
+  const double* r;
+  const double* z;
+  const double* rinv2dx; /* 1 / (2 dx r_i) */
+  const double* rinv2;   /* 1 / r_i^2 */
+  const void* Er;        /* (nr, nr) */
+  const void* Er_inv_w;  /* (nr, nr), E_r^-1 diag(r) */
+  const void* EzinvT;    /* (nz, nz) */
+  const void* EzT;       /* (nz, nz) */
+  const void* inv_eig;   /* (nr, nz) */
+  void* gemm_work;       /* 2 nr nz */
+  double* state;         /* AXI_ST_WORDS doubles */
+  double* partials;      /* one double per stencil tile of the case */
+  double* history;       /* optional: 2 doubles (dt, Cd) per step, or NULL */
+  int64_t history_len;
+} axi_case;
+
+/* Host-side planning: validates the cases, assigns each its first tile
+ * (cases[k].stencil_tile0) and returns the device bytes the plan needs. */
+int axi_plan_init(axi_case* cases, int n_cases, int64_t* plan_bytes, int* n_tiles);
+/* Copies the case table and the tile table into plan_dev (caller-allocated,
+ * plan_bytes); synchronises the stream. */
+int axi_plan_upload(const axi_case* cases, int n_cases, void* plan_dev, void* stream);
+/* Advances every case of the plan by n_steps steps (fields float64 / float32). */
+int axi_rigid_step_f64(const axi_case* cases, int n_cases, const void* plan_dev, int n_tiles,
+                       int n_steps, void* stream);
+int axi_rigid_step_f32(const axi_case* cases, int n_cases, const void* plan_dev, int n_tiles,
+                       int n_steps, void* stream);
+/* One phase of a step (0 kill, 1 transform, 2 velocity max, 3 penalise,
+ * 4 advection + diffusion stage 1, 5 diffusion stage 2); running phases 0..5
+ * in order equals one axi_rigid_step. Lets a caller time each kernel. */
+int axi_rigid_phase_f64(const axi_case* cases, int n_cases, const void* plan_dev, int n_tiles,
+                        int phase, void* stream);
+int axi_rigid_phase_f32(const axi_case* cases, int n_cases, const void* plan_dev, int n_tiles,
+                        int phase, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,250 @@
+"""Fused, graph-capturable per-timestep engine for many rigid-body cases.
+
+``RigidEnsemble`` keeps every field of every case resident on one GPU and
+advances all of them with one sequence of launches per step
+(include/axisym_gb300.h: axi_rigid_step_f64 / _f32): the loop body of
+examples/FlowPastSphere/flow_past_sphere.py:107-188 per case, with dt, drag
+and time kept on the device. Cases may differ in grid size, viscosity, body
+and penalisation parameters. ``precision="f64"`` is the plain path;
+``"f32"`` runs the fields and transforms in FP32 with FP64 eigendecomposition,
+coordinates and drag accumulation.
+"""
+import ctypes
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .kernels.FastDiagonalisationStokesSolver import FastDiagonalisationStokesSolver
+from .kernels.smooth_Heaviside import smooth_Heaviside
+
+ST_T, ST_DT, ST_CD, ST_STEPS, ST_UMAX, ST_COUNT, ST_STATUS, ST_FORCE = range(8)
+ST_WORDS = 8
+
+
+class AxiCase(ctypes.Structure):
+    """Mirror of ``axi_case`` in include/axisym_gb300.h."""
+    _fields_ = [
+        ("nr", ctypes.c_int32), ("nz", ctypes.c_int32), ("kill_width", ctypes.c_int32),
+        ("stencil_tile0", ctypes.c_int32),
+        ("dx", ctypes.c_double), ("nu", ctypes.c_double), ("lam", ctypes.c_double),
+        ("U0", ctypes.c_double), ("t_ramp", ctypes.c_double), ("cfl", ctypes.c_double),
+        ("U_body", ctypes.c_double), ("cd_scale", ctypes.c_double),
+        ("dt_diff", ctypes.c_double), ("eps", ctypes.c_double),
+        ("omega", ctypes.c_void_p), ("psi", ctypes.c_void_p), ("u_z", ctypes.c_void_p),
+        ("u_r", ctypes.c_void_p), ("chi", ctypes.c_void_p), ("w_adv", ctypes.c_void_p),
+        ("w_tmp", ctypes.c_void_p),
+        ("r", ctypes.c_void_p), ("z", ctypes.c_void_p), ("rinv2dx", ctypes.c_void_p),
+        ("rinv2", ctypes.c_void_p),
+        ("Er", ctypes.c_void_p), ("Er_inv_w", ctypes.c_void_p), ("EzinvT", ctypes.c_void_p),
+        ("EzT", ctypes.c_void_p), ("inv_eig", ctypes.c_void_p),
+        ("gemm_work", ctypes.c_void_p), ("state", ctypes.c_void_p),
+        ("partials", ctypes.c_void_p), ("history", ctypes.c_void_p),
+        ("history_len", ctypes.c_int64),
+    ]
+
+
+
+
+@dataclass
+class RigidBodyCase:
+    """One flow-past-a-rigid-body case (defaults: the 512 x 256 sphere,
+    z in [0, 2], r in [0, 1], Re 100)."""
+    nz: int = 512
+    nr: int = 256
+    dx: float = 1.0 / 256
+    z_cm: float = 0.5
+    r_sphere: float = 0.0625
+    U0: float = 1.0
+    Re: float = 100.0
+    lam: float = 1e4
+    cfl: float = 0.1
+    kill_width: int = 3
+    ramp: bool = True
+    noise: float = 1e-6
+    seed: int = 0
+    body: str = "sphere"       # sphere | spheroid | torus
+    aspect: float = 1.0        # spheroid: axial / radial semi-axis
+    torus_R: float = 0.0       # torus: ring radius (r_sphere is the tube radius)
+    U_body: float = 0.0
+
+    @property
+    def nu(self):
+        return self.U0 * 2 * self.r_sphere / self.Re
+
+    @property
+    def t_ramp(self):
+        return 20 * self.r_sphere / self.U0
+
+    @property
+    def moll_zone(self):
+        return self.dx * 2 ** 0.5
+
+    def level_set(self, Z, R):
+        """Signed distance-like level set, positive inside the body
+        (examples/FlowPastSphere/flow_past_sphere.py:81,
+        examples/SpheroidStreaming/spheroid_streaming.py:92-96,
+        examples/TorusStreaming/torus_streaming.py:94-96)."""
+        if self.body == "sphere":
+            return -np.sqrt((Z - self.z_cm) ** 2 + R ** 2) + self.r_sphere
+        if self.body == "spheroid":
+            a, b = self.r_sphere * self.aspect, self.r_sphere
+            return self.r_sphere * (1.0 - np.sqrt(((Z - self.z_cm) / a) ** 2 + (R / b) ** 2))
+        if self.body == "torus":
+            return -np.sqrt((Z - self.z_cm) ** 2 + (R - self.torus_R) ** 2) + self.r_sphere
+        raise ValueError(f"unknown body {self.body!r}")
+
+
+def grid(nz, nr, dx):
+    z = np.linspace(dx / 2, nz * dx - dx / 2, nz)
+    r = np.linspace(dx / 2, nr * dx - dx / 2, nr)
+    return z, r
+
+
+class _Bases:
+    """Spectral bases shared by all cases with the same (nr, nz, dx)."""
+
+    def __init__(self, nr, nz, dx, dtype, device):
+        solver = FastDiagonalisationStokesSolver(nr, nz, dx, device=device)
+        d = solver.engine.dev
+        self.t = {k: d[k].to(dtype).contiguous() for k in
+                  ("Er", "Er_inv_w", "EzinvT", "EzT", "inv_eig")}
+
+
+class RigidEnsemble:
+    """All cases resident on one GPU, advanced together."""
+
+    def __init__(self, cases, precision="f64", device="cuda", history_steps=0,
+                 initial_vorticity=None):
+        if precision not in ("f64", "f32"):
+            raise ValueError("precision must be 'f64' or 'f32'")
+        self.precision = precision
+        self.dtype = torch.float64 if precision == "f64" else torch.float32
+        self.device = torch.device(device)
+        self.cases = list(cases)
+        self._keep = []
+        bases = {}
+        n = len(self.cases)
+        self.structs = (AxiCase * n)()
+        self.fields = []
+        self.state = torch.zeros((n, ST_WORDS), dtype=torch.float64, device=self.device)
+        self.history = (torch.zeros((n, max(history_steps, 1), 2), dtype=torch.float64,
+                                    device=self.device) if history_steps else None)
+        f = dict(dtype=self.dtype, device=self.device)
+        f64 = dict(dtype=torch.float64, device=self.device)
+        for k, c in enumerate(self.cases):
+            z, r = grid(c.nz, c.nr, c.dx)
+            Z, R = np.meshgrid(z, r)
+            key = (c.nr, c.nz, c.dx)
+            if key not in bases:
+                bases[key] = _Bases(c.nr, c.nz, c.dx, self.dtype, self.device)
+            b = bases[key]
+            if initial_vorticity is not None and initial_vorticity[k] is not None:
+                w0 = np.asarray(initial_vorticity[k], dtype=np.float64)
+            else:
+                w0 = c.noise * np.random.default_rng(c.seed).standard_normal((c.nr, c.nz))
+            chi64 = torch.zeros((c.nr, c.nz), **f64)
+            smooth_Heaviside(chi64, torch.tensor(c.level_set(Z, R), **f64), c.moll_zone)
+            t = dict(
+                omega=torch.tensor(w0, **f64).to(self.dtype),
+                psi=torch.zeros((c.nr, c.nz), **f),
+                u_z=torch.zeros((c.nr, c.nz), **f),
+                u_r=torch.zeros((c.nr, c.nz), **f),
+                chi=chi64.to(self.dtype),
+                w_adv=torch.zeros((c.nr, c.nz), **f),
+                w_tmp=torch.zeros((c.nr, c.nz), **f),
+                r=torch.tensor(r, **f64),
+                z=torch.tensor(z, **f64),
+                rinv2dx=torch.tensor(1.0 / (2 * c.dx * r), **f64),
+                rinv2=torch.tensor(1.0 / (r * r), **f64),
+                gemm_work=torch.zeros(2 * c.nr * c.nz, **f),
+                partials=torch.zeros(((c.nr + 7) // 8) * ((c.nz + 31) // 32) + 8, **f64),
+            )
+            self.fields.append(t)
+            s = self.structs[k]
+            s.nr, s.nz, s.kill_width = c.nr, c.nz, c.kill_width
+            s.dx, s.nu, s.lam, s.U0 = c.dx, c.nu, c.lam, c.U0
+            s.t_ramp = c.t_ramp if c.ramp else 0.0
+            s.cfl, s.U_body = c.cfl, c.U_body
+            s.cd_scale = 2 * 2 * math.pi * c.dx * c.dx * c.lam / (math.pi * c.r_sphere ** 2)
+            s.dt_diff = 0.9 * c.dx ** 2 / 4 / c.nu
+            s.eps = float(np.finfo(float).eps)
+            for name in ("omega", "psi", "u_z", "u_r", "chi", "w_adv", "w_tmp", "r", "z",
+                         "rinv2dx", "rinv2", "gemm_work", "partials"):
+                setattr(s, name, t[name].data_ptr())
+            for name, v in b.t.items():
+                setattr(s, name, v.data_ptr())
+            s.state = self.state[k].data_ptr()
+            if self.history is not None:
+                s.history = self.history[k].data_ptr()
+                s.history_len = history_steps
+            else:
+                s.history = None
+                s.history_len = 0
+        self._bases = bases
+        lib = N.lib()
+        nbytes = ctypes.c_int64(0)
+        ntiles = ctypes.c_int(0)
+        N.check(lib.axi_plan_init(ctypes.addressof(self.structs), n, ctypes.byref(nbytes),
+                                  ctypes.byref(ntiles)), "plan_init")
+        self.n_tiles = ntiles.value
+        self.plan = torch.empty(int(nbytes.value), dtype=torch.uint8, device=self.device)
+        N.check(lib.axi_plan_upload(ctypes.addressof(self.structs), n,
+                                    ctypes.c_void_p(self.plan.data_ptr()),
+                                    ctypes.c_void_p(torch.cuda.current_stream(
+                                        self.device).cuda_stream)), "plan_upload")
+        self._step_fn = getattr(lib, f"axi_rigid_step_{precision}")
+        self.graph = None
+
+    @property
+    def n_cases(self):
+        return len(self.cases)
+
+    def cells(self):
+        return sum(c.nr * c.nz for c in self.cases)
+
+    def step(self, n=1, stream=None):
+        """Advance every case by n steps (asynchronous on torch's current stream)."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        N.check(self._step_fn(ctypes.addressof(self.structs), self.n_cases,
+                              ctypes.c_void_p(self.plan.data_ptr()), self.n_tiles, int(n),
+                              ctypes.c_void_p(s.cuda_stream)), "rigid_step")
+
+    PHASES = ("kill", "transform", "vel_max", "penalise", "adv_diff1", "diff2")
+
+    def phase(self, ph, stream=None):
+        """Run one phase of a step (see PHASES); all six in order = one step."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        fn = getattr(N.lib(), f"axi_rigid_phase_{self.precision}")
+        N.check(fn(ctypes.addressof(self.structs), self.n_cases,
+                   ctypes.c_void_p(self.plan.data_ptr()), self.n_tiles, int(ph),
+                   ctypes.c_void_p(s.cuda_stream)), "rigid_phase")
+
+    def capture(self, steps_per_replay=1):
+        """Capture `steps_per_replay` steps into a CUDA graph (replay with replay())."""
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.step(steps_per_replay, stream=s)
+        torch.cuda.synchronize(self.device)
+        self.graph = g
+        self.graph_steps = steps_per_replay
+        return g
+
+    def replay(self):
+        self.graph.replay()
+
+    def status(self):
+        """Sticky status bits per case (0 = healthy)."""
+        st = self.state[:, ST_STATUS].cpu().numpy().view(np.uint64)
+        return (st & 0xFFFFFFFF).astype(np.int64)
+
+    def vorticity(self, k):
+        return self.fields[k]["omega"]
+
+    def time(self):
+        return self.state[:, ST_T].cpu().numpy()
