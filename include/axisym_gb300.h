@@ -277,24 +277,31 @@ int axi_dgemm_f64(double* C, int ldc, const double* A, int lda, const double* B,
 /* Words of the per-case device state block (doubles). */
 enum {
   AXI_ST_T = 0,        /* simulated time */
-  AXI_ST_DT = 1,       /* last time step */
-  AXI_ST_CD = 2,       /* last drag coefficient */
+  AXI_ST_DT = 1,       /* time step of the current / last step */
+  AXI_ST_CD = 2,       /* drag coefficient of the last step */
   AXI_ST_STEPS = 3,    /* steps taken */
   AXI_ST_UMAX = 4,     /* bits of max(|u_z| + |u_r|) of the current step (uint64) */
-  AXI_ST_COUNT = 5,    /* reduction counter of the current step (uint32 in the low word) */
+  AXI_ST_COUNT = 5,    /* tile counters of the current step (two uint32) */
   AXI_ST_STATUS = 6,   /* sticky axi_status bits (uint32 in the low word) */
-  AXI_ST_FORCE = 7,    /* last body force sum (FP64) */
-  AXI_ST_WORDS = 8
+  AXI_ST_FORCE = 7,    /* last sum of r chi u_z over the grid (FP64) */
+  AXI_ST_UFREE = 8,    /* free stream of the current step, U0 * ramp(t) */
+  AXI_ST_LAMDT = 9,    /* lam * dt */
+  AXI_ST_ADV = 10,     /* -dt / dx (ENO3 flux factor) */
+  AXI_ST_C1 = 11,      /* 0.5 nu dt (RK2 stage 1) */
+  AXI_ST_C2 = 12,      /* nu dt (RK2 stage 2) */
+  AXI_ST_WORDS = 16
 };
 
 /* One flow-past-rigid-body case. Fields are (nr, nz) row-major in the engine
- * precision (double for _f64, float for _f32); r, z, rinv2dx, rinv2 are
- * double vectors of length nr / nz / nr / nr. */
+ * precision (double for _f64, float for _f32); rinv2dx, rinv2 and rw are
+ * per-row vectors (length nr) in the engine precision; r and z are double
+ * vectors of length nr and nz. */
 typedef struct axi_case {
   int32_t nr, nz;
   int32_t kill_width;
   int32_t stencil_tile0; /* first stencil tile of this case in the plan */
   double dx, nu, lam, U0, t_ramp, cfl, U_body, cd_scale, dt_diff, eps;
+  double inv_dx2, inv_2dx;
   void* omega;
   void* psi;
   void* u_z;
@@ -304,8 +311,9 @@ typedef struct axi_case {
   void* w_tmp;   /* scratch: RK2 stage */
   const double* r;
   const double* z;
-  const double* rinv2dx; /* 1 / (2 dx r_i) */
-  const double* rinv2;   /* 1 / r_i^2 */
+  const void* rinv2dx;   /* 1 / (2 dx r_i) */
+  const void* rinv2;     /* 1 / r_i^2 */
+  const void* rw;        /* r_i (drag weight) */
   const void* Er;        /* (nr, nr) */
   const void* Er_inv_w;  /* (nr, nr), E_r^-1 diag(r) */
   const void* EzinvT;    /* (nz, nz) */
@@ -318,24 +326,35 @@ typedef struct axi_case {
   int64_t history_len;
 } axi_case;
 
-/* Host-side planning: validates the cases, assigns each its first tile
- * (cases[k].stencil_tile0) and returns the device bytes the plan needs. */
-int axi_plan_init(axi_case* cases, int n_cases, int64_t* plan_bytes, int* n_tiles);
-/* Copies the case table and the tile table into plan_dev (caller-allocated,
- * plan_bytes); synchronises the stream. */
-int axi_plan_upload(const axi_case* cases, int n_cases, void* plan_dev, void* stream);
-/* Advances every case of the plan by n_steps steps (fields float64 / float32). */
-int axi_rigid_step_f64(const axi_case* cases, int n_cases, const void* plan_dev, int n_tiles,
-                       int n_steps, void* stream);
-int axi_rigid_step_f32(const axi_case* cases, int n_cases, const void* plan_dev, int n_tiles,
-                       int n_steps, void* stream);
-/* One phase of a step (0 kill, 1 transform, 2 velocity max, 3 penalise,
- * 4 advection + diffusion stage 1, 5 diffusion stage 2); running phases 0..5
- * in order equals one axi_rigid_step. Lets a caller time each kernel. */
-int axi_rigid_phase_f64(const axi_case* cases, int n_cases, const void* plan_dev, int n_tiles,
-                        int phase, void* stream);
-int axi_rigid_phase_f32(const axi_case* cases, int n_cases, const void* plan_dev, int n_tiles,
-                        int phase, void* stream);
+/* Launch plan of a set of cases: tile tables in device memory. */
+typedef struct axi_plan_info {
+  int32_t n_cases;
+  int32_t n_stencil_tiles; /* 32 x 8 cell tiles over all cases */
+  int32_t n_gemm_tiles;    /* output tiles of the grouped spectral products */
+  int32_t elem_bytes;      /* 8: float64 fields, 4: float32 fields */
+  int64_t bytes;           /* device bytes the plan needs */
+} axi_plan_info;
+
+/* Host only: validates the cases, assigns each its first tile
+ * (cases[k].stencil_tile0) and fills `info` (sizes of the plan). */
+int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, axi_plan_info* info);
+/* Copies the case table and tile tables into plan_dev (caller-allocated,
+ * info->bytes); synchronises the stream. Re-upload after changing a case. */
+int axi_plan_upload(const axi_case* cases, const axi_plan_info* info, void* plan_dev,
+                    void* stream);
+/* Advances every case of the plan by n_steps steps (float64 / float32 fields). */
+int axi_rigid_step_f64(const axi_plan_info* info, const void* plan_dev, int n_steps,
+                       void* stream);
+int axi_rigid_step_f32(const axi_plan_info* info, const void* plan_dev, int n_steps,
+                       void* stream);
+/* One phase of a step (0 kill, 1 spectral transform, 2 velocity max and dt,
+ * 3 penalisation and drag, 4 advection + diffusion stage 1, 5 diffusion stage
+ * 2); running phases 0..5 in order equals one step. Lets a caller time each
+ * kernel. */
+int axi_rigid_phase_f64(const axi_plan_info* info, const void* plan_dev, int phase,
+                        void* stream);
+int axi_rigid_phase_f32(const axi_plan_info* info, const void* plan_dev, int phase,
+                        void* stream);
 
 #ifdef __cplusplus
 }

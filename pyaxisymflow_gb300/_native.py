@@ -50,12 +50,12 @@ def _signatures():
             I, [P, P, P, P, P, P, P, P, P, D, I, I, P, P, I, P, P, P]),
         "axi_fd_transform_f64": (I, [P, I, P, I, P, P, P, P, P, P, I, I, P]),
         "axi_dgemm_f64": (I, [P, I, P, I, P, I, P, I, I, I, P]),
-        "axi_plan_init": (I, [P, I, _c.POINTER(I64), _c.POINTER(I)]),
-        "axi_plan_upload": (I, [P, I, P, P]),
-        "axi_rigid_step_f64": (I, [P, I, P, I, I, P]),
-        "axi_rigid_step_f32": (I, [P, I, P, I, I, P]),
-        "axi_rigid_phase_f64": (I, [P, I, P, I, I, P]),
-        "axi_rigid_phase_f32": (I, [P, I, P, I, I, P]),
+        "axi_plan_init": (I, [P, I, I, P]),
+        "axi_plan_upload": (I, [P, P, P, P]),
+        "axi_rigid_step_f64": (I, [P, P, I, P]),
+        "axi_rigid_step_f32": (I, [P, P, I, P]),
+        "axi_rigid_phase_f64": (I, [P, P, I, P]),
+        "axi_rigid_phase_f32": (I, [P, P, I, P]),
     }
     for s in ("f64", "f32"):
         T = _real(s)

@@ -8,30 +8,32 @@
 // time live in a per-case state block, so a step needs no host round trip and
 // a run of steps can be captured in a CUDA graph.
 //
-// Launches per step (each covers every case of the plan):
-//   kill_reset   one block per case: sine tapers, state reset
-//   transform    four dense products per case (spectral Poisson solve)
-//   vel_max      per tile: velocity, max(|u_z| + |u_r|) -> atomicMax
+// Launches per step, each covering every case of the plan:
+//   kill_reset   one block per case: sine tapers, free stream of this step,
+//                counters cleared
+//   transform    four grouped dense products (the spectral Poisson solve)
+//   vel_max      per tile: max(|u_z| + |u_r|); the last tile of a case turns
+//                it into dt and the dt-dependent constants of the step
 //   penalise     per tile: velocity + Brinkman + curl(u_pen - u) into omega,
-//                drag partials; the last tile of a case finalises dt/Cd/t
+//                drag partials; the last tile of a case finalises the drag
 //   adv_diff1    per tile: ENO3 advection (axis mirror by index reflection,
 //                halo 3 in shared memory) + RK2 stage 1
-//   diff2        per tile: RK2 stage 2 into omega
-// Arithmetic uses FMA and precomputed reciprocals (1 / (2 dx r), 1 / r^2);
-// parity with the reference is to a relative L2 of 1e-12 after N steps in
-// FP64. Reductions (max, drag) are order-independent or in a fixed order.
+//   diff2        per tile: RK2 stage 2 into omega; advances the time
+//
+// GB300 runs FP64 at 1/70 of its FP32 rate, so the FP32 engine keeps every
+// per-cell operation in FP32: per-row factors (1 / (2 dx r), 1 / r^2, r) are
+// precomputed vectors in the engine precision and the per-step scalars are
+// computed once per case. FP64 remains where the reference needs it: the
+// axis / outer-boundary one-sided rows of u_z (the r = 0 closure), the time
+// step, time and the drag sums across warps and tiles.
 #include "axi_common.cuh"
-#include "gemm_simt.cuh"
 
 namespace {
 
 constexpr int TX = 32;
 constexpr int TY = 8;
 constexpr int NT = TX * TY;
-
-struct TileRec {
-  int c, i0, j0, idx;  // case, first row, first column, tile index within the case
-};
+constexpr double kPi = 3.141592653589793;
 
 template <typename T>
 __device__ __forceinline__ T* F(void* p) {
@@ -42,41 +44,18 @@ __device__ __forceinline__ const T* CF(const void* p) {
   return static_cast<const T*>(p);
 }
 
-__device__ __forceinline__ double ramp_prefac(const axi_case& k, double t) {
-  // examples/FlowPastSphere/flow_past_sphere.py:118-121
-  if (k.t_ramp > 0.0 && t < k.t_ramp) return sin(0.5 * 3.141592653589793 * t / k.t_ramp);
-  return 1.0;
+__device__ __forceinline__ unsigned int* counter(const axi_case& k, int which) {
+  return reinterpret_cast<unsigned int*>(&k.state[AXI_ST_COUNT]) + which;
 }
 
-__device__ __forceinline__ double step_dt(const axi_case& k) {
-  // flow_past_sphere.py:150-153: min(0.9 dx^2 / 4 / nu, CFL dx / (max|u| + eps))
-  const double umax = __longlong_as_double(
-      (long long)*reinterpret_cast<const unsigned long long*>(&k.state[AXI_ST_UMAX]));
-  const double cfl_dt = (k.cfl * k.dx) / (umax + k.eps);
-  return fmin(k.dt_diff, cfl_dt);
-}
-
-// d(psi)/dr * 1 / (2 dx) at (i, j) with one-sided rows at the axis and the
-// outer boundary (kernels/compute_velocity_from_psi.py:10-12), in double.
-template <typename T, typename Acc>
-__device__ __forceinline__ double dpsi_dr(Acc psi, int i, int j, int nr) {
-  if (i == 0) return -(double)psi(2, j) + 4.0 * (double)psi(1, j) - 3.0 * (double)psi(0, j);
-  if (i == nr - 1)
-    return (double)psi(nr - 3, j) - 4.0 * (double)psi(nr - 2, j) + 3.0 * (double)psi(nr - 1, j);
-  return (double)psi(i + 1, j) - (double)psi(i - 1, j);
-}
-
-template <typename T, typename Acc>
-__device__ __forceinline__ double dpsi_dz(Acc psi, int i, int j, int nz) {
-  if (j == 0) return -(double)psi(i, 2) + 4.0 * (double)psi(i, 1) - 3.0 * (double)psi(i, 0);
-  if (j == nz - 1)
-    return (double)psi(i, nz - 3) - 4.0 * (double)psi(i, nz - 2) + 3.0 * (double)psi(i, nz - 1);
-  return (double)psi(i, j + 1) - (double)psi(i, j - 1);
+inline int tiles_of(const axi_case& k) { return ((k.nr + TY - 1) / TY) * ((k.nz + TX - 1) / TX); }
+__device__ __forceinline__ unsigned int dev_tiles_of(const axi_case& k) {
+  return (unsigned int)(((k.nr + TY - 1) / TY) * ((k.nz + TX - 1) / TX));
 }
 
 // ---------------------------------------------------------------------------
 // kill_reset: kernels/kill_boundary_vorticity_sine.py:4-27 (literal 1 - Z,
-// 1 - R), then clear the per-step reduction words.
+// 1 - R), the ramped free stream (flow_past_sphere.py:118-121), counters.
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void kill_reset_kernel(const axi_case* __restrict__ cases) {
@@ -84,20 +63,24 @@ __global__ void kill_reset_kernel(const axi_case* __restrict__ cases) {
   T* w = F<T>(k.omega);
   const int nr = k.nr, nz = k.nz, wd = k.kill_width;
   const double dx = k.dx, half_dx = 0.5 * k.dx;
-  const double pi = 3.141592653589793;
   if (threadIdx.x == 0) {
     *reinterpret_cast<unsigned long long*>(&k.state[AXI_ST_UMAX]) = 0ull;
-    *reinterpret_cast<unsigned int*>(&k.state[AXI_ST_COUNT]) = 0u;
+    counter(k, 0)[0] = 0u;
+    counter(k, 1)[0] = 0u;
+    const double t = k.state[AXI_ST_T];
+    double prefac = 1.0;
+    if (k.t_ramp > 0.0 && t < k.t_ramp) prefac = sin(0.5 * kPi * t / k.t_ramp);
+    k.state[AXI_ST_UFREE] = k.U0 * prefac;
   }
   for (int i = threadIdx.x; i < nr; i += blockDim.x) {
     T* row = w + (long long)i * nz;
     const double left = (double)row[wd - 1];
     double nl[8];
-    for (int q = 0; q < wd; ++q) nl[q] = sin(pi * (k.z[q] - half_dx) / 2 / (wd - 1) / dx) * left;
+    for (int q = 0; q < wd; ++q) nl[q] = sin(kPi * (k.z[q] - half_dx) / 2 / (wd - 1) / dx) * left;
     for (int q = 0; q < wd; ++q) row[q] = (T)nl[q];
     const double right = (double)row[nz - wd];
     for (int q = 0; q < wd; ++q)
-      nl[q] = sin(pi * (1 - k.z[nz - wd + q] - half_dx) / 2 / (wd - 1) / dx) * right;
+      nl[q] = sin(kPi * (1 - k.z[nz - wd + q] - half_dx) / 2 / (wd - 1) / dx) * right;
     for (int q = 0; q < wd; ++q) row[nz - wd + q] = (T)nl[q];
   }
   __syncthreads();
@@ -105,66 +88,111 @@ __global__ void kill_reset_kernel(const axi_case* __restrict__ cases) {
     const double src = (double)w[(long long)(nr - wd) * nz + j];
     for (int q = 0; q < wd; ++q) {
       const int i = nr - wd + q;
-      w[(long long)i * nz + j] = (T)(sin(pi * (1 - k.r[i] - half_dx) / 2 / (wd - 1) / dx) * src);
+      w[(long long)i * nz + j] = (T)(sin(kPi * (1 - k.r[i] - half_dx) / 2 / (wd - 1) / dx) * src);
     }
     w[j] = T(0);
   }
 }
 
 // ---------------------------------------------------------------------------
-// vel_max: max over the case of |u_z| + |u_r| (flow_past_sphere.py:152)
+// velocity from psi (kernels/compute_velocity_from_psi.py:9-17) plus the free
+// stream. psi(a, b) is an accessor; interior cells run in T, the one-sided
+// rows / columns at the grid edges in double.
+// ---------------------------------------------------------------------------
+template <typename T, typename Acc>
+__device__ __forceinline__ void velocity_at(const axi_case& k, Acc psi, int i, int j, T rinv,
+                                            T ufree, T& uz, T& ur) {
+  const int nr = k.nr, nz = k.nz;
+  if (i == 0 || i == nr - 1) {
+    double d;
+    if (i == 0)
+      d = -(double)psi(2, j) + 4.0 * (double)psi(1, j) - 3.0 * (double)psi(0, j);
+    else
+      d = (double)psi(nr - 3, j) - 4.0 * (double)psi(nr - 2, j) + 3.0 * (double)psi(nr - 1, j);
+    uz = (T)(d * (0.5 / k.dx) / k.r[i]) + ufree;
+  } else {
+    uz = (psi(i + 1, j) - psi(i - 1, j)) * rinv + ufree;
+  }
+  if (j == 0 || j == nz - 1) {
+    double d;
+    if (j == 0)
+      d = -(double)psi(i, 2) + 4.0 * (double)psi(i, 1) - 3.0 * (double)psi(i, 0);
+    else
+      d = (double)psi(i, nz - 3) - 4.0 * (double)psi(i, nz - 2) + 3.0 * (double)psi(i, nz - 1);
+    ur = (T)(-d) * rinv;
+  } else {
+    ur = -(psi(i, j + 1) - psi(i, j - 1)) * rinv;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// vel_max: max over the case of |u_z| + |u_r| (flow_past_sphere.py:150-153);
+// the last tile of the case derives dt and the per-step constants.
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict__ cases,
                                                      const int4* __restrict__ tiles) {
+  __shared__ unsigned long long wm[NT / 32];
+  __shared__ bool last;
   const int4 tr = tiles[blockIdx.x];
   const axi_case& k = cases[tr.x];
   const int i = tr.y + threadIdx.x / TX;
   const int j = tr.z + threadIdx.x % TX;
   const int nr = k.nr, nz = k.nz;
   const T* psi = CF<T>(k.psi);
-  double v = 0.0;
+  const T ufree = (T)k.state[AXI_ST_UFREE];
+  T v = T(0);
   if (i < nr && j < nz) {
     auto acc = [&](int a, int b) { return psi[(long long)a * nz + b]; };
-    const double prefac = ramp_prefac(k, k.state[AXI_ST_T]);
-    const double uz = (double)(T)(dpsi_dr<T>(acc, i, j, nr) * k.rinv2dx[i]) + k.U0 * prefac;
-    const double ur = (double)(T)(-dpsi_dz<T>(acc, i, j, nz) * k.rinv2dx[i]);
-    v = fabs((double)(T)uz) + fabs(ur);
+    T uz, ur;
+    velocity_at<T>(k, acc, i, j, CF<T>(k.rinv2dx)[i], ufree, uz, ur);
+    v = fabs(uz) + fabs(ur);
   }
-  // block max (NaN propagates: its bit pattern compares above +inf)
-  unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  // Non-negative values order like their bit patterns (a NaN sorts above
+  // +inf, so it propagates to the maximum).
+  unsigned long long bits = sizeof(T) == 8
+                                ? (unsigned long long)__double_as_longlong((double)v)
+                                : (unsigned long long)__float_as_uint((float)v);
   for (int o = 16; o > 0; o >>= 1) {
-    unsigned long long other = __shfl_down_sync(0xffffffffu, bits, o);
+    const unsigned long long other = __shfl_down_sync(0xffffffffu, bits, o);
     bits = other > bits ? other : bits;
   }
-  __shared__ unsigned long long wmax[NT / 32];
-  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = bits;
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = bits;
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long m = 0;
-    for (int q = 0; q < NT / 32; ++q) m = wmax[q] > m ? wmax[q] : m;
+    for (int q = 0; q < NT / 32; ++q) m = wm[q] > m ? wm[q] : m;
     atomicMax(reinterpret_cast<unsigned long long*>(&k.state[AXI_ST_UMAX]), m);
+    __threadfence();
+    last = (atomicAdd(counter(k, 0), 1u) == dev_tiles_of(k) - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    const unsigned long long mb =
+        atomicAdd(reinterpret_cast<unsigned long long*>(&k.state[AXI_ST_UMAX]), 0ull);
+    const double umax = sizeof(T) == 8 ? __longlong_as_double((long long)mb)
+                                       : (double)__uint_as_float((unsigned int)mb);
+    if (!(umax <= 1.7976931348623157e308))
+      atomicOr(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_STATUS]), 1u << AXI_ERR_NONFINITE);
+    const double dt = fmin(k.dt_diff, (k.cfl * k.dx) / (umax + k.eps));
+    k.state[AXI_ST_DT] = dt;
+    k.state[AXI_ST_LAMDT] = k.lam * dt;
+    k.state[AXI_ST_ADV] = -dt / k.dx;
+    k.state[AXI_ST_C1] = 0.5 * k.nu * dt;
+    k.state[AXI_ST_C2] = k.nu * dt;
   }
 }
 
 // ---------------------------------------------------------------------------
-// penalise: flow_past_sphere.py:156-175 (Brinkman, penalisation vorticity, drag)
+// penalise: flow_past_sphere.py:156-175 (kernels/brinkmann_penalize.py:11-16,
+// kernels/compute_vorticity_from_velocity.py:11-13 on u_pen - u, drag)
 // ---------------------------------------------------------------------------
-// Penalised velocity at (gi, gj): u from psi (plus the ramped free stream),
-// then (u + lam dt chi U_body) / (1 + lam dt chi) (kernels/brinkmann_penalize.py:11-16).
-template <typename T, typename Acc>
-__device__ __forceinline__ void penalised_velocity(const axi_case& k, Acc psi, int gi, int gj,
-                                                   double prefac, double lamdt, T chi, T& uz,
-                                                   T& ur, T& pz, T& pr) {
-  const double drv = dpsi_dr<T>(psi, gi, gj, k.nr);
-  const double dzv = dpsi_dz<T>(psi, gi, gj, k.nz);
-  const double rinv = k.rinv2dx[gi];
-  uz = (T)((double)(T)(drv * rinv) + k.U0 * prefac);
-  ur = (T)(-dzv * rinv);
-  const double lc = lamdt * (double)chi;
-  const double inv = 1.0 / (1.0 + lc);
-  pz = (T)(((double)uz + lc * k.U_body) * inv);
-  pr = (T)((double)ur * inv);
+template <typename T>
+__device__ __forceinline__ void penalise_point(T uz, T ur, T lc, T ubody, T& pz, T& pr) {
+  const T inv = T(1) / (T(1) + lc);
+  pz = (uz + lc * ubody) * inv;
+  pr = ur * inv;
 }
 
 template <typename T>
@@ -181,26 +209,27 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
   const int i0 = tr.y, j0 = tr.z;
   const T* psi = CF<T>(k.psi);
   const T* chi = CF<T>(k.chi);
-  const double dt = step_dt(k);
-  const double prefac = ramp_prefac(k, k.state[AXI_ST_T]);
-  const double lamdt = k.lam * dt;
-  // psi tile with halo 2 (every one-sided boundary stencil stays inside it)
+  const T* rinv2dx = CF<T>(k.rinv2dx);
+  const T ufree = (T)k.state[AXI_ST_UFREE];
+  const T lamdt = (T)k.state[AXI_ST_LAMDT];
+  const T ubody = (T)k.U_body;
+  const T inv2dx = (T)k.inv_2dx;
   for (int e = threadIdx.x; e < (TY + 4) * (TX + 4); e += NT) {
     const int a = e / (TX + 4), b = e % (TX + 4);
     const int gi = i0 - 2 + a, gj = j0 - 2 + b;
     ps[a][b] = (gi >= 0 && gi < nr && gj >= 0 && gj < nz) ? psi[(long long)gi * nz + gj] : T(0);
   }
   __syncthreads();
+  // every one-sided stencil of an edge cell stays inside the halo-2 tile
   auto sp = [&](int gi, int gj) { return ps[gi - i0 + 2][gj - j0 + 2]; };
-  // u_pen - u on the tile and a one-cell halo
   for (int e = threadIdx.x; e < (TY + 2) * (TX + 2); e += NT) {
     const int a = e / (TX + 2), b = e % (TX + 2);
     const int gi = i0 - 1 + a, gj = j0 - 1 + b;
     T dz = T(0), dr = T(0);
     if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
       T uz, ur, pz, pr;
-      penalised_velocity<T>(k, sp, gi, gj, prefac, lamdt, chi[(long long)gi * nz + gj], uz, ur,
-                            pz, pr);
+      velocity_at<T>(k, sp, gi, gj, rinv2dx[gi], ufree, uz, ur);
+      penalise_point<T>(uz, ur, lamdt * chi[(long long)gi * nz + gj], ubody, pz, pr);
       dz = pz - uz;
       dr = pr - ur;
     }
@@ -208,7 +237,7 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
     dur[a][b] = dr;
   }
   __syncthreads();
-  double cd_part = 0.0;
+  T cd_part = T(0);
   {
     const int a = threadIdx.x / TX, b = threadIdx.x % TX;
     const int gi = i0 + a, gj = j0 + b;
@@ -216,14 +245,12 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
       const long long c = (long long)gi * nz + gj;
       const T ch = chi[c];
       T uz, ur, pz, pr;
-      penalised_velocity<T>(k, sp, gi, gj, prefac, lamdt, ch, uz, ur, pz, pr);
+      velocity_at<T>(k, sp, gi, gj, rinv2dx[gi], ufree, uz, ur);
+      penalise_point<T>(uz, ur, lamdt * ch, ubody, pz, pr);
       F<T>(k.u_z)[c] = pz;
       F<T>(k.u_r)[c] = pr;
-      // drag integrand R chi u_z (flow_past_sphere.py:173), FP64
-      cd_part = k.r[gi] * (double)ch * (double)pz;
+      cd_part = CF<T>(k.rw)[gi] * ch * pz;  // drag integrand r chi u_z
       if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
-        // compute_vorticity_from_velocity.py:11-13 on u_pen - u
-        const T inv2dx = (T)(0.5 / k.dx);
         const T pw = (dur[a + 1][b + 2] - dur[a + 1][b]) * inv2dx -
                      (duz[a + 2][b + 1] - duz[a][b + 1]) * inv2dx;
         T* w = F<T>(k.omega);
@@ -231,39 +258,34 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
       }
     }
   }
-  // drag: tile sum in a fixed order (warp shuffles, then warps in order)
-  double x = cd_part;
+  // drag: warp sums in T, then warps and tiles in double, fixed order
+  T x = cd_part;
   for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)x;
   __syncthreads();
-  const unsigned int ntiles = (unsigned int)(((nr + TY - 1) / TY) * ((nz + TX - 1) / TX));
+  const unsigned int ntiles = dev_tiles_of(k);
   if (threadIdx.x == 0) {
     double sum = 0.0;
     for (int q = 0; q < NT / 32; ++q) sum += red[q];
     k.partials[tr.w] = sum;
     __threadfence();
-    const unsigned int done =
-        atomicAdd(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_COUNT]), 1u);
-    last = (done == ntiles - 1);
+    last = (atomicAdd(counter(k, 1), 1u) == ntiles - 1);
   }
   __syncthreads();
   if (last && threadIdx.x == 0) {
-    // last tile of the case: case totals in tile order, then dt / Cd
     __threadfence();
     double sum = 0.0;
     for (unsigned int q = 0; q < ntiles; ++q) sum += ((volatile double*)k.partials)[q];
     const double cd = k.cd_scale * sum;
-    const double umax = __longlong_as_double(
-        (long long)*reinterpret_cast<const unsigned long long*>(&k.state[AXI_ST_UMAX]));
-    if (!(umax <= 1.7976931348623157e308) || !(cd == cd))
+    if (!(cd == cd) || !(fabs(cd) <= 1.7976931348623157e308))
       atomicOr(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_STATUS]), 1u << AXI_ERR_NONFINITE);
+    const double dt = k.state[AXI_ST_DT];
     const long long step = (long long)k.state[AXI_ST_STEPS];
     if (k.history && step < k.history_len) {
       k.history[2 * step] = dt;
       k.history[2 * step + 1] = cd;
     }
     k.state[AXI_ST_CD] = cd;
-    k.state[AXI_ST_DT] = dt;
     k.state[AXI_ST_FORCE] = sum;
   }
 }
@@ -295,8 +317,9 @@ __global__ void __launch_bounds__(NT) adv_diff1_kernel(const axi_case* __restric
   const T* w = CF<T>(k.omega);
   const T* uz = CF<T>(k.u_z);
   const T* ur = CF<T>(k.u_r);
-  const double dt = k.state[AXI_ST_DT];
-  const T a = (T)(-dt / k.dx);
+  const T a = (T)k.state[AXI_ST_ADV];
+  const T c1 = (T)k.state[AXI_ST_C1];
+  const T inv_dx2 = (T)k.inv_dx2;
   for (int e = threadIdx.x; e < (TY + 2 * H) * (TX + 2 * H); e += NT) {
     const int p = e / (TX + 2 * H), q = e % (TX + 2 * H);
     const int gi = i0 - H + p, gj = j0 - H + q;
@@ -325,9 +348,11 @@ __global__ void __launch_bounds__(NT) adv_diff1_kernel(const axi_case* __restric
     const int gi = i0 - 1 + p, gj = j0 - 1 + q;
     T val = T(0);
     if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
-      const int P = p + H - 1, Q = q + H - 1;  // position in the halo-3 tiles
+      const int P = p + H - 1, Q = q + H - 1;
       const T f0 = sw[P][Q];
       T flux = T(0);
+      // pystencils ghost layers: no flux in the last two rows and the first
+      // and last two columns
       if (gi < nr - 2 && gj >= 2 && gj < nz - 2) {
         const T xf = face_flux(sw[P][Q - 1], f0, sw[P][Q + 1], sw[P][Q + 2], sz[P][Q - 1],
                                sz[P][Q], sz[P][Q + 1], sz[P][Q + 2]);
@@ -354,10 +379,9 @@ __global__ void __launch_bounds__(NT) adv_diff1_kernel(const axi_case* __restric
     T tmp = c0;
     if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
       const T n = wa[p + 2][q + 1], s = wa[p][q + 1], e = wa[p + 1][q + 2], ww = wa[p + 1][q];
-      const T inv_dx2 = (T)(1.0 / (k.dx * k.dx));
-      const T lap = (n + s + e + ww - T(4) * c0) * inv_dx2 + (n - s) * (T)k.rinv2dx[gi] -
-                    c0 * (T)k.rinv2[gi];
-      tmp = c0 + (T)(0.5 * k.nu * dt) * lap;
+      const T lap = (n + s + e + ww - T(4) * c0) * inv_dx2 + (n - s) * CF<T>(k.rinv2dx)[gi] -
+                    c0 * CF<T>(k.rinv2)[gi];
+      tmp = c0 + c1 * lap;
     }
     const long long c = (long long)gi * nz + gj;
     F<T>(k.w_adv)[c] = c0;
@@ -375,7 +399,6 @@ __global__ void __launch_bounds__(NT) diff2_kernel(const axi_case* __restrict__ 
   const axi_case& k = cases[tr.x];
   const int nr = k.nr, nz = k.nz;
   const int gi = tr.y + threadIdx.x / TX, gj = tr.z + threadIdx.x % TX;
-  const double dt = k.state[AXI_ST_DT];
   if (gi < nr && gj < nz) {
     const long long c = (long long)gi * nz + gj;
     const T* wa = CF<T>(k.w_adv);
@@ -383,75 +406,172 @@ __global__ void __launch_bounds__(NT) diff2_kernel(const axi_case* __restrict__ 
     T v = wa[c];
     if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
       const T c0 = tm[c], n = tm[c + nz], s = tm[c - nz], e = tm[c + 1], ww = tm[c - 1];
-      const T inv_dx2 = (T)(1.0 / (k.dx * k.dx));
-      const T lap = (n + s + e + ww - T(4) * c0) * inv_dx2 + (n - s) * (T)k.rinv2dx[gi] -
-                    c0 * (T)k.rinv2[gi];
-      v = v + (T)(k.nu * dt) * lap;
+      const T lap = (n + s + e + ww - T(4) * c0) * (T)k.inv_dx2 +
+                    (n - s) * CF<T>(k.rinv2dx)[gi] - c0 * CF<T>(k.rinv2)[gi];
+      v = v + (T)k.state[AXI_ST_C2] * lap;
     }
     F<T>(k.omega)[c] = v;
   }
   if (tr.w == 0 && threadIdx.x == 0) {
-    k.state[AXI_ST_T] += dt;
+    k.state[AXI_ST_T] += k.state[AXI_ST_DT];
     k.state[AXI_ST_STEPS] += 1.0;
   }
 }
 
-inline int tiles_of(const axi_case& k) { return ((k.nr + TY - 1) / TY) * ((k.nz + TX - 1) / TX); }
+// ---------------------------------------------------------------------------
+// Grouped SIMT GEMM over all cases: the four products of the spectral solve
+// (kernels/FastDiagonalisationStokesSolver.py:137-156, association A (B C)):
+//   stage 0  w1  = omega * EzinvT              (K = nz)
+//   stage 1  w2  = (Er_inv_w * w1) .* inv_eig  (K = nr)
+//   stage 2  w1  = w2 * EzT                    (K = nz)
+//   stage 3  psi = Er * w1                     (K = nr)
+// Every stage writes an (nr, nz) result, so one tile table serves all four.
+// The FP64 configuration uses small register tiles so that even a single
+// 256 x 512 case puts several warps on every SM sub-partition (the FP64 pipe,
+// not latency, is the limit).
+// ---------------------------------------------------------------------------
+template <typename T> struct GemmCfg;
+template <> struct GemmCfg<double> {
+  static constexpr int BM = 32, BN = 32, BK = 32, RM = 2, RN = 2;
+};
+template <> struct GemmCfg<float> {
+  static constexpr int BM = 64, BN = 64, BK = 16, RM = 4, RN = 4;
+};
 
-// Phases of one step, in launch order.
+template <typename T>
+constexpr int gemm_threads() {
+  return (GemmCfg<T>::BM / GemmCfg<T>::RM) * (GemmCfg<T>::BN / GemmCfg<T>::RN);
+}
+
+template <typename T, int STAGE>
+__global__ void __launch_bounds__(gemm_threads<T>())
+    grouped_gemm_kernel(const axi_case* __restrict__ cases, const int4* __restrict__ tiles) {
+  using C = GemmCfg<T>;
+  constexpr int BM = C::BM, BN = C::BN, BK = C::BK, RM = C::RM, RN = C::RN;
+  constexpr int TXG = BN / RN, NTH = gemm_threads<T>();
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Bs[BK][BN];
+  const int4 tr = tiles[blockIdx.x];
+  const axi_case& k = cases[tr.x];
+  const int M = k.nr, N = k.nz;
+  const T* A;
+  const T* B;
+  const T* S = nullptr;
+  T* Cm;
+  int K, lda;
+  T* w1 = F<T>(k.gemm_work);
+  T* w2 = w1 + (size_t)M * N;
+  if (STAGE == 0) {
+    A = CF<T>(k.omega); lda = N; B = CF<T>(k.EzinvT); K = N; Cm = w1;
+  } else if (STAGE == 1) {
+    A = CF<T>(k.Er_inv_w); lda = M; B = w1; K = M; Cm = w2; S = CF<T>(k.inv_eig);
+  } else if (STAGE == 2) {
+    A = w2; lda = N; B = CF<T>(k.EzT); K = N; Cm = w1;
+  } else {
+    A = CF<T>(k.Er); lda = M; B = w1; K = M; Cm = F<T>(k.psi);
+  }
+  const int ldb = N;
+  const int tx = threadIdx.x % TXG, ty = threadIdx.x / TXG;
+  const int m0 = tr.y, n0 = tr.z;
+  T acc[RM][RN];
+#pragma unroll
+  for (int p = 0; p < RM; ++p)
+#pragma unroll
+    for (int q = 0; q < RN; ++q) acc[p][q] = T(0);
+  for (int k0 = 0; k0 < K; k0 += BK) {
+    for (int e = threadIdx.x; e < BM * BK; e += NTH) {
+      const int r = e / BK, kk = e % BK;
+      const int gm = m0 + r, gk = k0 + kk;
+      As[kk][r] = (gm < M && gk < K) ? A[(long long)gm * lda + gk] : T(0);
+    }
+    for (int e = threadIdx.x; e < BK * BN; e += NTH) {
+      const int kk = e / BN, cc = e % BN;
+      const int gk = k0 + kk, gn = n0 + cc;
+      Bs[kk][cc] = (gk < K && gn < N) ? B[(long long)gk * ldb + gn] : T(0);
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < BK; ++kk) {
+      T av[RM], bv[RN];
+#pragma unroll
+      for (int p = 0; p < RM; ++p) av[p] = As[kk][ty * RM + p];
+#pragma unroll
+      for (int q = 0; q < RN; ++q) bv[q] = Bs[kk][tx + q * TXG];
+#pragma unroll
+      for (int p = 0; p < RM; ++p)
+#pragma unroll
+        for (int q = 0; q < RN; ++q) acc[p][q] = fma(av[p], bv[q], acc[p][q]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < RM; ++p) {
+    const int gm = m0 + ty * RM + p;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int q = 0; q < RN; ++q) {
+      const int gn = n0 + tx + q * TXG;
+      if (gn >= N) continue;
+      const long long c = (long long)gm * N + gn;
+      T v = acc[p][q];
+      if (S) v *= S[c];
+      Cm[c] = v;
+    }
+  }
+}
+
+// Plan layout in device memory: [axi_case x n][stencil tiles][gemm tiles].
+struct PlanView {
+  const axi_case* cases;
+  const int4* stencil;
+  const int4* gemm;
+};
+
+inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+inline PlanView plan_view(const void* plan_dev, const axi_plan_info* info) {
+  const char* base = static_cast<const char*>(plan_dev);
+  PlanView v;
+  v.cases = reinterpret_cast<const axi_case*>(base);
+  const size_t off1 = align16(info->n_cases * sizeof(axi_case));
+  v.stencil = reinterpret_cast<const int4*>(base + off1);
+  v.gemm = reinterpret_cast<const int4*>(base + off1 + info->n_stencil_tiles * sizeof(int4));
+  return v;
+}
+
 enum { PH_KILL = 0, PH_TRANSFORM = 1, PH_VEL_MAX = 2, PH_PENALISE = 3, PH_ADV_DIFF1 = 4,
        PH_DIFF2 = 5, PH_COUNT = 6 };
 
 template <typename T>
-int run_phase(int phase, const axi_case* hcases, int n_cases, const axi_case* dcases,
-              const int4* tiles, int n_tiles, cudaStream_t s) {
+int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStream_t s) {
+  const int nt = info->n_stencil_tiles, ng = info->n_gemm_tiles;
   switch (phase) {
     case PH_KILL:
-      kill_reset_kernel<T><<<n_cases, 256, 0, s>>>(dcases);
+      kill_reset_kernel<T><<<info->n_cases, 256, 0, s>>>(v.cases);
       break;
     case PH_TRANSFORM:
-      for (int c = 0; c < n_cases; ++c) {
-        const axi_case& k = hcases[c];
-        AXI_TRY(axi_gemm::fd_transform<T>(
-            static_cast<T*>(k.psi), k.nz, static_cast<const T*>(k.omega), k.nz,
-            static_cast<const T*>(k.Er_inv_w), static_cast<const T*>(k.EzinvT),
-            static_cast<const T*>(k.inv_eig), static_cast<const T*>(k.Er),
-            static_cast<const T*>(k.EzT), static_cast<T*>(k.gemm_work), k.nr, k.nz, s));
-      }
+      grouped_gemm_kernel<T, 0><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
+      grouped_gemm_kernel<T, 1><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
+      grouped_gemm_kernel<T, 2><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
+      grouped_gemm_kernel<T, 3><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
       break;
     case PH_VEL_MAX:
-      vel_max_kernel<T><<<n_tiles, NT, 0, s>>>(dcases, tiles);
+      vel_max_kernel<T><<<nt, NT, 0, s>>>(v.cases, v.stencil);
       break;
     case PH_PENALISE:
-      penalise_kernel<T><<<n_tiles, NT, 0, s>>>(dcases, tiles);
+      penalise_kernel<T><<<nt, NT, 0, s>>>(v.cases, v.stencil);
       break;
     case PH_ADV_DIFF1:
-      adv_diff1_kernel<T><<<n_tiles, NT, 0, s>>>(dcases, tiles);
+      adv_diff1_kernel<T><<<nt, NT, 0, s>>>(v.cases, v.stencil);
       break;
     case PH_DIFF2:
-      diff2_kernel<T><<<n_tiles, NT, 0, s>>>(dcases, tiles);
+      diff2_kernel<T><<<nt, NT, 0, s>>>(v.cases, v.stencil);
       break;
     default:
       axi::set_error("rigid_phase: unknown phase %d", phase);
       return AXI_ERR_INVALID;
   }
   return axi::launch_status("rigid_phase");
-}
-
-inline const int4* tile_table(const void* plan_dev, int n_cases) {
-  return reinterpret_cast<const int4*>(static_cast<const char*>(plan_dev) +
-                                       ((n_cases * sizeof(axi_case) + 15) & ~size_t(15)));
-}
-
-template <typename T>
-int rigid_step(const axi_case* hcases, int n_cases, const void* plan_dev, int n_tiles,
-               int n_steps, cudaStream_t s, const char* what) {
-  const axi_case* dcases = static_cast<const axi_case*>(plan_dev);
-  const int4* tiles = tile_table(plan_dev, n_cases);
-  for (int step = 0; step < n_steps; ++step)
-    for (int ph = 0; ph < PH_COUNT; ++ph)
-      AXI_TRY(run_phase<T>(ph, hcases, n_cases, dcases, tiles, n_tiles, s));
-  return axi::launch_status(what);
 }
 
 int validate(const axi_case* cases, int n_cases, const char* what) {
@@ -468,8 +588,8 @@ int validate(const axi_case* cases, int n_cases, const char* what) {
       return AXI_ERR_INVALID;
     }
     const void* ptrs[] = {k.omega, k.psi, k.u_z, k.u_r, k.chi, k.w_adv, k.w_tmp, k.r, k.z,
-                          k.rinv2dx, k.rinv2, k.Er, k.Er_inv_w, k.EzinvT, k.EzT, k.inv_eig,
-                          k.gemm_work, k.state, k.partials};
+                          k.rinv2dx, k.rinv2, k.rw, k.Er, k.Er_inv_w, k.EzinvT, k.EzT,
+                          k.inv_eig, k.gemm_work, k.state, k.partials};
     for (const void* p : ptrs) {
       if (!p) {
         axi::set_error("%s: case %d has a null pointer", what, c);
@@ -480,37 +600,99 @@ int validate(const axi_case* cases, int n_cases, const char* what) {
   return AXI_OK;
 }
 
-}  // namespace
-
-extern "C" int axi_plan_init(axi_case* cases, int n_cases, int64_t* plan_bytes, int* n_tiles) {
-  axi::clear_error();
-  AXI_TRY(validate(cases, n_cases, "plan_init"));
-  int total = 0;
-  for (int c = 0; c < n_cases; ++c) {
-    cases[c].stencil_tile0 = total;
-    total += tiles_of(cases[c]);
+int gemm_tile_dims(int elem_bytes, int* bm, int* bn) {
+  if (elem_bytes == 8) {
+    *bm = GemmCfg<double>::BM;
+    *bn = GemmCfg<double>::BN;
+  } else if (elem_bytes == 4) {
+    *bm = GemmCfg<float>::BM;
+    *bn = GemmCfg<float>::BN;
+  } else {
+    axi::set_error("plan_init: element size must be 4 or 8 (got %d)", elem_bytes);
+    return AXI_ERR_INVALID;
   }
-  *n_tiles = total;
-  *plan_bytes = (int64_t)(((n_cases * sizeof(axi_case) + 15) & ~size_t(15)) + total * sizeof(int4));
   return AXI_OK;
 }
 
-extern "C" int axi_plan_upload(const axi_case* cases, int n_cases, void* plan_dev, void* stream) {
+template <typename T>
+int check_info(const axi_plan_info* info, const char* what) {
+  if (!info || info->elem_bytes != (int)sizeof(T) || info->n_cases <= 0) {
+    axi::set_error("%s: plan was built for %d-byte fields", what, info ? info->elem_bytes : 0);
+    return AXI_ERR_INVALID;
+  }
+  return AXI_OK;
+}
+
+template <typename T>
+int rigid_step(const axi_plan_info* info, const void* plan_dev, int n_steps, cudaStream_t s,
+               const char* what) {
+  AXI_TRY(check_info<T>(info, what));
+  const PlanView v = plan_view(plan_dev, info);
+  for (int step = 0; step < n_steps; ++step)
+    for (int ph = 0; ph < PH_COUNT; ++ph) AXI_TRY(run_phase<T>(ph, info, v, s));
+  return axi::launch_status(what);
+}
+
+template <typename T>
+int rigid_phase(const axi_plan_info* info, const void* plan_dev, int phase, cudaStream_t s) {
+  AXI_TRY(check_info<T>(info, "rigid_phase"));
+  return run_phase<T>(phase, info, plan_view(plan_dev, info), s);
+}
+
+}  // namespace
+
+extern "C" int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, axi_plan_info* info) {
   axi::clear_error();
-  AXI_TRY(validate(cases, n_cases, "plan_upload"));
+  AXI_TRY(validate(cases, n_cases, "plan_init"));
+  AXI_TRY(axi::check_ptr("plan_init", info, "info"));
+  int bm, bn;
+  AXI_TRY(gemm_tile_dims(elem_bytes, &bm, &bn));
+  int nt = 0, ng = 0;
+  for (int c = 0; c < n_cases; ++c) {
+    cases[c].stencil_tile0 = nt;
+    nt += tiles_of(cases[c]);
+    ng += ((cases[c].nr + bm - 1) / bm) * ((cases[c].nz + bn - 1) / bn);
+  }
+  info->n_cases = n_cases;
+  info->n_stencil_tiles = nt;
+  info->n_gemm_tiles = ng;
+  info->elem_bytes = elem_bytes;
+  info->bytes = (int64_t)(align16(n_cases * sizeof(axi_case)) + (size_t)(nt + ng) * sizeof(int4));
+  return AXI_OK;
+}
+
+extern "C" int axi_plan_upload(const axi_case* cases, const axi_plan_info* info, void* plan_dev,
+                               void* stream) {
+  axi::clear_error();
+  AXI_TRY(axi::check_ptr("plan_upload", info, "info"));
+  AXI_TRY(validate(cases, info->n_cases, "plan_upload"));
   AXI_TRY(axi::check_ptr("plan_upload", plan_dev, "plan_dev"));
-  int total = 0;
-  for (int c = 0; c < n_cases; ++c) total += tiles_of(cases[c]);
-  const size_t head = (n_cases * sizeof(axi_case) + 15) & ~size_t(15);
-  std::string buf(head + total * sizeof(int4), '\0');
-  memcpy(&buf[0], cases, n_cases * sizeof(axi_case));
+  int bm, bn;
+  AXI_TRY(gemm_tile_dims(info->elem_bytes, &bm, &bn));
+  const int n = info->n_cases;
+  const size_t head = align16(n * sizeof(axi_case));
+  std::string buf((size_t)info->bytes, '\0');
+  memcpy(&buf[0], cases, n * sizeof(axi_case));
   int4* t = reinterpret_cast<int4*>(&buf[head]);
   int q = 0;
-  for (int c = 0; c < n_cases; ++c) {
+  for (int c = 0; c < n; ++c) {
     const axi_case& k = cases[c];
     int idx = 0;
     for (int i0 = 0; i0 < k.nr; i0 += TY)
       for (int j0 = 0; j0 < k.nz; j0 += TX) t[q++] = make_int4(c, i0, j0, idx++);
+  }
+  if (q != info->n_stencil_tiles) {
+    axi::set_error("plan_upload: cases changed since plan_init");
+    return AXI_ERR_INVALID;
+  }
+  for (int c = 0; c < n; ++c) {
+    const axi_case& k = cases[c];
+    for (int m0 = 0; m0 < k.nr; m0 += bm)
+      for (int n0 = 0; n0 < k.nz; n0 += bn) t[q++] = make_int4(c, m0, n0, 0);
+  }
+  if (q != info->n_stencil_tiles + info->n_gemm_tiles) {
+    axi::set_error("plan_upload: cases changed since plan_init");
+    return AXI_ERR_INVALID;
   }
   cudaStream_t s = axi::as_stream(stream);
   if (cudaMemcpyAsync(plan_dev, buf.data(), buf.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
@@ -519,34 +701,30 @@ extern "C" int axi_plan_upload(const axi_case* cases, int n_cases, void* plan_de
   return AXI_OK;
 }
 
-extern "C" int axi_rigid_step_f64(const axi_case* cases, int n_cases, const void* plan_dev,
-                                  int n_tiles, int n_steps, void* stream) {
+extern "C" int axi_rigid_step_f64(const axi_plan_info* info, const void* plan_dev, int n_steps,
+                                  void* stream) {
   axi::clear_error();
   AXI_TRY(axi::check_ptr("rigid_step", plan_dev, "plan_dev"));
-  return rigid_step<double>(cases, n_cases, plan_dev, n_tiles, n_steps, axi::as_stream(stream),
-                            "rigid_step_f64");
+  return rigid_step<double>(info, plan_dev, n_steps, axi::as_stream(stream), "rigid_step_f64");
 }
 
-extern "C" int axi_rigid_step_f32(const axi_case* cases, int n_cases, const void* plan_dev,
-                                  int n_tiles, int n_steps, void* stream) {
+extern "C" int axi_rigid_step_f32(const axi_plan_info* info, const void* plan_dev, int n_steps,
+                                  void* stream) {
   axi::clear_error();
   AXI_TRY(axi::check_ptr("rigid_step", plan_dev, "plan_dev"));
-  return rigid_step<float>(cases, n_cases, plan_dev, n_tiles, n_steps, axi::as_stream(stream),
-                           "rigid_step_f32");
+  return rigid_step<float>(info, plan_dev, n_steps, axi::as_stream(stream), "rigid_step_f32");
 }
 
-extern "C" int axi_rigid_phase_f64(const axi_case* cases, int n_cases, const void* plan_dev,
-                                   int n_tiles, int phase, void* stream) {
+extern "C" int axi_rigid_phase_f64(const axi_plan_info* info, const void* plan_dev, int phase,
+                                   void* stream) {
   axi::clear_error();
   AXI_TRY(axi::check_ptr("rigid_phase", plan_dev, "plan_dev"));
-  return run_phase<double>(phase, cases, n_cases, static_cast<const axi_case*>(plan_dev),
-                           tile_table(plan_dev, n_cases), n_tiles, axi::as_stream(stream));
+  return rigid_phase<double>(info, plan_dev, phase, axi::as_stream(stream));
 }
 
-extern "C" int axi_rigid_phase_f32(const axi_case* cases, int n_cases, const void* plan_dev,
-                                   int n_tiles, int phase, void* stream) {
+extern "C" int axi_rigid_phase_f32(const axi_plan_info* info, const void* plan_dev, int phase,
+                                   void* stream) {
   axi::clear_error();
   AXI_TRY(axi::check_ptr("rigid_phase", plan_dev, "plan_dev"));
-  return run_phase<float>(phase, cases, n_cases, static_cast<const axi_case*>(plan_dev),
-                          tile_table(plan_dev, n_cases), n_tiles, axi::as_stream(stream));
+  return rigid_phase<float>(info, plan_dev, phase, axi::as_stream(stream));
 }

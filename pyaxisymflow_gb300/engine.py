@@ -21,7 +21,8 @@ from .kernels.FastDiagonalisationStokesSolver import FastDiagonalisationStokesSo
 from .kernels.smooth_Heaviside import smooth_Heaviside
 
 ST_T, ST_DT, ST_CD, ST_STEPS, ST_UMAX, ST_COUNT, ST_STATUS, ST_FORCE = range(8)
-ST_WORDS = 8
+ST_UFREE, ST_LAMDT, ST_ADV, ST_C1, ST_C2 = range(8, 13)
+ST_WORDS = 16
 
 
 class AxiCase(ctypes.Structure):
@@ -33,11 +34,12 @@ class AxiCase(ctypes.Structure):
         ("U0", ctypes.c_double), ("t_ramp", ctypes.c_double), ("cfl", ctypes.c_double),
         ("U_body", ctypes.c_double), ("cd_scale", ctypes.c_double),
         ("dt_diff", ctypes.c_double), ("eps", ctypes.c_double),
+        ("inv_dx2", ctypes.c_double), ("inv_2dx", ctypes.c_double),
         ("omega", ctypes.c_void_p), ("psi", ctypes.c_void_p), ("u_z", ctypes.c_void_p),
         ("u_r", ctypes.c_void_p), ("chi", ctypes.c_void_p), ("w_adv", ctypes.c_void_p),
         ("w_tmp", ctypes.c_void_p),
         ("r", ctypes.c_void_p), ("z", ctypes.c_void_p), ("rinv2dx", ctypes.c_void_p),
-        ("rinv2", ctypes.c_void_p),
+        ("rinv2", ctypes.c_void_p), ("rw", ctypes.c_void_p),
         ("Er", ctypes.c_void_p), ("Er_inv_w", ctypes.c_void_p), ("EzinvT", ctypes.c_void_p),
         ("EzT", ctypes.c_void_p), ("inv_eig", ctypes.c_void_p),
         ("gemm_work", ctypes.c_void_p), ("state", ctypes.c_void_p),
@@ -103,6 +105,13 @@ def grid(nz, nr, dx):
     return z, r
 
 
+class AxiPlanInfo(ctypes.Structure):
+    """Mirror of ``axi_plan_info`` in include/axisym_gb300.h."""
+    _fields_ = [("n_cases", ctypes.c_int32), ("n_stencil_tiles", ctypes.c_int32),
+                ("n_gemm_tiles", ctypes.c_int32), ("elem_bytes", ctypes.c_int32),
+                ("bytes", ctypes.c_int64)]
+
+
 class _Bases:
     """Spectral bases shared by all cases with the same (nr, nz, dx)."""
 
@@ -157,8 +166,9 @@ class RigidEnsemble:
                 w_tmp=torch.zeros((c.nr, c.nz), **f),
                 r=torch.tensor(r, **f64),
                 z=torch.tensor(z, **f64),
-                rinv2dx=torch.tensor(1.0 / (2 * c.dx * r), **f64),
-                rinv2=torch.tensor(1.0 / (r * r), **f64),
+                rinv2dx=torch.tensor(1.0 / (2 * c.dx * r), **f64).to(self.dtype),
+                rinv2=torch.tensor(1.0 / (r * r), **f64).to(self.dtype),
+                rw=torch.tensor(r, **f64).to(self.dtype),
                 gemm_work=torch.zeros(2 * c.nr * c.nz, **f),
                 partials=torch.zeros(((c.nr + 7) // 8) * ((c.nz + 31) // 32) + 8, **f64),
             )
@@ -171,8 +181,10 @@ class RigidEnsemble:
             s.cd_scale = 2 * 2 * math.pi * c.dx * c.dx * c.lam / (math.pi * c.r_sphere ** 2)
             s.dt_diff = 0.9 * c.dx ** 2 / 4 / c.nu
             s.eps = float(np.finfo(float).eps)
+            s.inv_dx2 = 1.0 / (c.dx * c.dx)
+            s.inv_2dx = 0.5 / c.dx
             for name in ("omega", "psi", "u_z", "u_r", "chi", "w_adv", "w_tmp", "r", "z",
-                         "rinv2dx", "rinv2", "gemm_work", "partials"):
+                         "rinv2dx", "rinv2", "rw", "gemm_work", "partials"):
                 setattr(s, name, t[name].data_ptr())
             for name, v in b.t.items():
                 setattr(s, name, v.data_ptr())
@@ -185,17 +197,18 @@ class RigidEnsemble:
                 s.history_len = 0
         self._bases = bases
         lib = N.lib()
-        nbytes = ctypes.c_int64(0)
-        ntiles = ctypes.c_int(0)
-        N.check(lib.axi_plan_init(ctypes.addressof(self.structs), n, ctypes.byref(nbytes),
-                                  ctypes.byref(ntiles)), "plan_init")
-        self.n_tiles = ntiles.value
-        self.plan = torch.empty(int(nbytes.value), dtype=torch.uint8, device=self.device)
-        N.check(lib.axi_plan_upload(ctypes.addressof(self.structs), n,
+        self.info = AxiPlanInfo()
+        esize = 8 if precision == "f64" else 4
+        N.check(lib.axi_plan_init(ctypes.addressof(self.structs), n, esize,
+                                  ctypes.byref(self.info)), "plan_init")
+        self.n_tiles = self.info.n_stencil_tiles
+        self.plan = torch.empty(int(self.info.bytes), dtype=torch.uint8, device=self.device)
+        N.check(lib.axi_plan_upload(ctypes.addressof(self.structs), ctypes.byref(self.info),
                                     ctypes.c_void_p(self.plan.data_ptr()),
                                     ctypes.c_void_p(torch.cuda.current_stream(
                                         self.device).cuda_stream)), "plan_upload")
         self._step_fn = getattr(lib, f"axi_rigid_step_{precision}")
+        self._phase_fn = getattr(lib, f"axi_rigid_phase_{precision}")
         self.graph = None
 
     @property
@@ -208,19 +221,16 @@ class RigidEnsemble:
     def step(self, n=1, stream=None):
         """Advance every case by n steps (asynchronous on torch's current stream)."""
         s = stream if stream is not None else torch.cuda.current_stream(self.device)
-        N.check(self._step_fn(ctypes.addressof(self.structs), self.n_cases,
-                              ctypes.c_void_p(self.plan.data_ptr()), self.n_tiles, int(n),
-                              ctypes.c_void_p(s.cuda_stream)), "rigid_step")
+        N.check(self._step_fn(ctypes.byref(self.info), ctypes.c_void_p(self.plan.data_ptr()),
+                              int(n), ctypes.c_void_p(s.cuda_stream)), "rigid_step")
 
     PHASES = ("kill", "transform", "vel_max", "penalise", "adv_diff1", "diff2")
 
     def phase(self, ph, stream=None):
         """Run one phase of a step (see PHASES); all six in order = one step."""
         s = stream if stream is not None else torch.cuda.current_stream(self.device)
-        fn = getattr(N.lib(), f"axi_rigid_phase_{self.precision}")
-        N.check(fn(ctypes.addressof(self.structs), self.n_cases,
-                   ctypes.c_void_p(self.plan.data_ptr()), self.n_tiles, int(ph),
-                   ctypes.c_void_p(s.cuda_stream)), "rigid_phase")
+        N.check(self._phase_fn(ctypes.byref(self.info), ctypes.c_void_p(self.plan.data_ptr()),
+                               int(ph), ctypes.c_void_p(s.cuda_stream)), "rigid_phase")
 
     def capture(self, steps_per_replay=1):
         """Capture `steps_per_replay` steps into a CUDA graph (replay with replay())."""
