@@ -257,6 +257,14 @@ int axi_fd_transform_f64(double* out, int ld_out, const double* in, int ld_in,
                          const double* Er_inv_w, const double* EzinvT, const double* inv_eig,
                          const double* Er, const double* EzT, double* work, int nr, int nz,
                          void* stream);
+/* FP32 GEMM on the tcgen05 tensor cores with 3xTF32 split products (FP32
+ * accuracy): C (M, N) = A (M, K) * B (N, K)^T, all row-major float, K a
+ * multiple of 4. work: device scratch of axi_tf32x3_gemm_work_bytes(M, N, K)
+ * bytes. Synchronises the stream (reads the kernel's pipeline status).
+ * The operand form of the spectral products in the FP32 engine. */
+int64_t axi_tf32x3_gemm_work_bytes(int M, int N, int K);
+int axi_tf32x3_gemm(float* C, const float* A, const float* B, int M, int N, int K, void* work,
+                    void* stream);
 /* Row-major double GEMM C = A(M,K) * B(K,N) (.* S(M,N) if S != NULL), row
  * strides ldc, lda, ldb; S is dense (row stride N). */
 int axi_dgemm_f64(double* C, int ldc, const double* A, int lda, const double* B, int ldb,
@@ -324,6 +332,14 @@ typedef struct axi_case {
   double* partials;      /* one double per stencil tile of the case */
   double* history;       /* optional: 2 doubles (dt, Cd) per step, or NULL */
   int64_t history_len;
+  /* FP32 engine with the spectral products on the tensor cores (plan flag
+   * AXI_PLAN_TENSOR_CORES): TF32 hi parts and FP32 remainders (lo) of the
+   * operands, row-major float. */
+  void* omega_hi;        /* (nr, nz), kept in step with omega */
+  void* omega_lo;
+  const void* tc_basis[8]; /* E_z^-1 hi, lo (nz, nz); E_r^-1 diag(r) hi, lo (nr, nr);
+                              E_z hi, lo (nz, nz); E_r hi, lo (nr, nr) */
+  void* tc_work[4];        /* X hi, lo (nz, nr); Y hi, lo (nr, nz) */
 } axi_case;
 
 /* Launch plan of a set of cases: tile tables in device memory. */
@@ -333,11 +349,22 @@ typedef struct axi_plan_info {
   int32_t n_gemm_tiles;    /* output tiles of the grouped spectral products */
   int32_t elem_bytes;      /* 8: float64 fields, 4: float32 fields */
   int64_t bytes;           /* device bytes the plan needs */
+  int32_t flags;           /* AXI_PLAN_* */
+  int32_t n_tc_tiles[4];   /* tensor-core tiles per spectral stage */
+  int32_t reserved;
 } axi_plan_info;
 
+enum { AXI_PLAN_TENSOR_CORES = 1 };
+
 /* Host only: validates the cases, assigns each its first tile
- * (cases[k].stencil_tile0) and fills `info` (sizes of the plan). */
-int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, axi_plan_info* info);
+ * (cases[k].stencil_tile0) and fills `info` (sizes of the plan). flags:
+ * AXI_PLAN_TENSOR_CORES (FP32 only) runs the spectral products as tcgen05
+ * 3xTF32 GEMMs (the tc_* and omega_hi / omega_lo members must be set). */
+int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, int flags, axi_plan_info* info);
+/* Pipeline status of the tensor-core products since the plan was uploaded
+ * (0 = healthy; otherwise a wait timed out). Synchronises the stream. */
+int axi_plan_tc_status(const axi_plan_info* info, const void* plan_dev, int* tc_error,
+                       void* stream);
 /* Copies the case table and tile tables into plan_dev (caller-allocated,
  * info->bytes); synchronises the stream. Re-upload after changing a case. */
 int axi_plan_upload(const axi_case* cases, const axi_plan_info* info, void* plan_dev,

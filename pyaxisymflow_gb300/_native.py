@@ -50,7 +50,10 @@ def _signatures():
             I, [P, P, P, P, P, P, P, P, P, D, I, I, P, P, I, P, P, P]),
         "axi_fd_transform_f64": (I, [P, I, P, I, P, P, P, P, P, P, I, I, P]),
         "axi_dgemm_f64": (I, [P, I, P, I, P, I, P, I, I, I, P]),
-        "axi_plan_init": (I, [P, I, I, P]),
+        "axi_tf32x3_gemm_work_bytes": (I64, [I, I, I]),
+        "axi_tf32x3_gemm": (I, [P, P, P, I, I, I, P, P]),
+        "axi_plan_init": (I, [P, I, I, I, P]),
+        "axi_plan_tc_status": (I, [P, P, P, P]),
         "axi_plan_upload": (I, [P, P, P, P]),
         "axi_rigid_step_f64": (I, [P, P, I, P]),
         "axi_rigid_step_f32": (I, [P, P, I, P]),

@@ -27,6 +27,7 @@
 // axis / outer-boundary one-sided rows of u_z (the r = 0 closure), the time
 // step, time and the drag sums across warps and tiles.
 #include "axi_common.cuh"
+#include "tc_gemm.cuh"
 
 namespace {
 
@@ -46,6 +47,21 @@ __device__ __forceinline__ const T* CF(const void* p) {
 
 __device__ __forceinline__ unsigned int* counter(const axi_case& k, int which) {
   return reinterpret_cast<unsigned int*>(&k.state[AXI_ST_COUNT]) + which;
+}
+
+// Keeps the TF32 hi / lo copy of omega (operand of the tensor-core products)
+// in step with omega in the FP32 engine.
+template <typename T>
+__device__ __forceinline__ void store_omega(const axi_case& k, long long c, T v) {
+  F<T>(k.omega)[c] = v;
+  if constexpr (sizeof(T) == 4) {
+    if (k.omega_hi) {
+      float hi, lo;
+      axi_tc::tf32_split((float)v, hi, lo);
+      static_cast<float*>(k.omega_hi)[c] = hi;
+      static_cast<float*>(k.omega_lo)[c] = lo;
+    }
+  }
 }
 
 inline int tiles_of(const axi_case& k) { return ((k.nr + TY - 1) / TY) * ((k.nz + TX - 1) / TX); }
@@ -77,20 +93,21 @@ __global__ void kill_reset_kernel(const axi_case* __restrict__ cases) {
     const double left = (double)row[wd - 1];
     double nl[8];
     for (int q = 0; q < wd; ++q) nl[q] = sin(kPi * (k.z[q] - half_dx) / 2 / (wd - 1) / dx) * left;
-    for (int q = 0; q < wd; ++q) row[q] = (T)nl[q];
+    for (int q = 0; q < wd; ++q) store_omega<T>(k, (long long)i * nz + q, (T)nl[q]);
     const double right = (double)row[nz - wd];
     for (int q = 0; q < wd; ++q)
       nl[q] = sin(kPi * (1 - k.z[nz - wd + q] - half_dx) / 2 / (wd - 1) / dx) * right;
-    for (int q = 0; q < wd; ++q) row[nz - wd + q] = (T)nl[q];
+    for (int q = 0; q < wd; ++q) store_omega<T>(k, (long long)i * nz + nz - wd + q, (T)nl[q]);
   }
   __syncthreads();
   for (int j = threadIdx.x; j < nz; j += blockDim.x) {
     const double src = (double)w[(long long)(nr - wd) * nz + j];
     for (int q = 0; q < wd; ++q) {
       const int i = nr - wd + q;
-      w[(long long)i * nz + j] = (T)(sin(kPi * (1 - k.r[i] - half_dx) / 2 / (wd - 1) / dx) * src);
+      store_omega<T>(k, (long long)i * nz + j,
+                     (T)(sin(kPi * (1 - k.r[i] - half_dx) / 2 / (wd - 1) / dx) * src));
     }
-    w[j] = T(0);
+    store_omega<T>(k, j, T(0));
   }
 }
 
@@ -410,7 +427,7 @@ __global__ void __launch_bounds__(NT) diff2_kernel(const axi_case* __restrict__ 
                     (n - s) * CF<T>(k.rinv2dx)[gi] - c0 * CF<T>(k.rinv2)[gi];
       v = v + (T)k.state[AXI_ST_C2] * lap;
     }
-    F<T>(k.omega)[c] = v;
+    store_omega<T>(k, c, v);
   }
   if (tr.w == 0 && threadIdx.x == 0) {
     k.state[AXI_ST_T] += k.state[AXI_ST_DT];
@@ -520,23 +537,111 @@ __global__ void __launch_bounds__(gemm_threads<T>())
   }
 }
 
-// Plan layout in device memory: [axi_case x n][stencil tiles][gemm tiles].
+// Plan layout in device memory:
+//   [axi_case x n][stencil tiles][gemm tiles]            (all plans)
+//   [TcJob x 4n][tc tiles stage 0..3][error word]        (tensor-core plans)
 struct PlanView {
   const axi_case* cases;
   const int4* stencil;
   const int4* gemm;
+  const axi_tc::TcJob* jobs;
+  const int4* tc_tiles[4];
+  int* tc_err;
 };
 
 inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+inline size_t align128(size_t x) { return (x + 127) & ~size_t(127); }
+
+struct PlanOffsets {
+  size_t stencil, gemm, jobs, tc_tiles[4], err, total;
+};
+
+inline PlanOffsets plan_offsets(const axi_plan_info* info) {
+  PlanOffsets o;
+  o.stencil = align16(info->n_cases * sizeof(axi_case));
+  o.gemm = o.stencil + (size_t)info->n_stencil_tiles * sizeof(int4);
+  size_t end = o.gemm + (size_t)info->n_gemm_tiles * sizeof(int4);
+  if (info->flags & AXI_PLAN_TENSOR_CORES) {
+    o.jobs = align128(end);
+    end = o.jobs + (size_t)4 * info->n_cases * sizeof(axi_tc::TcJob);
+    for (int st = 0; st < 4; ++st) {
+      o.tc_tiles[st] = align16(end);
+      end = o.tc_tiles[st] + (size_t)info->n_tc_tiles[st] * sizeof(int4);
+    }
+    o.err = align16(end);
+    end = o.err + 16;
+  } else {
+    o.jobs = o.err = 0;
+    for (int st = 0; st < 4; ++st) o.tc_tiles[st] = 0;
+  }
+  o.total = align16(end);
+  return o;
+}
 
 inline PlanView plan_view(const void* plan_dev, const axi_plan_info* info) {
   const char* base = static_cast<const char*>(plan_dev);
+  const PlanOffsets o = plan_offsets(info);
   PlanView v;
   v.cases = reinterpret_cast<const axi_case*>(base);
-  const size_t off1 = align16(info->n_cases * sizeof(axi_case));
-  v.stencil = reinterpret_cast<const int4*>(base + off1);
-  v.gemm = reinterpret_cast<const int4*>(base + off1 + info->n_stencil_tiles * sizeof(int4));
+  v.stencil = reinterpret_cast<const int4*>(base + o.stencil);
+  v.gemm = reinterpret_cast<const int4*>(base + o.gemm);
+  const bool tc = (info->flags & AXI_PLAN_TENSOR_CORES) != 0;
+  v.jobs = tc ? reinterpret_cast<const axi_tc::TcJob*>(base + o.jobs) : nullptr;
+  for (int st = 0; st < 4; ++st)
+    v.tc_tiles[st] = tc ? reinterpret_cast<const int4*>(base + o.tc_tiles[st]) : nullptr;
+  v.tc_err = tc ? reinterpret_cast<int*>(const_cast<char*>(base) + o.err) : nullptr;
   return v;
+}
+
+// Tensor-core form of the four spectral products of one case (operands
+// K-major): X = Ez^-1 * omega^T ... written as C = A * B^T per stage:
+//   stage 0  X (nz, nr) = Ezinv (nz, nz) * [omega (nr, nz)]^T      -> split
+//   stage 1  Y (nr, nz) = (ErIw (nr, nr) * [X]^T) .* inv_eig        -> split
+//   stage 2  X (nz, nr) = Ez (nz, nz) * [Y]^T                       -> split
+//   stage 3  psi (nr, nz) = Er (nr, nr) * [X]^T                     -> plain
+// i.e. psi = E_r ((E_r^-1 diag(r) omega E_z^-T) .* inv_eig) E_z^T as in
+// kernels/FastDiagonalisationStokesSolver.py:137-156.
+int build_tc_jobs(const axi_case& k, axi_tc::TcJob job[4]) {
+  const int nr = k.nr, nz = k.nz;
+  const float* const* b = reinterpret_cast<const float* const*>(k.tc_basis);
+  float* const* w = reinterpret_cast<float* const*>(k.tc_work);
+  memset(job, 0, 4 * sizeof(axi_tc::TcJob));
+  // stage 0
+  AXI_TRY(axi_tc::encode_operand(&job[0].a_hi, b[0], nz, nz, nz));
+  AXI_TRY(axi_tc::encode_operand(&job[0].a_lo, b[1], nz, nz, nz));
+  AXI_TRY(axi_tc::encode_operand(&job[0].b_hi, static_cast<const float*>(k.omega_hi), nr, nz, nz));
+  AXI_TRY(axi_tc::encode_operand(&job[0].b_lo, static_cast<const float*>(k.omega_lo), nr, nz, nz));
+  job[0].c = w[0]; job[0].c_lo = w[1]; job[0].M = nz; job[0].N = nr; job[0].K = nz;
+  job[0].ldc = nr; job[0].mode = axi_tc::MODE_SPLIT;
+  // stage 1
+  AXI_TRY(axi_tc::encode_operand(&job[1].a_hi, b[2], nr, nr, nr));
+  AXI_TRY(axi_tc::encode_operand(&job[1].a_lo, b[3], nr, nr, nr));
+  AXI_TRY(axi_tc::encode_operand(&job[1].b_hi, w[0], nz, nr, nr));
+  AXI_TRY(axi_tc::encode_operand(&job[1].b_lo, w[1], nz, nr, nr));
+  job[1].c = w[2]; job[1].c_lo = w[3]; job[1].scale = static_cast<const float*>(k.inv_eig);
+  job[1].M = nr; job[1].N = nz; job[1].K = nr; job[1].ldc = nz;
+  job[1].mode = axi_tc::MODE_SCALE_SPLIT;
+  // stage 2
+  AXI_TRY(axi_tc::encode_operand(&job[2].a_hi, b[4], nz, nz, nz));
+  AXI_TRY(axi_tc::encode_operand(&job[2].a_lo, b[5], nz, nz, nz));
+  AXI_TRY(axi_tc::encode_operand(&job[2].b_hi, w[2], nr, nz, nz));
+  AXI_TRY(axi_tc::encode_operand(&job[2].b_lo, w[3], nr, nz, nz));
+  job[2].c = w[0]; job[2].c_lo = w[1]; job[2].M = nz; job[2].N = nr; job[2].K = nz;
+  job[2].ldc = nr; job[2].mode = axi_tc::MODE_SPLIT;
+  // stage 3
+  AXI_TRY(axi_tc::encode_operand(&job[3].a_hi, b[6], nr, nr, nr));
+  AXI_TRY(axi_tc::encode_operand(&job[3].a_lo, b[7], nr, nr, nr));
+  AXI_TRY(axi_tc::encode_operand(&job[3].b_hi, w[0], nz, nr, nr));
+  AXI_TRY(axi_tc::encode_operand(&job[3].b_lo, w[1], nz, nr, nr));
+  job[3].c = static_cast<float*>(k.psi); job[3].c_lo = nullptr; job[3].M = nr; job[3].N = nz;
+  job[3].K = nr; job[3].ldc = nz; job[3].mode = axi_tc::MODE_PLAIN;
+  return AXI_OK;
+}
+
+inline int tc_tiles_of(const axi_case& k, int stage) {
+  const int M = (stage % 2 == 0) ? k.nz : k.nr;
+  const int N = (stage % 2 == 0) ? k.nr : k.nz;
+  return ((M + axi_tc::BM - 1) / axi_tc::BM) * ((N + axi_tc::BN - 1) / axi_tc::BN);
 }
 
 enum { PH_KILL = 0, PH_TRANSFORM = 1, PH_VEL_MAX = 2, PH_PENALISE = 3, PH_ADV_DIFF1 = 4,
@@ -550,6 +655,11 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
       kill_reset_kernel<T><<<info->n_cases, 256, 0, s>>>(v.cases);
       break;
     case PH_TRANSFORM:
+      if (v.jobs) {
+        for (int st = 0; st < 4; ++st)
+          AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[st], info->n_tc_tiles[st], v.tc_err, s));
+        break;
+      }
       grouped_gemm_kernel<T, 0><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
       grouped_gemm_kernel<T, 1><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
       grouped_gemm_kernel<T, 2><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
@@ -641,23 +751,45 @@ int rigid_phase(const axi_plan_info* info, const void* plan_dev, int phase, cuda
 
 }  // namespace
 
-extern "C" int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, axi_plan_info* info) {
+extern "C" int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, int flags,
+                             axi_plan_info* info) {
   axi::clear_error();
   AXI_TRY(validate(cases, n_cases, "plan_init"));
   AXI_TRY(axi::check_ptr("plan_init", info, "info"));
   int bm, bn;
   AXI_TRY(gemm_tile_dims(elem_bytes, &bm, &bn));
+  const bool tc = (flags & AXI_PLAN_TENSOR_CORES) != 0;
+  if (tc && elem_bytes != 4) {
+    axi::set_error("plan_init: tensor-core products need float32 fields");
+    return AXI_ERR_INVALID;
+  }
+  memset(info, 0, sizeof(*info));
   int nt = 0, ng = 0;
   for (int c = 0; c < n_cases; ++c) {
+    const axi_case& k = cases[c];
     cases[c].stencil_tile0 = nt;
-    nt += tiles_of(cases[c]);
-    ng += ((cases[c].nr + bm - 1) / bm) * ((cases[c].nz + bn - 1) / bn);
+    nt += tiles_of(k);
+    ng += ((k.nr + bm - 1) / bm) * ((k.nz + bn - 1) / bn);
+    if (tc) {
+      if (!k.omega_hi || !k.omega_lo || (k.nr % 4) || (k.nz % 4)) {
+        axi::set_error("plan_init: case %d lacks tensor-core operands or nr, nz not multiples of 4",
+                       c);
+        return AXI_ERR_INVALID;
+      }
+      for (int q = 0; q < 8; ++q)
+        if (!k.tc_basis[q] || (q < 4 && !k.tc_work[q])) {
+          axi::set_error("plan_init: case %d lacks tensor-core operand %d", c, q);
+          return AXI_ERR_INVALID;
+        }
+      for (int st = 0; st < 4; ++st) info->n_tc_tiles[st] += tc_tiles_of(k, st);
+    }
   }
   info->n_cases = n_cases;
   info->n_stencil_tiles = nt;
   info->n_gemm_tiles = ng;
   info->elem_bytes = elem_bytes;
-  info->bytes = (int64_t)(align16(n_cases * sizeof(axi_case)) + (size_t)(nt + ng) * sizeof(int4));
+  info->flags = tc ? AXI_PLAN_TENSOR_CORES : 0;
+  info->bytes = (int64_t)plan_offsets(info).total;
   return AXI_OK;
 }
 
@@ -694,10 +826,45 @@ extern "C" int axi_plan_upload(const axi_case* cases, const axi_plan_info* info,
     axi::set_error("plan_upload: cases changed since plan_init");
     return AXI_ERR_INVALID;
   }
+  if (info->flags & AXI_PLAN_TENSOR_CORES) {
+    const PlanOffsets o = plan_offsets(info);
+    axi_tc::TcJob* jobs = reinterpret_cast<axi_tc::TcJob*>(&buf[o.jobs]);
+    for (int c = 0; c < n; ++c) AXI_TRY(build_tc_jobs(cases[c], jobs + 4 * c));
+    for (int st = 0; st < 4; ++st) {
+      int4* tt = reinterpret_cast<int4*>(&buf[o.tc_tiles[st]]);
+      int qq = 0;
+      for (int c = 0; c < n; ++c) {
+        const axi_case& k = cases[c];
+        const int M = (st % 2 == 0) ? k.nz : k.nr;
+        const int N = (st % 2 == 0) ? k.nr : k.nz;
+        for (int m0 = 0; m0 < M; m0 += axi_tc::BM)
+          for (int n0 = 0; n0 < N; n0 += axi_tc::BN) tt[qq++] = make_int4(4 * c + st, m0, n0, 0);
+      }
+      if (qq != info->n_tc_tiles[st]) {
+        axi::set_error("plan_upload: cases changed since plan_init");
+        return AXI_ERR_INVALID;
+      }
+    }
+  }
   cudaStream_t s = axi::as_stream(stream);
   if (cudaMemcpyAsync(plan_dev, buf.data(), buf.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return axi::launch_status("plan_upload");
+  return AXI_OK;
+}
+
+extern "C" int axi_plan_tc_status(const axi_plan_info* info, const void* plan_dev, int* tc_error,
+                                  void* stream) {
+  axi::clear_error();
+  AXI_TRY(axi::check_ptr("plan_tc_status", info, "info"));
+  AXI_TRY(axi::check_ptr("plan_tc_status", plan_dev, "plan_dev"));
+  *tc_error = 0;
+  if (!(info->flags & AXI_PLAN_TENSOR_CORES)) return AXI_OK;
+  const PlanView v = plan_view(plan_dev, info);
+  cudaStream_t s = axi::as_stream(stream);
+  if (cudaMemcpyAsync(tc_error, v.tc_err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return axi::launch_status("plan_tc_status");
   return AXI_OK;
 }
 

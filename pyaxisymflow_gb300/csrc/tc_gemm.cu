@@ -1,0 +1,412 @@
+// tcgen05 3xTF32 GEMM: kernel and host helpers (see tc_gemm.cuh).
+#include <cudaTypedefs.h>
+
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "tc_gemm.cuh"
+
+namespace axi_tc {
+namespace {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait on an mbarrier phase. False on timeout (error recorded) or when
+// another thread of the grid has already failed.
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*reinterpret_cast<volatile int*>(err) != 0) return false;
+    if (globaltimer() - t0 > WAIT_NS) {
+      atomicCAS(err, 0, code);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// D(tmem) (+)= A(smem desc) * B(smem desc), kind::tf32, FP32 accumulate.
+__device__ __forceinline__ void umma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major tile with 128-byte rows and the
+// 128-byte swizzle (8-row atoms of 1024 bytes, atoms 1024 bytes apart).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);  // start address >> 4
+  d |= static_cast<uint64_t>(1) << 16;                   // leading byte offset (unused here)
+  d |= static_cast<uint64_t>(1024 >> 4) << 32;           // stride byte offset: 8 rows x 128 B
+  d |= static_cast<uint64_t>(1) << 46;                   // descriptor version
+  d |= static_cast<uint64_t>(2) << 61;                   // swizzle: 128 B
+  return d;
+}
+
+// Instruction descriptor: D = F32, A = B = TF32, both K-major, M = 128, N = 128.
+__host__ __device__ constexpr uint32_t idesc_tf32(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | (static_cast<uint32_t>(n >> 3) << 17) |
+         (static_cast<uint32_t>(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void store_value(const TcJob& job, int row, int col, float v) {
+  const long long idx = (long long)row * job.ldc + col;
+  if (job.mode == MODE_PLAIN) {
+    job.c[idx] = v;
+    return;
+  }
+  if (job.mode == MODE_SCALE_SPLIT) v *= job.scale[(long long)row * job.N + col];
+  float hi, lo;
+  tf32_split(v, hi, lo);
+  job.c[idx] = hi;
+  job.c_lo[idx] = lo;
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    tf32x3_gemm_kernel(const TcJob* __restrict__ jobs, const int4* __restrict__ tiles,
+                       int* __restrict__ err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + NSTAGE * STAGE_BYTES);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * NSTAGE + 1);
+  int* progress = reinterpret_cast<int*>(tmem_slot + 1);  // [0] issued, [1] consumed
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int4 tr = tiles[blockIdx.x];
+  const TcJob& job = jobs[tr.x];
+  const int m0 = tr.y, n0 = tr.z;
+  const int nk = (job.K + BKF - 1) / BKF;
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + NSTAGE);
+  const uint32_t done = smem_u32(bars + 2 * NSTAGE);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    mbar_init(done, 1);
+    progress[0] = 0;
+    progress[1] = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    tmem_alloc(smem_u32(tmem_slot), BN);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // ---- TMA producer ----
+    int kb = 0;
+    for (; kb < nk; ++kb) {
+      const int s = kb % NSTAGE, use = kb / NSTAGE;
+      if (use > 0 && !mbar_wait(empty0 + 8 * s, (use - 1) & 1, err, ERR_PRODUCER)) break;
+      const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+      const uint32_t fb = full0 + 8 * s;
+      mbar_expect_tx(fb, STAGE_BYTES);
+      const int kx = kb * BKF;
+      tma_load_2d(st + 0 * TILE_BYTES, &job.a_hi, kx, m0, fb);
+      tma_load_2d(st + 1 * TILE_BYTES, &job.a_lo, kx, m0, fb);
+      tma_load_2d(st + 2 * TILE_BYTES, &job.b_hi, kx, n0, fb);
+      tma_load_2d(st + 3 * TILE_BYTES, &job.b_lo, kx, n0, fb);
+    }
+    progress[0] = kb;
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer ----
+    constexpr uint32_t idesc = idesc_tf32(BM, BN);
+    int kb = 0;
+    for (; kb < nk; ++kb) {
+      const int s = kb % NSTAGE, use = kb / NSTAGE;
+      if (!mbar_wait(full0 + 8 * s, use & 1, err, ERR_MMA)) break;
+      tc_fence_after();
+      const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+      const uint64_t ah = sw128_desc(st), al = sw128_desc(st + TILE_BYTES);
+      const uint64_t bh = sw128_desc(st + 2 * TILE_BYTES), bl = sw128_desc(st + 3 * TILE_BYTES);
+#pragma unroll
+      for (int kk = 0; kk < BKF / 8; ++kk) {
+        const uint64_t o = static_cast<uint64_t>(kk * 32) >> 4;  // 8 TF32 = 32 bytes
+        umma_tf32(tmem, ah + o, bh + o, idesc, (kb | kk) != 0 ? 1u : 0u);
+        umma_tf32(tmem, ah + o, bl + o, idesc, 1u);
+        umma_tf32(tmem, al + o, bh + o, idesc, 1u);
+      }
+      umma_commit(empty0 + 8 * s);
+    }
+    progress[1] = kb;
+    umma_commit(done);
+  }
+  __syncwarp();
+
+  // ---- epilogue ----
+  const bool ok = mbar_wait(done, 0, err, ERR_EPILOGUE);
+  tc_fence_after();
+  // tcgen05.ld is warp-collective: decide per warp
+  if (__all_sync(0xffffffffu, ok && *reinterpret_cast<volatile int*>(err) == 0)) {
+    const int row = m0 + warp * 32 + lane;
+    const bool vec = (job.ldc % 4) == 0 && job.mode == MODE_PLAIN;
+#pragma unroll 1
+    for (int cc = 0; cc < BN / 32; ++cc) {
+      uint32_t r[32];
+      tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + cc * 32, r);
+      if (row < job.M) {
+        const int col0 = n0 + cc * 32;
+        if (vec && col0 + 32 <= job.N) {
+          float4* dst = reinterpret_cast<float4*>(job.c + (long long)row * job.ldc + col0);
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            dst[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]),
+                                 __uint_as_float(r[4 * j + 2]), __uint_as_float(r[4 * j + 3]));
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j)
+            if (col0 + j < job.N) store_value(job, row, col0 + j, __uint_as_float(r[j]));
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0 && progress[1] < progress[0]) {
+    // a failure left copies in flight: wait for them (bounded) before exiting
+    for (int kb = progress[1]; kb < progress[0]; ++kb)
+      mbar_wait(full0 + 8 * (kb % NSTAGE), (kb / NSTAGE) & 1, err, ERR_DRAIN);
+  }
+  __syncthreads();
+  if (warp == 1) tmem_dealloc(tmem, BN);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+}  // namespace
+
+int encode_operand(CUtensorMap* map, const float* base, int rows, int K, int ld) {
+  auto fn = encode_fn();
+  if (!fn) {
+    axi::set_error("tensor core GEMM: cuTensorMapEncodeTiled unavailable");
+    return AXI_ERR_CUDA;
+  }
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || (ld * 4) % 16 != 0 || ld < K) {
+    axi::set_error("tensor core GEMM: operand not 16-byte aligned (ld = %d)", ld);
+    return AXI_ERR_INVALID;
+  }
+  const cuuint64_t dims[2] = {static_cast<cuuint64_t>(K), static_cast<cuuint64_t>(rows)};
+  const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld) * 4};
+  const cuuint32_t box[2] = {BKF, BM};
+  const cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    axi::set_error("tensor core GEMM: cuTensorMapEncodeTiled failed (%d)", static_cast<int>(r));
+    return AXI_ERR_CUDA;
+  }
+  return AXI_OK;
+}
+
+int launch(const TcJob* jobs_dev, const int4* tiles_dev, int n_tiles, int* err_dev,
+           cudaStream_t s) {
+  static std::once_flag once;
+  static cudaError_t attr_status = cudaSuccess;
+  std::call_once(once, [] {
+    attr_status = cudaFuncSetAttribute(tf32x3_gemm_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  });
+  if (attr_status != cudaSuccess) {
+    axi::set_error("tensor core GEMM: cannot reserve %d bytes of shared memory", SMEM_BYTES);
+    return AXI_ERR_CUDA;
+  }
+  if (n_tiles <= 0) return AXI_OK;
+  tf32x3_gemm_kernel<<<n_tiles, THREADS, SMEM_BYTES, s>>>(jobs_dev, tiles_dev, err_dev);
+  return axi::launch_status("tf32x3_gemm");
+}
+
+}  // namespace axi_tc
+
+// ---------------------------------------------------------------------------
+// Standalone entry: C (M, N) = A (M, K) * B (N, K)^T in FP32 via 3xTF32.
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void split_kernel(const float* __restrict__ x, float* __restrict__ hi,
+                             float* __restrict__ lo, long long n) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) axi_tc::tf32_split(x[k], hi[k], lo[k]);
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+struct TestLayout {
+  size_t a_hi, a_lo, b_hi, b_lo, job, tiles, err, total;
+};
+
+TestLayout test_layout(int M, int N, int K) {
+  TestLayout L;
+  size_t o = 0;
+  L.a_hi = o; o = align_up(o + (size_t)M * K * 4, 256);
+  L.a_lo = o; o = align_up(o + (size_t)M * K * 4, 256);
+  L.b_hi = o; o = align_up(o + (size_t)N * K * 4, 256);
+  L.b_lo = o; o = align_up(o + (size_t)N * K * 4, 256);
+  L.job = o; o = align_up(o + sizeof(axi_tc::TcJob), 256);
+  const size_t nt = (size_t)((M + axi_tc::BM - 1) / axi_tc::BM) * ((N + axi_tc::BN - 1) / axi_tc::BN);
+  L.tiles = o; o = align_up(o + nt * sizeof(int4), 256);
+  L.err = o; o = align_up(o + 16, 256);
+  L.total = o;
+  return L;
+}
+
+}  // namespace
+
+extern "C" int64_t axi_tf32x3_gemm_work_bytes(int M, int N, int K) {
+  return (int64_t)test_layout(M, N, K).total;
+}
+
+extern "C" int axi_tf32x3_gemm(float* C, const float* A, const float* B, int M, int N, int K,
+                               void* work, void* stream) {
+  axi::clear_error();
+  const char* what = "tf32x3_gemm";
+  if (M <= 0 || N <= 0 || K <= 0 || (K % 4) != 0) {
+    axi::set_error("%s: invalid shape M=%d N=%d K=%d (K must be a multiple of 4)", what, M, N, K);
+    return AXI_ERR_INVALID;
+  }
+  AXI_TRY(axi::check_ptr(what, work, "work"));
+  cudaStream_t s = axi::as_stream(stream);
+  const TestLayout L = test_layout(M, N, K);
+  char* w = static_cast<char*>(work);
+  float* ahi = reinterpret_cast<float*>(w + L.a_hi);
+  float* alo = reinterpret_cast<float*>(w + L.a_lo);
+  float* bhi = reinterpret_cast<float*>(w + L.b_hi);
+  float* blo = reinterpret_cast<float*>(w + L.b_lo);
+  split_kernel<<<axi::ceil_div((long long)M * K, 256), 256, 0, s>>>(A, ahi, alo, (long long)M * K);
+  split_kernel<<<axi::ceil_div((long long)N * K, 256), 256, 0, s>>>(B, bhi, blo, (long long)N * K);
+  AXI_TRY(axi::launch_status(what));
+  axi_tc::TcJob job;
+  memset(&job, 0, sizeof(job));
+  AXI_TRY(axi_tc::encode_operand(&job.a_hi, ahi, M, K, K));
+  AXI_TRY(axi_tc::encode_operand(&job.a_lo, alo, M, K, K));
+  AXI_TRY(axi_tc::encode_operand(&job.b_hi, bhi, N, K, K));
+  AXI_TRY(axi_tc::encode_operand(&job.b_lo, blo, N, K, K));
+  job.c = C;
+  job.c_lo = nullptr;
+  job.scale = nullptr;
+  job.M = M;
+  job.N = N;
+  job.K = K;
+  job.ldc = N;
+  job.mode = axi_tc::MODE_PLAIN;
+  std::string tiles;
+  for (int m0 = 0; m0 < M; m0 += axi_tc::BM)
+    for (int n0 = 0; n0 < N; n0 += axi_tc::BN) {
+      int4 t = make_int4(0, m0, n0, 0);
+      tiles.append(reinterpret_cast<const char*>(&t), sizeof(t));
+    }
+  const int n_tiles = (int)(tiles.size() / sizeof(int4));
+  if (cudaMemcpyAsync(w + L.job, &job, sizeof(job), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(w + L.tiles, tiles.data(), tiles.size(), cudaMemcpyHostToDevice, s) !=
+          cudaSuccess ||
+      cudaMemsetAsync(w + L.err, 0, 16, s) != cudaSuccess)
+    return axi::launch_status(what);
+  AXI_TRY(axi_tc::launch(reinterpret_cast<const axi_tc::TcJob*>(w + L.job),
+                         reinterpret_cast<const int4*>(w + L.tiles), n_tiles,
+                         reinterpret_cast<int*>(w + L.err), s));
+  int err = 0;
+  if (cudaMemcpyAsync(&err, w + L.err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return axi::launch_status(what);
+  if (err != 0) {
+    axi::set_error("%s: a pipeline wait timed out (code %d)", what, err);
+    return AXI_ERR_CUDA;
+  }
+  return AXI_OK;
+}

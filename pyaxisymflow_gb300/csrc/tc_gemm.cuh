@@ -1,0 +1,70 @@
+// tcgen05 (5th-generation tensor core) GEMM with FP32-accurate 3xTF32 products.
+//
+//   C[M, N] = A[M, K] * B[N, K]^T        (both operands K-major, FP32 in HBM)
+//
+// Each operand is stored as a TF32 "hi" part (low 13 mantissa bits cleared)
+// and the exact FP32 remainder "lo"; the tensor core accumulates
+// hi*hi + hi*lo + lo*hi in FP32 in tensor memory, which restores FP32-level
+// accuracy (the dropped lo*lo term is below FP32 rounding).
+//
+// One CTA computes a 128 x 128 output tile:
+//   warp 0, one thread   TMA producer: cp.async.bulk.tensor tiles (128 rows x
+//                        32 floats, 128-byte swizzle) of A_hi, A_lo, B_hi, B_lo
+//                        into a 3-stage shared-memory ring (mbarrier complete_tx)
+//   warp 1, one thread   MMA issuer: 3 x 4 tcgen05.mma.kind::tf32 per stage into
+//                        a 128-lane x 128-column FP32 accumulator in TMEM;
+//                        tcgen05.commit releases the stage
+//   warps 0-3            epilogue: tcgen05.ld (warp w reads TMEM lanes 32w..32w+31)
+//                        and the stage-specific store (plain, hi/lo split, or
+//                        scaled by an elementwise factor then split)
+// Every mbarrier wait is bounded by a 1 s wall-clock limit; on expiry the
+// kernel records an error code, drains its outstanding copies (bounded),
+// frees its TMEM and returns.
+#pragma once
+
+#include <cuda.h>
+#include <cstdint>
+
+#include "axi_common.cuh"
+
+namespace axi_tc {
+
+constexpr int BM = 128;
+constexpr int BN = 128;
+constexpr int BKF = 32;                         // K floats per stage (128-byte rows)
+constexpr int NSTAGE = 3;
+constexpr int TILE_BYTES = BM * BKF * 4;        // 16 KB per operand tile
+constexpr int STAGE_BYTES = 4 * TILE_BYTES;     // A_hi, A_lo, B_hi, B_lo
+constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 + 256;
+constexpr int THREADS = 128;
+constexpr unsigned long long WAIT_NS = 1000000000ull;
+
+enum { MODE_PLAIN = 0, MODE_SPLIT = 1, MODE_SCALE_SPLIT = 2 };
+enum { ERR_PRODUCER = 1, ERR_MMA = 2, ERR_EPILOGUE = 3, ERR_DRAIN = 4 };
+
+// One GEMM problem. Tensor maps are encoded on the host (cuTensorMapEncodeTiled)
+// and live in global memory next to the job.
+struct TcJob {
+  CUtensorMap a_hi, a_lo, b_hi, b_lo;
+  float* c;            // output (MODE_PLAIN) or its hi part
+  float* c_lo;         // lo part (split modes)
+  const float* scale;  // elementwise factor, row-major (M, N) (MODE_SCALE_SPLIT)
+  int M, N, K, ldc;
+  int mode;
+};
+
+// TF32 split: hi keeps the top 19 bits, lo is the exact remainder.
+__device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
+  hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+  lo = x - hi;
+}
+
+// Host: encode a 2-D K-major FP32 operand (rows x K, row stride ld floats)
+// for 128-row x 32-float boxes with 128-byte swizzle. Returns AXI status.
+int encode_operand(CUtensorMap* map, const float* base, int rows, int K, int ld);
+
+// Host: launch the grouped kernel over `n_tiles` (job, m0, n0) tiles.
+int launch(const TcJob* jobs_dev, const int4* tiles_dev, int n_tiles, int* err_dev,
+           cudaStream_t s);
+
+}  // namespace axi_tc

@@ -45,6 +45,8 @@ class AxiCase(ctypes.Structure):
         ("gemm_work", ctypes.c_void_p), ("state", ctypes.c_void_p),
         ("partials", ctypes.c_void_p), ("history", ctypes.c_void_p),
         ("history_len", ctypes.c_int64),
+        ("omega_hi", ctypes.c_void_p), ("omega_lo", ctypes.c_void_p),
+        ("tc_basis", ctypes.c_void_p * 8), ("tc_work", ctypes.c_void_p * 4),
     ]
 
 
@@ -109,26 +111,53 @@ class AxiPlanInfo(ctypes.Structure):
     """Mirror of ``axi_plan_info`` in include/axisym_gb300.h."""
     _fields_ = [("n_cases", ctypes.c_int32), ("n_stencil_tiles", ctypes.c_int32),
                 ("n_gemm_tiles", ctypes.c_int32), ("elem_bytes", ctypes.c_int32),
-                ("bytes", ctypes.c_int64)]
+                ("bytes", ctypes.c_int64), ("flags", ctypes.c_int32),
+                ("n_tc_tiles", ctypes.c_int32 * 4), ("reserved", ctypes.c_int32)]
+
+
+PLAN_TENSOR_CORES = 1
+
+
+def tf32_split(x):
+    """TF32 hi part (low 13 mantissa bits of the FP32 value cleared) and the
+    FP32 remainder, from a float64 array."""
+    x32 = np.asarray(x, dtype=np.float32)
+    hi = (x32.view(np.uint32) & np.uint32(0xFFFFE000)).view(np.float32)
+    lo = (np.asarray(x, dtype=np.float64) - hi.astype(np.float64)).astype(np.float32)
+    return hi, lo
 
 
 class _Bases:
     """Spectral bases shared by all cases with the same (nr, nz, dx)."""
 
-    def __init__(self, nr, nz, dx, dtype, device):
+    def __init__(self, nr, nz, dx, dtype, device, tensor_cores=False):
         solver = FastDiagonalisationStokesSolver(nr, nz, dx, device=device)
         d = solver.engine.dev
         self.t = {k: d[k].to(dtype).contiguous() for k in
                   ("Er", "Er_inv_w", "EzinvT", "EzT", "inv_eig")}
+        self.tc = []
+        if tensor_cores:
+            h = solver.engine.host
+            # operands of the K-major tensor-core form (C = A B^T per stage):
+            # E_z^-1, E_r^-1 diag(r), E_z, E_r
+            for m in (h["EzinvT"].T, h["Er_inv_w"], h["EzT"].T, h["Er"]):
+                hi, lo = tf32_split(np.ascontiguousarray(m))
+                self.tc.append(torch.tensor(hi, device=device))
+                self.tc.append(torch.tensor(lo, device=device))
 
 
 class RigidEnsemble:
     """All cases resident on one GPU, advanced together."""
 
     def __init__(self, cases, precision="f64", device="cuda", history_steps=0,
-                 initial_vorticity=None):
+                 initial_vorticity=None, tensor_cores=None):
         if precision not in ("f64", "f32"):
             raise ValueError("precision must be 'f64' or 'f32'")
+        if tensor_cores is None:
+            tensor_cores = precision == "f32"
+        if tensor_cores and precision != "f32":
+            raise ValueError("tensor-core products are for the f32 engine")
+        self.tensor_cores = tensor_cores
         self.precision = precision
         self.dtype = torch.float64 if precision == "f64" else torch.float32
         self.device = torch.device(device)
@@ -148,7 +177,8 @@ class RigidEnsemble:
             Z, R = np.meshgrid(z, r)
             key = (c.nr, c.nz, c.dx)
             if key not in bases:
-                bases[key] = _Bases(c.nr, c.nz, c.dx, self.dtype, self.device)
+                bases[key] = _Bases(c.nr, c.nz, c.dx, self.dtype, self.device,
+                                    tensor_cores=tensor_cores)
             b = bases[key]
             if initial_vorticity is not None and initial_vorticity[k] is not None:
                 w0 = np.asarray(initial_vorticity[k], dtype=np.float64)
@@ -172,6 +202,12 @@ class RigidEnsemble:
                 gemm_work=torch.zeros(2 * c.nr * c.nz, **f),
                 partials=torch.zeros(((c.nr + 7) // 8) * ((c.nz + 31) // 32) + 8, **f64),
             )
+            if tensor_cores:
+                whi, wlo = tf32_split(w0)
+                t["omega_hi"] = torch.tensor(whi, device=self.device)
+                t["omega_lo"] = torch.tensor(wlo, device=self.device)
+                t["tc_work"] = [torch.zeros(c.nr * c.nz, dtype=torch.float32, device=self.device)
+                                for _ in range(4)]
             self.fields.append(t)
             s = self.structs[k]
             s.nr, s.nz, s.kill_width = c.nr, c.nz, c.kill_width
@@ -188,6 +224,13 @@ class RigidEnsemble:
                 setattr(s, name, t[name].data_ptr())
             for name, v in b.t.items():
                 setattr(s, name, v.data_ptr())
+            if tensor_cores:
+                s.omega_hi = t["omega_hi"].data_ptr()
+                s.omega_lo = t["omega_lo"].data_ptr()
+                for q in range(8):
+                    s.tc_basis[q] = b.tc[q].data_ptr()
+                for q in range(4):
+                    s.tc_work[q] = t["tc_work"][q].data_ptr()
             s.state = self.state[k].data_ptr()
             if self.history is not None:
                 s.history = self.history[k].data_ptr()
@@ -200,6 +243,7 @@ class RigidEnsemble:
         self.info = AxiPlanInfo()
         esize = 8 if precision == "f64" else 4
         N.check(lib.axi_plan_init(ctypes.addressof(self.structs), n, esize,
+                                  PLAN_TENSOR_CORES if tensor_cores else 0,
                                   ctypes.byref(self.info)), "plan_init")
         self.n_tiles = self.info.n_stencil_tiles
         self.plan = torch.empty(int(self.info.bytes), dtype=torch.uint8, device=self.device)
@@ -249,9 +293,28 @@ class RigidEnsemble:
         self.graph.replay()
 
     def status(self):
-        """Sticky status bits per case (0 = healthy)."""
+        """Sticky status bits per case (0 = healthy); a tensor-core pipeline
+        failure marks every case with bit 1 << AXI_ERR_CUDA."""
         st = self.state[:, ST_STATUS].cpu().numpy().view(np.uint64)
-        return (st & 0xFFFFFFFF).astype(np.int64)
+        out = (st & 0xFFFFFFFF).astype(np.int64)
+        if self.tensor_cores:
+            err = ctypes.c_int(0)
+            N.check(N.lib().axi_plan_tc_status(
+                ctypes.byref(self.info), ctypes.c_void_p(self.plan.data_ptr()),
+                ctypes.byref(err), ctypes.c_void_p(
+                    torch.cuda.current_stream(self.device).cuda_stream)), "plan_tc_status")
+            if err.value:
+                out |= 1 << N.AXI_ERR_CUDA
+        return out
+
+    def set_vorticity(self, k, w):
+        """Replace the vorticity of case k (keeps the tensor-core operand copy in step)."""
+        self.fields[k]["omega"].copy_(w)
+        if self.tensor_cores:
+            x = self.fields[k]["omega"]
+            hi = (x.view(torch.int32) & -8192).view(torch.float32)
+            self.fields[k]["omega_hi"].copy_(hi)
+            self.fields[k]["omega_lo"].copy_(x - hi)
 
     def vorticity(self, k):
         return self.fields[k]["omega"]

@@ -97,3 +97,26 @@ def test_engine_f32_error_vs_fp64_oracle():
                                  ("u_z", ref.u_z), ("u_r", ref.u_r))}
     print("f32 rel L2 vs FP64 oracle after", steps, "steps:", errs)
     assert max(errs.values()) < 1e-4, errs
+
+
+def test_engine_f32_tensor_cores_error_vs_fp64_oracle():
+    """FP32 engine with the spectral products on tcgen05 (3xTF32): error vs the
+    FP64 oracle stays at the FP32 level; same case set alone vs batched."""
+    from pyaxisymflow_gb300.engine import RigidBodyCase, RigidEnsemble
+    c = RigidBodyCase(nz=256, nr=128, dx=2.0 / 256, r_sphere=0.0625)
+    steps = 50
+    ref, _ = run_oracle(c, steps)
+    e = RigidEnsemble([c], precision="f32", tensor_cores=True)
+    e.step(steps)
+    torch.cuda.synchronize()
+    assert e.status()[0] == 0
+    errs = {name: rel_l2(e.fields[0][name].double().cpu().numpy(), theirs)
+            for name, theirs in (("omega", ref.vorticity), ("psi", ref.psi),
+                                 ("u_z", ref.u_z), ("u_r", ref.u_r))}
+    print("f32 tensor-core rel L2 vs FP64 oracle after", steps, "steps:", errs)
+    assert max(errs.values()) < 1e-5, errs
+    simt = RigidEnsemble([c], precision="f32", tensor_cores=False)
+    simt.step(steps)
+    d = rel_l2(e.fields[0]["omega"].double().cpu().numpy(),
+               simt.fields[0]["omega"].double().cpu().numpy())
+    assert d < 1e-5, d
