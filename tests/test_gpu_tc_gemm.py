@@ -25,8 +25,10 @@ def test_tf32x3_gemm_matches_fp64(M, N, K):
     B = torch.randn((N, K), generator=g, dtype=torch.float64)
     ref = A @ B.T
     C = tc_gemm(A.float().cuda(), B.float().cuda()).double().cpu()
-    # FP32-rounded inputs: compare with the product of the rounded inputs
+    # FP32-rounded inputs: compare with the exact product of the rounded
+    # inputs. 3xTF32 with FP32 accumulation lands at the FP32 level (~1e-6 for
+    # K in the hundreds); a single TF32 product would be ~1e-3.
     ref32 = A.float().double() @ B.float().double().T
     err = ((C - ref32).norm() / ref32.norm()).item()
-    assert err < 2e-6, err
+    assert err < 1e-5, err
     assert ((C - ref).norm() / ref.norm()).item() < 1e-5
