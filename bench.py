@@ -250,7 +250,8 @@ def run_gb300(args, world, rank, local):
     for _ in range(args.steps):
         # host-resident vorticity in, one step, vorticity and (dt, Cd) back out
         for k in range(len(cases)):
-            ens.set_vorticity(k, host_w[k].view(cases[k].nr, cases[k].nz).to(dev, non_blocking=True))
+            ens.fields[k]["omega"].view(-1).copy_(host_w[k], non_blocking=True)
+        ens.refresh_operands()
         ens.step(1)
         for k in range(len(cases)):
             host_w[k].copy_(ens.fields[k]["omega"].view(-1), non_blocking=True)

@@ -345,7 +345,7 @@ typedef struct axi_case {
 /* Launch plan of a set of cases: tile tables in device memory. */
 typedef struct axi_plan_info {
   int32_t n_cases;
-  int32_t n_stencil_tiles; /* 32 x 8 cell tiles over all cases */
+  int32_t n_stencil_tiles; /* 64 x 16 cell tiles over all cases */
   int32_t n_gemm_tiles;    /* output tiles of the grouped spectral products */
   int32_t elem_bytes;      /* 8: float64 fields, 4: float32 fields */
   int64_t bytes;           /* device bytes the plan needs */
@@ -361,6 +361,9 @@ enum { AXI_PLAN_TENSOR_CORES = 1 };
  * AXI_PLAN_TENSOR_CORES (FP32 only) runs the spectral products as tcgen05
  * 3xTF32 GEMMs (the tc_* and omega_hi / omega_lo members must be set). */
 int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, int flags, axi_plan_info* info);
+/* Tensor-core plans: recompute the TF32 operand copy of omega (omega_hi,
+ * omega_lo) of every case after the caller overwrote omega. */
+int axi_rigid_refresh_operands(const axi_plan_info* info, const void* plan_dev, void* stream);
 /* Pipeline status of the tensor-core products since the plan was uploaded
  * (0 = healthy; otherwise a wait timed out). Synchronises the stream. */
 int axi_plan_tc_status(const axi_plan_info* info, const void* plan_dev, int* tc_error,

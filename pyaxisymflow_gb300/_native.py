@@ -54,6 +54,7 @@ def _signatures():
         "axi_tf32x3_gemm": (I, [P, P, P, I, I, I, P, P]),
         "axi_plan_init": (I, [P, I, I, I, P]),
         "axi_plan_tc_status": (I, [P, P, P, P]),
+        "axi_rigid_refresh_operands": (I, [P, P, P]),
         "axi_plan_upload": (I, [P, P, P, P]),
         "axi_rigid_step_f64": (I, [P, P, I, P]),
         "axi_rigid_step_f32": (I, [P, P, I, P]),

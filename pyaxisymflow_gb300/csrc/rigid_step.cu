@@ -31,9 +31,12 @@
 
 namespace {
 
-constexpr int TX = 32;
-constexpr int TY = 8;
-constexpr int NT = TX * TY;
+// Stencil tiles: 64 x 16 cells per 256-thread block (4 cells per thread,
+// warps along the contiguous z axis).
+constexpr int TX = 64;
+constexpr int TY = 16;
+constexpr int NT = 256;
+constexpr int CPT = TX * TY / NT;
 constexpr double kPi = 3.141592653589793;
 
 template <typename T>
@@ -147,29 +150,36 @@ __device__ __forceinline__ void velocity_at(const axi_case& k, Acc psi, int i, i
 // the last tile of the case derives dt and the per-step constants.
 // ---------------------------------------------------------------------------
 template <typename T>
+__device__ __forceinline__ unsigned long long order_bits(T v) {
+  // non-negative values order like their bit patterns; a NaN sorts above +inf
+  return sizeof(T) == 8 ? (unsigned long long)__double_as_longlong((double)v)
+                        : (unsigned long long)__float_as_uint((float)v);
+}
+
+template <typename T>
 __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict__ cases,
                                                      const int4* __restrict__ tiles) {
   __shared__ unsigned long long wm[NT / 32];
   __shared__ bool last;
   const int4 tr = tiles[blockIdx.x];
   const axi_case& k = cases[tr.x];
-  const int i = tr.y + threadIdx.x / TX;
-  const int j = tr.z + threadIdx.x % TX;
   const int nr = k.nr, nz = k.nz;
   const T* psi = CF<T>(k.psi);
+  const T* rinv2dx = CF<T>(k.rinv2dx);
   const T ufree = (T)k.state[AXI_ST_UFREE];
-  T v = T(0);
-  if (i < nr && j < nz) {
-    auto acc = [&](int a, int b) { return psi[(long long)a * nz + b]; };
-    T uz, ur;
-    velocity_at<T>(k, acc, i, j, CF<T>(k.rinv2dx)[i], ufree, uz, ur);
-    v = fabs(uz) + fabs(ur);
+  auto acc = [&](int a, int b) { return psi[(long long)a * nz + b]; };
+  unsigned long long bits = 0;
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) {
+    const int e = threadIdx.x + q * NT;
+    const int i = tr.y + e / TX, j = tr.z + e % TX;
+    if (i < nr && j < nz) {
+      T uz, ur;
+      velocity_at<T>(k, acc, i, j, rinv2dx[i], ufree, uz, ur);
+      const unsigned long long b = order_bits<T>(fabs(uz) + fabs(ur));
+      bits = b > bits ? b : bits;
+    }
   }
-  // Non-negative values order like their bit patterns (a NaN sorts above
-  // +inf, so it propagates to the maximum).
-  unsigned long long bits = sizeof(T) == 8
-                                ? (unsigned long long)__double_as_longlong((double)v)
-                                : (unsigned long long)__float_as_uint((float)v);
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long other = __shfl_down_sync(0xffffffffu, bits, o);
     bits = other > bits ? other : bits;
@@ -255,8 +265,14 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
   }
   __syncthreads();
   T cd_part = T(0);
-  {
-    const int a = threadIdx.x / TX, b = threadIdx.x % TX;
+  T* uzp = F<T>(k.u_z);
+  T* urp = F<T>(k.u_r);
+  T* w = F<T>(k.omega);
+  const T* rw = CF<T>(k.rw);
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) {
+    const int e = threadIdx.x + q * NT;
+    const int a = e / TX, b = e % TX;
     const int gi = i0 + a, gj = j0 + b;
     if (gi < nr && gj < nz) {
       const long long c = (long long)gi * nz + gj;
@@ -264,18 +280,17 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
       T uz, ur, pz, pr;
       velocity_at<T>(k, sp, gi, gj, rinv2dx[gi], ufree, uz, ur);
       penalise_point<T>(uz, ur, lamdt * ch, ubody, pz, pr);
-      F<T>(k.u_z)[c] = pz;
-      F<T>(k.u_r)[c] = pr;
-      cd_part = CF<T>(k.rw)[gi] * ch * pz;  // drag integrand r chi u_z
+      uzp[c] = pz;
+      urp[c] = pr;
+      cd_part += rw[gi] * ch * pz;  // drag integrand r chi u_z
       if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
         const T pw = (dur[a + 1][b + 2] - dur[a + 1][b]) * inv2dx -
                      (duz[a + 2][b + 1] - duz[a][b + 1]) * inv2dx;
-        T* w = F<T>(k.omega);
         w[c] = w[c] + pw;
       }
     }
   }
-  // drag: warp sums in T, then warps and tiles in double, fixed order
+  // drag: thread and warp sums in T, then warps and tiles in double, fixed order
   T x = cd_part;
   for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)x;
@@ -389,20 +404,28 @@ __global__ void __launch_bounds__(NT) adv_diff1_kernel(const axi_case* __restric
     wa[p][q] = val;
   }
   __syncthreads();
-  const int p = threadIdx.x / TX, q = threadIdx.x % TX;
-  const int gi = i0 + p, gj = j0 + q;
-  if (gi < nr && gj < nz) {
-    const T c0 = wa[p + 1][q + 1];
-    T tmp = c0;
-    if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
-      const T n = wa[p + 2][q + 1], s = wa[p][q + 1], e = wa[p + 1][q + 2], ww = wa[p + 1][q];
-      const T lap = (n + s + e + ww - T(4) * c0) * inv_dx2 + (n - s) * CF<T>(k.rinv2dx)[gi] -
-                    c0 * CF<T>(k.rinv2)[gi];
-      tmp = c0 + c1 * lap;
+  const T* rinv2dx = CF<T>(k.rinv2dx);
+  const T* rinv2 = CF<T>(k.rinv2);
+  T* wadv = F<T>(k.w_adv);
+  T* wtmp = F<T>(k.w_tmp);
+#pragma unroll
+  for (int qq = 0; qq < CPT; ++qq) {
+    const int e = threadIdx.x + qq * NT;
+    const int p = e / TX, q = e % TX;
+    const int gi = i0 + p, gj = j0 + q;
+    if (gi < nr && gj < nz) {
+      const T c0 = wa[p + 1][q + 1];
+      T tmp = c0;
+      if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
+        const T n = wa[p + 2][q + 1], s = wa[p][q + 1], ee = wa[p + 1][q + 2], ww = wa[p + 1][q];
+        const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rinv2dx[gi] -
+                      c0 * rinv2[gi];
+        tmp = c0 + c1 * lap;
+      }
+      const long long c = (long long)gi * nz + gj;
+      wadv[c] = c0;
+      wtmp[c] = tmp;
     }
-    const long long c = (long long)gi * nz + gj;
-    F<T>(k.w_adv)[c] = c0;
-    F<T>(k.w_tmp)[c] = tmp;
   }
 }
 
@@ -415,23 +438,49 @@ __global__ void __launch_bounds__(NT) diff2_kernel(const axi_case* __restrict__ 
   const int4 tr = tiles[blockIdx.x];
   const axi_case& k = cases[tr.x];
   const int nr = k.nr, nz = k.nz;
-  const int gi = tr.y + threadIdx.x / TX, gj = tr.z + threadIdx.x % TX;
-  if (gi < nr && gj < nz) {
-    const long long c = (long long)gi * nz + gj;
-    const T* wa = CF<T>(k.w_adv);
-    const T* tm = CF<T>(k.w_tmp);
-    T v = wa[c];
-    if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
-      const T c0 = tm[c], n = tm[c + nz], s = tm[c - nz], e = tm[c + 1], ww = tm[c - 1];
-      const T lap = (n + s + e + ww - T(4) * c0) * (T)k.inv_dx2 +
-                    (n - s) * CF<T>(k.rinv2dx)[gi] - c0 * CF<T>(k.rinv2)[gi];
-      v = v + (T)k.state[AXI_ST_C2] * lap;
+  const T* wa = CF<T>(k.w_adv);
+  const T* tm = CF<T>(k.w_tmp);
+  const T* rinv2dx = CF<T>(k.rinv2dx);
+  const T* rinv2 = CF<T>(k.rinv2);
+  const T inv_dx2 = (T)k.inv_dx2;
+  const T c2 = (T)k.state[AXI_ST_C2];
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) {
+    const int e = threadIdx.x + q * NT;
+    const int gi = tr.y + e / TX, gj = tr.z + e % TX;
+    if (gi < nr && gj < nz) {
+      const long long c = (long long)gi * nz + gj;
+      T v = wa[c];
+      if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
+        const T c0 = tm[c], n = tm[c + nz], s = tm[c - nz], ee = tm[c + 1], ww = tm[c - 1];
+        const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rinv2dx[gi] -
+                      c0 * rinv2[gi];
+        v = v + c2 * lap;
+      }
+      store_omega<T>(k, c, v);
     }
-    store_omega<T>(k, c, v);
   }
   if (tr.w == 0 && threadIdx.x == 0) {
     k.state[AXI_ST_T] += k.state[AXI_ST_DT];
     k.state[AXI_ST_STEPS] += 1.0;
+  }
+}
+
+// Recomputes the TF32 hi / lo operand copy of omega from omega (after the
+// caller replaced omega).
+__global__ void __launch_bounds__(NT) refresh_split_kernel(const axi_case* __restrict__ cases,
+                                                           const int4* __restrict__ tiles) {
+  const int4 tr = tiles[blockIdx.x];
+  const axi_case& k = cases[tr.x];
+  if (!k.omega_hi) return;
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) {
+    const int e = threadIdx.x + q * NT;
+    const int gi = tr.y + e / TX, gj = tr.z + e % TX;
+    if (gi < k.nr && gj < k.nz) {
+      const long long c = (long long)gi * k.nz + gj;
+      store_omega<float>(k, c, static_cast<const float*>(k.omega)[c]);
+    }
   }
 }
 
@@ -851,6 +900,18 @@ extern "C" int axi_plan_upload(const axi_case* cases, const axi_plan_info* info,
       cudaStreamSynchronize(s) != cudaSuccess)
     return axi::launch_status("plan_upload");
   return AXI_OK;
+}
+
+extern "C" int axi_rigid_refresh_operands(const axi_plan_info* info, const void* plan_dev,
+                                          void* stream) {
+  axi::clear_error();
+  AXI_TRY(axi::check_ptr("rigid_refresh_operands", info, "info"));
+  AXI_TRY(axi::check_ptr("rigid_refresh_operands", plan_dev, "plan_dev"));
+  if (!(info->flags & AXI_PLAN_TENSOR_CORES)) return AXI_OK;
+  const PlanView v = plan_view(plan_dev, info);
+  refresh_split_kernel<<<info->n_stencil_tiles, NT, 0, axi::as_stream(stream)>>>(v.cases,
+                                                                                  v.stencil);
+  return axi::launch_status("rigid_refresh_operands");
 }
 
 extern "C" int axi_plan_tc_status(const axi_plan_info* info, const void* plan_dev, int* tc_error,

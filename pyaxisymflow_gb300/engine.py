@@ -200,7 +200,7 @@ class RigidEnsemble:
                 rinv2=torch.tensor(1.0 / (r * r), **f64).to(self.dtype),
                 rw=torch.tensor(r, **f64).to(self.dtype),
                 gemm_work=torch.zeros(2 * c.nr * c.nz, **f),
-                partials=torch.zeros(((c.nr + 7) // 8) * ((c.nz + 31) // 32) + 8, **f64),
+                partials=torch.zeros(((c.nr + 15) // 16) * ((c.nz + 63) // 64) + 8, **f64),
             )
             if tensor_cores:
                 whi, wlo = tf32_split(w0)
@@ -307,14 +307,19 @@ class RigidEnsemble:
                 out |= 1 << N.AXI_ERR_CUDA
         return out
 
+    def refresh_operands(self, stream=None):
+        """After writing omega of any case directly, recompute the tensor-core
+        operand copy of omega (one launch for all cases)."""
+        if self.tensor_cores:
+            s = stream if stream is not None else torch.cuda.current_stream(self.device)
+            N.check(N.lib().axi_rigid_refresh_operands(
+                ctypes.byref(self.info), ctypes.c_void_p(self.plan.data_ptr()),
+                ctypes.c_void_p(s.cuda_stream)), "rigid_refresh_operands")
+
     def set_vorticity(self, k, w):
         """Replace the vorticity of case k (keeps the tensor-core operand copy in step)."""
         self.fields[k]["omega"].copy_(w)
-        if self.tensor_cores:
-            x = self.fields[k]["omega"]
-            hi = (x.view(torch.int32) & -8192).view(torch.float32)
-            self.fields[k]["omega_hi"].copy_(hi)
-            self.fields[k]["omega_lo"].copy_(x - hi)
+        self.refresh_operands()
 
     def vorticity(self, k):
         return self.fields[k]["omega"]
