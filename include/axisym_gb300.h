@@ -265,6 +265,22 @@ int axi_fd_transform_f64(double* out, int ld_out, const double* in, int ld_in,
 int64_t axi_tf32x3_gemm_work_bytes(int M, int N, int K);
 int axi_tf32x3_gemm(float* C, const float* A, const float* B, int M, int N, int K, void* work,
                     void* stream);
+/* Allocation-free form of axi_fd_transform_f64 (no counterpart in the
+ * reference). For callers that cannot call cudaMalloc: code that captures its
+ * time loop into a CUDA graph, or a host whose device memory is owned by
+ * another allocator. The two intermediate products live in a device array
+ * inside this library, sized for nr * nz <= axi_fd_transform_static_max_cells()
+ * (512 x 1024 cells, 8 MiB, resident on every GPU that loads the library until
+ * the process exits); larger grids are rejected with AXI_ERR_INVALID. The
+ * first call on each device looks up the array's device address (with that
+ * device current): make that first call before any stream capture. All calls
+ * share the array, so calls that overlap on the GPU (other streams, other
+ * host threads) race; serialise them on one stream. Nothing is allocated. */
+int64_t axi_fd_transform_static_max_cells(void);
+int axi_fd_transform_static_f64(double* out, int ld_out, const double* in, int ld_in,
+                                const double* Er_inv_w, const double* EzinvT,
+                                const double* inv_eig, const double* Er, const double* EzT,
+                                int nr, int nz, void* stream);
 /* Row-major double GEMM C = A(M,K) * B(K,N) (.* S(M,N) if S != NULL), row
  * strides ldc, lda, ldb; S is dense (row stride N). */
 int axi_dgemm_f64(double* C, int ldc, const double* A, int lda, const double* B, int ldb,

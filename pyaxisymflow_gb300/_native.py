@@ -49,6 +49,8 @@ def _signatures():
         "axi_extrapolate_eta_with_least_squares_f64": (
             I, [P, P, P, P, P, P, P, P, P, D, I, I, P, P, I, P, P, P]),
         "axi_fd_transform_f64": (I, [P, I, P, I, P, P, P, P, P, P, I, I, P]),
+        "axi_fd_transform_static_max_cells": (I64, []),
+        "axi_fd_transform_static_f64": (I, [P, I, P, I, P, P, P, P, P, I, I, P]),
         "axi_dgemm_f64": (I, [P, I, P, I, P, I, P, I, I, I, P]),
         "axi_tf32x3_gemm_work_bytes": (I64, [I, I, I]),
         "axi_tf32x3_gemm": (I, [P, P, P, I, I, I, P, P]),

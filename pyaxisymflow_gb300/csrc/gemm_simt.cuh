@@ -94,16 +94,22 @@ inline int gemm(T* C, int ldc, const T* A, int lda, const T* B, int ldb, const T
 // out = Er ((Er_inv_w in EzinvT) .* inv_eig) EzT, keeping the reference's
 // association A (B C) (kernels/FastDiagonalisationStokesSolver.py:137-156).
 template <typename T>
-inline int fd_transform(T* out, int ld_out, const T* in, int ld_in, const T* Er_inv_w,
-                        const T* EzinvT, const T* inv_eig, const T* Er, const T* EzT, T* work,
-                        int nr, int nz, cudaStream_t s) {
-  T* w1 = work;
-  T* w2 = work + (size_t)nr * nz;
+inline int fd_transform_split(T* out, int ld_out, const T* in, int ld_in, const T* Er_inv_w,
+                              const T* EzinvT, const T* inv_eig, const T* Er, const T* EzT, T* w1,
+                              T* w2, int nr, int nz, cudaStream_t s) {
   AXI_TRY(gemm<T>(w1, nz, in, ld_in, EzinvT, nz, nullptr, nr, nz, nz, s));   // in E_z^-T
   AXI_TRY(gemm<T>(w2, nz, Er_inv_w, nr, w1, nz, inv_eig, nr, nz, nr, s));   // E_r^-1 (.) ./ L
   AXI_TRY(gemm<T>(w1, nz, w2, nz, EzT, nz, nullptr, nr, nz, nz, s));        // (.) E_z^T
   AXI_TRY(gemm<T>(out, ld_out, Er, nr, w1, nz, nullptr, nr, nz, nr, s));    // E_r (.)
   return AXI_OK;
+}
+
+template <typename T>
+inline int fd_transform(T* out, int ld_out, const T* in, int ld_in, const T* Er_inv_w,
+                        const T* EzinvT, const T* inv_eig, const T* Er, const T* EzT, T* work,
+                        int nr, int nz, cudaStream_t s) {
+  return fd_transform_split<T>(out, ld_out, in, ld_in, Er_inv_w, EzinvT, inv_eig, Er, EzT, work,
+                               work + (size_t)nr * nz, nr, nz, s);
 }
 
 }  // namespace axi_gemm
