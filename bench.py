@@ -8,9 +8,10 @@ of examples/FlowPastSphere/flow_past_sphere.py:107-188). value = cell-updates
 per second over the whole job (all ranks): cells of all cases x steps / time.
 
 Workloads (synthetic, seeded; there is no dataset):
-  ensemble64  64 rigid-sphere cases, nz in {256, 512, 768, 1024}, nr = nz / 2,
-              z in [0, 2], r in [0, 1], Re log-uniform in [10, 1000], sphere
-              radius uniform in [0.04, 0.12], seed 4
+  ensemble64  64 freely sedimenting rigid spheres, nz in {256, 512, 768, 1024},
+              nr = nz / 2, z in [0, 2], r in [0, 1], Re log-uniform in
+              [10, 1000] (velocity scale 1), sphere radius uniform in
+              [0.04, 0.12], density ratio uniform in [1.5, 4], seed 4
   sphere512   one 512 x 256 rigid sphere, Re 100, radius 0.0625 at z = 0.5
 
 --impl reference times the reference's CPU path restated by the oracle
@@ -50,8 +51,10 @@ def ensemble_cases(workload, seed=4):
         nz = int(rng.choice([256, 512, 768, 1024]))
         Re = float(np.exp(rng.uniform(np.log(10.0), np.log(1000.0))))
         radius = float(rng.uniform(0.04, 0.12))
+        ratio = float(rng.uniform(1.5, 4.0))
         cases.append(RigidBodyCase(nz=nz, nr=nz // 2, dx=2.0 / nz, r_sphere=radius, Re=Re,
-                                   z_cm=0.5, seed=1000 + k))
+                                   z_cm=1.5, U0=0.0, ramp=False, sediment=True, rho_s=ratio,
+                                   seed=1000 + k))
     return cases
 
 
@@ -142,18 +145,29 @@ def cpu_oracle_rate(cases, steps):
     from oracle import simulation as sim
     runs = []
     for c in cases:
-        oc = sim.RigidSphereCase(nz=c.nz, nr=c.nr, dx=c.dx, z_cm=c.z_cm, r_sphere=c.r_sphere,
-                                 U0=c.U0, Re=c.Re, lam=c.lam, cfl=c.cfl, kill_width=c.kill_width,
-                                 ramp=c.ramp, noise=c.noise, seed=c.seed)
-        st, coords = sim.rigid_sphere_init(oc, K)
+        if c.sediment:
+            oc = sim.SedimentingCase(nz=c.nz, nr=c.nr, dx=c.dx, z_cm=c.z_cm,
+                                     r_sphere=c.r_sphere, rho_f=c.rho_f, rho_s=c.rho_s,
+                                     nu=c.nu, lam=c.lam, cfl=c.cfl, kill_width=c.kill_width,
+                                     gravity=c.gravity)
+            w0 = c.noise * np.random.default_rng(c.seed).standard_normal((c.nr, c.nz))
+            st, coords = sim.sedimenting_init(oc, K, vorticity=w0)
+            step = sim.sedimenting_step
+        else:
+            oc = sim.RigidSphereCase(nz=c.nz, nr=c.nr, dx=c.dx, z_cm=c.z_cm,
+                                     r_sphere=c.r_sphere, U0=c.U0, Re=c.Re, lam=c.lam,
+                                     cfl=c.cfl, kill_width=c.kill_width, ramp=c.ramp,
+                                     noise=c.noise, seed=c.seed)
+            st, coords = sim.rigid_sphere_init(oc, K)
+            step = sim.rigid_sphere_step
         solver = K.FastDiagonalisationStokesSolver(oc.nr, oc.nz, oc.dx)
         adv = K.gen_advect_vorticity_via_eno3(oc.dx, oc.nr, oc.nz)
-        runs.append((oc, st, coords, solver, adv))
+        runs.append((oc, st, coords, solver, adv, step))
     cells = 0
     t0 = time.perf_counter()
     for _ in range(steps):
-        for oc, st, coords, solver, adv in runs:
-            sim.rigid_sphere_step(oc, st, coords, solver, adv, K)
+        for oc, st, coords, solver, adv, step in runs:
+            step(oc, st, coords, solver, adv, K)
             cells += oc.nr * oc.nz
     dt = time.perf_counter() - t0
     return cells / dt, dt, cells

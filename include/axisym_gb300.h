@@ -313,19 +313,33 @@ enum {
   AXI_ST_ADV = 10,     /* -dt / dx (ENO3 flux factor) */
   AXI_ST_C1 = 11,      /* 0.5 nu dt (RK2 stage 1) */
   AXI_ST_C2 = 12,      /* nu dt (RK2 stage 2) */
-  AXI_ST_WORDS = 16
+  AXI_ST_ZCM = 13,     /* sedimenting body: centre z */
+  AXI_ST_UBODY = 14,   /* sedimenting body: velocity along z */
+  AXI_ST_DIFF = 15,    /* sedimenting body: last velocity increment (unsteady force) */
+  AXI_ST_FTOTAL = 16,  /* sedimenting body: last total force */
+  AXI_ST_WORDS = 24
 };
+
+enum { AXI_CASE_SEDIMENTING = 1 };
 
 /* One flow-past-rigid-body case. Fields are (nr, nz) row-major in the engine
  * precision (double for _f64, float for _f32); rinv2dx, rinv2 and rw are
- * per-row vectors (length nr) in the engine precision; r and z are double
- * vectors of length nr and nz. */
+ * per-row vectors (length nr) and zw a per-column vector (length nz) in the
+ * engine precision; r and z are double vectors of length nr and nz. partials
+ * holds 2 doubles per stencil tile of the case. */
 typedef struct axi_case {
   int32_t nr, nz;
   int32_t kill_width;
   int32_t stencil_tile0; /* first stencil tile of this case in the plan */
   double dx, nu, lam, U0, t_ramp, cfl, U_body, cd_scale, dt_diff, eps;
   double inv_dx2, inv_2dx;
+  /* AXI_CASE_SEDIMENTING: a rigid sphere of radius r_body falling along z
+   * (examples/SedimentingRigidSphere/falling_rigid_sphere.py:136-181): the
+   * Brinkman target is the body velocity, the force integral and the body ODE
+   * run on the device in FP64 and the mask is rebuilt every step. */
+  int32_t flags;
+  int32_t pad0;
+  double rho_f, rho_s, grav, part_mass, part_vol, r_body, blend_w;
   void* omega;
   void* psi;
   void* u_z;
@@ -338,6 +352,7 @@ typedef struct axi_case {
   const void* rinv2dx;   /* 1 / (2 dx r_i) */
   const void* rinv2;     /* 1 / r_i^2 */
   const void* rw;        /* r_i (drag weight) */
+  const void* zw;        /* z_j */
   const void* Er;        /* (nr, nr) */
   const void* Er_inv_w;  /* (nr, nr), E_r^-1 diag(r) */
   const void* EzinvT;    /* (nz, nz) */

@@ -239,7 +239,8 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
   const T* rinv2dx = CF<T>(k.rinv2dx);
   const T ufree = (T)k.state[AXI_ST_UFREE];
   const T lamdt = (T)k.state[AXI_ST_LAMDT];
-  const T ubody = (T)k.U_body;
+  const bool sediment = (k.flags & AXI_CASE_SEDIMENTING) != 0;
+  const T ubody = (T)(sediment ? k.state[AXI_ST_UBODY] : k.U_body);
   const T inv2dx = (T)k.inv_2dx;
   for (int e = threadIdx.x; e < (TY + 4) * (TX + 4); e += NT) {
     const int a = e / (TX + 4), b = e % (TX + 4);
@@ -282,7 +283,9 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
       penalise_point<T>(uz, ur, lamdt * ch, ubody, pz, pr);
       uzp[c] = pz;
       urp[c] = pr;
-      cd_part += rw[gi] * ch * pz;  // drag integrand r chi u_z
+      // drag / penalisation force integrand r chi (u_z - U_body)
+      // (flow_past_sphere.py:173, compute_forces.py:14)
+      cd_part += rw[gi] * ch * (pz - ubody);
       if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
         const T pw = (dur[a + 1][b + 2] - dur[a + 1][b]) * inv2dx -
                      (duz[a + 2][b + 1] - duz[a][b + 1]) * inv2dx;
@@ -308,17 +311,24 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
     __threadfence();
     double sum = 0.0;
     for (unsigned int q = 0; q < ntiles; ++q) sum += ((volatile double*)k.partials)[q];
-    const double cd = k.cd_scale * sum;
-    if (!(cd == cd) || !(fabs(cd) <= 1.7976931348623157e308))
-      atomicOr(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_STATUS]), 1u << AXI_ERR_NONFINITE);
     const double dt = k.state[AXI_ST_DT];
-    const long long step = (long long)k.state[AXI_ST_STEPS];
-    if (k.history && step < k.history_len) {
-      k.history[2 * step] = dt;
-      k.history[2 * step + 1] = cd;
-    }
-    k.state[AXI_ST_CD] = cd;
+    if (!(sum == sum) || !(fabs(sum) <= 1.7976931348623157e308))
+      atomicOr(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_STATUS]), 1u << AXI_ERR_NONFINITE);
     k.state[AXI_ST_FORCE] = sum;
+    if (sediment) {
+      // compute_forces.py:14-15 and falling_rigid_sphere.py:155
+      const double f_pen = k.rho_f * k.lam * sum;
+      const double f_un = (k.state[AXI_ST_DIFF] * k.part_vol) / dt;
+      k.state[AXI_ST_FTOTAL] = 2.0 * kPi * k.dx * k.dx * f_pen + f_un;
+    } else {
+      const double cd = k.cd_scale * sum;
+      const long long step = (long long)k.state[AXI_ST_STEPS];
+      if (k.history && step < k.history_len) {
+        k.history[2 * step] = dt;
+        k.history[2 * step + 1] = cd;
+      }
+      k.state[AXI_ST_CD] = cd;
+    }
   }
 }
 
@@ -432,9 +442,22 @@ __global__ void __launch_bounds__(NT) adv_diff1_kernel(const axi_case* __restric
 // ---------------------------------------------------------------------------
 // diff2: RK2 stage 2 (kernels/diffusion_RK2.py:27-44); advances the time
 // ---------------------------------------------------------------------------
+// Smoothed Heaviside of a sphere level set (kernels/smooth_Heaviside.py:10-14,
+// level set of falling_rigid_sphere.py:156).
+template <typename T>
+__device__ __forceinline__ T sphere_mask(T z, T r, T zc, T radius, T w) {
+  const T dz = z - zc;
+  const T phi = -sqrt(dz * dz + r * r) + radius;
+  T h = phi >= w ? T(1) : T(0);
+  if (fabs(phi) < w) h += T(0.5) * (T(1) + phi / w + dev_sin(Pi<T>::v * phi / w) / Pi<T>::v);
+  return h;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(NT) diff2_kernel(const axi_case* __restrict__ cases,
                                                    const int4* __restrict__ tiles) {
+  __shared__ double red[NT / 32];
+  __shared__ bool last;
   const int4 tr = tiles[blockIdx.x];
   const axi_case& k = cases[tr.x];
   const int nr = k.nr, nz = k.nz;
@@ -444,6 +467,9 @@ __global__ void __launch_bounds__(NT) diff2_kernel(const axi_case* __restrict__ 
   const T* rinv2 = CF<T>(k.rinv2);
   const T inv_dx2 = (T)k.inv_dx2;
   const T c2 = (T)k.state[AXI_ST_C2];
+  const bool sediment = (k.flags & AXI_CASE_SEDIMENTING) != 0;
+  const T zc = (T)k.state[AXI_ST_ZCM];
+  T cd_part = T(0);
 #pragma unroll
   for (int q = 0; q < CPT; ++q) {
     const int e = threadIdx.x + q * NT;
@@ -458,10 +484,58 @@ __global__ void __launch_bounds__(NT) diff2_kernel(const axi_case* __restrict__ 
         v = v + c2 * lap;
       }
       store_omega<T>(k, c, v);
+      if (sediment) {
+        // mask at the body position of this step (falling_rigid_sphere.py:156-157),
+        // then the drag integrand with the new mask (:164-173)
+        const T ch = sphere_mask<T>(CF<T>(k.zw)[gj], CF<T>(k.rw)[gi], zc, (T)k.r_body,
+                                    (T)k.blend_w);
+        F<T>(k.chi)[c] = ch;
+        cd_part += CF<T>(k.rw)[gi] * ch * CF<T>(k.u_z)[c];
+      }
     }
   }
-  if (tr.w == 0 && threadIdx.x == 0) {
-    k.state[AXI_ST_T] += k.state[AXI_ST_DT];
+  if (!sediment) {
+    if (tr.w == 0 && threadIdx.x == 0) {
+      k.state[AXI_ST_T] += k.state[AXI_ST_DT];
+      k.state[AXI_ST_STEPS] += 1.0;
+    }
+    return;
+  }
+  T x = cd_part;
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)x;
+  __syncthreads();
+  const unsigned int ntiles = dev_tiles_of(k);
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int q = 0; q < NT / 32; ++q) sum += red[q];
+    k.partials[ntiles + tr.w] = sum;
+    __threadfence();
+    last = (atomicAdd(counter(k, 1), 1u) == 2 * ntiles - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double sum = 0.0;
+    for (unsigned int q = 0; q < ntiles; ++q) sum += ((volatile double*)k.partials)[ntiles + q];
+    const double cd = k.cd_scale * sum;
+    const double dt = k.state[AXI_ST_DT];
+    // body ODE, falling_rigid_sphere.py:176-181 (FP64)
+    const double ft = k.state[AXI_ST_FTOTAL];
+    const double u_old = k.state[AXI_ST_UBODY];
+    const double acc = -k.grav / k.rho_s + ft / k.part_mass;
+    k.state[AXI_ST_UBODY] = u_old + dt * (-k.grav + ft / k.part_mass);
+    k.state[AXI_ST_DIFF] = dt * acc;
+    k.state[AXI_ST_ZCM] = k.state[AXI_ST_ZCM] + u_old * dt + 0.5 * dt * dt * acc;
+    if (!(cd == cd) || !(ft == ft))
+      atomicOr(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_STATUS]), 1u << AXI_ERR_NONFINITE);
+    const long long step = (long long)k.state[AXI_ST_STEPS];
+    if (k.history && step < k.history_len) {
+      k.history[2 * step] = dt;
+      k.history[2 * step + 1] = cd;
+    }
+    k.state[AXI_ST_CD] = cd;
+    k.state[AXI_ST_T] += dt;
     k.state[AXI_ST_STEPS] += 1.0;
   }
 }
@@ -747,7 +821,7 @@ int validate(const axi_case* cases, int n_cases, const char* what) {
       return AXI_ERR_INVALID;
     }
     const void* ptrs[] = {k.omega, k.psi, k.u_z, k.u_r, k.chi, k.w_adv, k.w_tmp, k.r, k.z,
-                          k.rinv2dx, k.rinv2, k.rw, k.Er, k.Er_inv_w, k.EzinvT, k.EzT,
+                          k.rinv2dx, k.rinv2, k.rw, k.zw, k.Er, k.Er_inv_w, k.EzinvT, k.EzT,
                           k.inv_eig, k.gemm_work, k.state, k.partials};
     for (const void* p : ptrs) {
       if (!p) {

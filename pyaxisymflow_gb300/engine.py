@@ -21,8 +21,9 @@ from .kernels.FastDiagonalisationStokesSolver import FastDiagonalisationStokesSo
 from .kernels.smooth_Heaviside import smooth_Heaviside
 
 ST_T, ST_DT, ST_CD, ST_STEPS, ST_UMAX, ST_COUNT, ST_STATUS, ST_FORCE = range(8)
-ST_UFREE, ST_LAMDT, ST_ADV, ST_C1, ST_C2 = range(8, 13)
-ST_WORDS = 16
+ST_UFREE, ST_LAMDT, ST_ADV, ST_C1, ST_C2, ST_ZCM, ST_UBODY, ST_DIFF, ST_FTOTAL = range(8, 17)
+ST_WORDS = 24
+CASE_SEDIMENTING = 1
 
 
 class AxiCase(ctypes.Structure):
@@ -35,11 +36,15 @@ class AxiCase(ctypes.Structure):
         ("U_body", ctypes.c_double), ("cd_scale", ctypes.c_double),
         ("dt_diff", ctypes.c_double), ("eps", ctypes.c_double),
         ("inv_dx2", ctypes.c_double), ("inv_2dx", ctypes.c_double),
+        ("flags", ctypes.c_int32), ("pad0", ctypes.c_int32),
+        ("rho_f", ctypes.c_double), ("rho_s", ctypes.c_double), ("grav", ctypes.c_double),
+        ("part_mass", ctypes.c_double), ("part_vol", ctypes.c_double),
+        ("r_body", ctypes.c_double), ("blend_w", ctypes.c_double),
         ("omega", ctypes.c_void_p), ("psi", ctypes.c_void_p), ("u_z", ctypes.c_void_p),
         ("u_r", ctypes.c_void_p), ("chi", ctypes.c_void_p), ("w_adv", ctypes.c_void_p),
         ("w_tmp", ctypes.c_void_p),
         ("r", ctypes.c_void_p), ("z", ctypes.c_void_p), ("rinv2dx", ctypes.c_void_p),
-        ("rinv2", ctypes.c_void_p), ("rw", ctypes.c_void_p),
+        ("rinv2", ctypes.c_void_p), ("rw", ctypes.c_void_p), ("zw", ctypes.c_void_p),
         ("Er", ctypes.c_void_p), ("Er_inv_w", ctypes.c_void_p), ("EzinvT", ctypes.c_void_p),
         ("EzT", ctypes.c_void_p), ("inv_eig", ctypes.c_void_p),
         ("gemm_work", ctypes.c_void_p), ("state", ctypes.c_void_p),
@@ -73,14 +78,22 @@ class RigidBodyCase:
     aspect: float = 1.0        # spheroid: axial / radial semi-axis
     torus_R: float = 0.0       # torus: ring radius (r_sphere is the tube radius)
     U_body: float = 0.0
+    # freely sedimenting sphere (examples/SedimentingRigidSphere/falling_rigid_sphere.py):
+    # no free stream, body velocity / position integrated on the device
+    sediment: bool = False
+    rho_f: float = 1.0
+    rho_s: float = 1.1
+    gravity: float = 9.81
+    U_ref: float = 1.0         # velocity scale of Re when U0 = 0
 
     @property
     def nu(self):
-        return self.U0 * 2 * self.r_sphere / self.Re
+        u = self.U0 if self.U0 != 0 else self.U_ref
+        return u * 2 * self.r_sphere / self.Re
 
     @property
     def t_ramp(self):
-        return 20 * self.r_sphere / self.U0
+        return 20 * self.r_sphere / self.U0 if self.U0 != 0 else 0.0
 
     @property
     def moll_zone(self):
@@ -199,8 +212,9 @@ class RigidEnsemble:
                 rinv2dx=torch.tensor(1.0 / (2 * c.dx * r), **f64).to(self.dtype),
                 rinv2=torch.tensor(1.0 / (r * r), **f64).to(self.dtype),
                 rw=torch.tensor(r, **f64).to(self.dtype),
+                zw=torch.tensor(z, **f64).to(self.dtype),
                 gemm_work=torch.zeros(2 * c.nr * c.nz, **f),
-                partials=torch.zeros(((c.nr + 15) // 16) * ((c.nz + 63) // 64) + 8, **f64),
+                partials=torch.zeros(2 * ((c.nr + 15) // 16) * ((c.nz + 63) // 64) + 8, **f64),
             )
             if tensor_cores:
                 whi, wlo = tf32_split(w0)
@@ -219,8 +233,21 @@ class RigidEnsemble:
             s.eps = float(np.finfo(float).eps)
             s.inv_dx2 = 1.0 / (c.dx * c.dx)
             s.inv_2dx = 0.5 / c.dx
+            if c.sediment:
+                if c.body != "sphere":
+                    raise ValueError("sedimenting bodies are spheres")
+                # falling_rigid_sphere.py:71-73 (mass and volume from the initial mask)
+                chi_h = chi64.cpu().numpy()
+                s.flags = CASE_SEDIMENTING
+                s.rho_f, s.rho_s = c.rho_f, c.rho_s
+                s.grav = (c.rho_s - c.rho_f) * c.gravity
+                s.part_mass = 2 * np.pi * c.dx * c.dx * c.rho_s * np.sum(chi_h * R)
+                s.part_vol = 2 * np.pi * c.dx * c.dx * np.sum(chi_h * R)
+                s.r_body = c.r_sphere
+                s.blend_w = c.moll_zone
+                self.state[k, ST_ZCM] = c.z_cm
             for name in ("omega", "psi", "u_z", "u_r", "chi", "w_adv", "w_tmp", "r", "z",
-                         "rinv2dx", "rinv2", "rw", "gemm_work", "partials"):
+                         "rinv2dx", "rinv2", "rw", "zw", "gemm_work", "partials"):
                 setattr(s, name, t[name].data_ptr())
             for name, v in b.t.items():
                 setattr(s, name, v.data_ptr())

@@ -120,3 +120,34 @@ def test_engine_f32_tensor_cores_error_vs_fp64_oracle():
     d = rel_l2(e.fields[0]["omega"].double().cpu().numpy(),
                simt.fields[0]["omega"].double().cpu().numpy())
     assert d < 1e-5, d
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-11), ("f32", 1e-4)])
+def test_engine_sedimenting_sphere_matches_oracle(precision, tol):
+    """Freely sedimenting sphere (examples/SedimentingRigidSphere/falling_rigid_sphere.py):
+    moving mask, FP64 force integral and body ODE on the device."""
+    from pyaxisymflow_gb300.engine import (ST_UBODY, ST_ZCM, RigidBodyCase, RigidEnsemble)
+    nz, nr, steps = 128, 64, 40
+    oc = sim.SedimentingCase(nz=nz, nr=nr, dx=1.0 / nz, r_sphere=0.08, z_cm=0.6, nu=0.01,
+                             rho_s=1.5)
+    w0 = 1e-3 * np.random.default_rng(5).standard_normal((nr, nz))
+    st, coords = sim.sedimenting_init(oc, K, vorticity=w0)
+    solver = K.FastDiagonalisationStokesSolver(oc.nr, oc.nz, oc.dx)
+    adv = K.gen_advect_vorticity_via_eno3(oc.dx, oc.nr, oc.nz)
+    for _ in range(steps):
+        sim.sedimenting_step(oc, st, coords, solver, adv, K)
+    c = RigidBodyCase(nz=nz, nr=nr, dx=oc.dx, z_cm=oc.z_cm, r_sphere=oc.r_sphere, U0=0.0,
+                      ramp=False, Re=1.0 * 2 * oc.r_sphere / oc.nu, lam=oc.lam, cfl=oc.cfl,
+                      sediment=True, rho_f=oc.rho_f, rho_s=oc.rho_s, gravity=oc.gravity)
+    assert abs(c.nu - oc.nu) < 1e-15
+    e = RigidEnsemble([c], precision=precision, initial_vorticity=[w0])
+    e.step(steps)
+    torch.cuda.synchronize()
+    assert e.status()[0] == 0
+    s = e.state[0].cpu().numpy()
+    assert abs(s[ST_ZCM] - st.part_Z_cm) <= tol * abs(st.part_Z_cm)
+    assert abs(s[ST_UBODY] - st.U_z_cm_part) <= tol * abs(st.U_z_cm_part) + 1e-14
+    err = rel_l2(e.fields[0]["omega"].double().cpu().numpy(), st.vorticity)
+    assert err < tol * 10, err
+    chi_err = np.abs(e.fields[0]["chi"].double().cpu().numpy() - st.char_func).max()
+    assert chi_err < (1e-12 if precision == "f64" else 1e-5), chi_err
