@@ -140,35 +140,42 @@ __device__ __forceinline__ void store_value(const TcJob& job, int row, int col, 
   job.c_lo[idx] = lo;
 }
 
+// Persistent, warp-specialised kernel (one CTA per SM, tiles strided over the
+// grid): warp 0 issues TMA, warp 1 issues MMAs into one of two TMEM
+// accumulators (2 x 128 columns), warps 2-5 drain the other accumulator, so
+// the epilogue of a tile overlaps the main loop of the next one.
 __global__ void __launch_bounds__(THREADS, 1)
     tf32x3_gemm_kernel(const TcJob* __restrict__ jobs, const int4* __restrict__ tiles,
-                       int* __restrict__ err) {
+                       int n_tiles, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + NSTAGE * STAGE_BYTES);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * NSTAGE + 1);
-  int* progress = reinterpret_cast<int*>(tmem_slot + 1);  // [0] issued, [1] consumed
+  // full[NSTAGE], empty[NSTAGE], acc_full[2], acc_empty[2], quiet
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * NSTAGE + 5);
+  int* progress = reinterpret_cast<int*>(tmem_slot + 1);  // [0] loads issued, [1] consumed
+  float* stage_out = reinterpret_cast<float*>(smem + NSTAGE * STAGE_BYTES + 256);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int4 tr = tiles[blockIdx.x];
-  const TcJob& job = jobs[tr.x];
-  const int m0 = tr.y, n0 = tr.z;
-  const int nk = (job.K + BKF - 1) / BKF;
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + NSTAGE);
-  const uint32_t done = smem_u32(bars + 2 * NSTAGE);
+  const uint32_t accf0 = smem_u32(bars + 2 * NSTAGE), acce0 = smem_u32(bars + 2 * NSTAGE + 2);
+  const uint32_t quiet = smem_u32(bars + 2 * NSTAGE + 4);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NSTAGE; ++s) {
       mbar_init(full0 + 8 * s, 1);
       mbar_init(empty0 + 8 * s, 1);
     }
-    mbar_init(done, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(accf0 + 8 * b, 1);
+      mbar_init(acce0 + 8 * b, EPI_WARPS);
+    }
+    mbar_init(quiet, 1);
     progress[0] = 0;
     progress[1] = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    tmem_alloc(smem_u32(tmem_slot), BN);
+    tmem_alloc(smem_u32(tmem_slot), 2 * BN);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -176,83 +183,123 @@ __global__ void __launch_bounds__(THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0 && lane == 0) {
-    // ---- TMA producer ----
-    int kb = 0;
-    for (; kb < nk; ++kb) {
-      const int s = kb % NSTAGE, use = kb / NSTAGE;
-      if (use > 0 && !mbar_wait(empty0 + 8 * s, (use - 1) & 1, err, ERR_PRODUCER)) break;
-      const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
-      const uint32_t fb = full0 + 8 * s;
-      mbar_expect_tx(fb, STAGE_BYTES);
-      const int kx = kb * BKF;
-      tma_load_2d(st + 0 * TILE_BYTES, &job.a_hi, kx, m0, fb);
-      tma_load_2d(st + 1 * TILE_BYTES, &job.a_lo, kx, m0, fb);
-      tma_load_2d(st + 2 * TILE_BYTES, &job.b_hi, kx, n0, fb);
-      tma_load_2d(st + 3 * TILE_BYTES, &job.b_lo, kx, n0, fb);
-    }
-    progress[0] = kb;
-  } else if (warp == 1 && lane == 0) {
-    // ---- MMA issuer ----
-    constexpr uint32_t idesc = idesc_tf32(BM, BN);
-    int kb = 0;
-    for (; kb < nk; ++kb) {
-      const int s = kb % NSTAGE, use = kb / NSTAGE;
-      if (!mbar_wait(full0 + 8 * s, use & 1, err, ERR_MMA)) break;
-      tc_fence_after();
-      const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
-      const uint64_t ah = sw128_desc(st), al = sw128_desc(st + TILE_BYTES);
-      const uint64_t bh = sw128_desc(st + 2 * TILE_BYTES), bl = sw128_desc(st + 3 * TILE_BYTES);
-#pragma unroll
-      for (int kk = 0; kk < BKF / 8; ++kk) {
-        const uint64_t o = static_cast<uint64_t>(kk * 32) >> 4;  // 8 TF32 = 32 bytes
-        umma_tf32(tmem, ah + o, bh + o, idesc, (kb | kk) != 0 ? 1u : 0u);
-        umma_tf32(tmem, ah + o, bl + o, idesc, 1u);
-        umma_tf32(tmem, al + o, bh + o, idesc, 1u);
-      }
-      umma_commit(empty0 + 8 * s);
-    }
-    progress[1] = kb;
-    umma_commit(done);
-  }
-  __syncwarp();
-
-  // ---- epilogue ----
-  const bool ok = mbar_wait(done, 0, err, ERR_EPILOGUE);
-  tc_fence_after();
-  // tcgen05.ld is warp-collective: decide per warp
-  if (__all_sync(0xffffffffu, ok && *reinterpret_cast<volatile int*>(err) == 0)) {
-    const int row = m0 + warp * 32 + lane;
-    const bool vec = (job.ldc % 4) == 0 && job.mode == MODE_PLAIN;
-#pragma unroll 1
-    for (int cc = 0; cc < BN / 32; ++cc) {
-      uint32_t r[32];
-      tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + cc * 32, r);
-      if (row < job.M) {
-        const int col0 = n0 + cc * 32;
-        if (vec && col0 + 32 <= job.N) {
-          float4* dst = reinterpret_cast<float4*>(job.c + (long long)row * job.ldc + col0);
-#pragma unroll
-          for (int j = 0; j < 8; ++j)
-            dst[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]),
-                                 __uint_as_float(r[4 * j + 2]), __uint_as_float(r[4 * j + 3]));
-        } else {
-#pragma unroll
-          for (int j = 0; j < 32; ++j)
-            if (col0 + j < job.N) store_value(job, row, col0 + j, __uint_as_float(r[j]));
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer: one continuous ring over all tiles of this CTA ----
+      int g = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+        const int4 tr = tiles[t];
+        const TcJob& job = jobs[tr.x];
+        const int nk = (job.K + BKF - 1) / BKF;
+        for (int kb = 0; kb < nk; ++kb, ++g) {
+          const int s = g % NSTAGE, use = g / NSTAGE;
+          if (use > 0 && !mbar_wait(empty0 + 8 * s, (use - 1) & 1, err, ERR_PRODUCER)) {
+            ok = false;
+            break;
+          }
+          const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+          const uint32_t fb = full0 + 8 * s;
+          mbar_expect_tx(fb, STAGE_BYTES);
+          const int kx = kb * BKF;
+          tma_load_2d(st + 0 * TILE_BYTES, &job.a_hi, kx, tr.y, fb);
+          tma_load_2d(st + 1 * TILE_BYTES, &job.a_lo, kx, tr.y, fb);
+          tma_load_2d(st + 2 * TILE_BYTES, &job.b_hi, kx, tr.z, fb);
+          tma_load_2d(st + 3 * TILE_BYTES, &job.b_lo, kx, tr.z, fb);
         }
       }
+      progress[0] = g;
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer ----
+      constexpr uint32_t idesc = idesc_tf32(BM, BN);
+      int g = 0, it = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x, ++it) {
+        const TcJob& job = jobs[tiles[t].x];
+        const int nk = (job.K + BKF - 1) / BKF;
+        const int buf = it & 1, ause = it >> 1;
+        if (ause > 0 && !mbar_wait(acce0 + 8 * buf, (ause - 1) & 1, err, ERR_MMA)) break;
+        tc_fence_after();
+        const uint32_t d = tmem + buf * BN;
+        for (int kb = 0; kb < nk; ++kb, ++g) {
+          const int s = g % NSTAGE, use = g / NSTAGE;
+          if (!mbar_wait(full0 + 8 * s, use & 1, err, ERR_MMA)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+          const uint64_t ah = sw128_desc(st), al = sw128_desc(st + TILE_BYTES);
+          const uint64_t bh = sw128_desc(st + 2 * TILE_BYTES),
+                         bl = sw128_desc(st + 3 * TILE_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < BKF / 8; ++kk) {
+            const uint64_t o = static_cast<uint64_t>(kk * 32) >> 4;  // 8 TF32 = 32 bytes
+            umma_tf32(d, ah + o, bh + o, idesc, (kb | kk) != 0 ? 1u : 0u);
+            umma_tf32(d, ah + o, bl + o, idesc, 1u);
+            umma_tf32(d, al + o, bh + o, idesc, 1u);
+          }
+          umma_commit(empty0 + 8 * s);
+        }
+        if (ok) umma_commit(accf0 + 8 * buf);
+      }
+      progress[1] = g;
+      // every MMA of this CTA has completed once `quiet` fires
+      umma_commit(quiet);
+      mbar_wait(quiet, 0, err, ERR_MMA);
+    }
+    __syncwarp();
+  } else {
+    // ---- epilogue warps 2..5: TMEM lane quarter = warp % 4 ----
+    const int q = warp & 3;
+    float* stg = stage_out + (warp - 2) * 32 * 33;
+    int it = 0;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
+      const int4 tr = tiles[t];
+      const TcJob& job = jobs[tr.x];
+      const int buf = it & 1;
+      const bool ok = mbar_wait(accf0 + 8 * buf, (it >> 1) & 1, err, ERR_EPILOGUE);
+      if (!__all_sync(0xffffffffu, ok && *reinterpret_cast<volatile int*>(err) == 0)) break;
+      tc_fence_after();
+      const int row0 = tr.y + 32 * q;
+#pragma unroll 1
+      for (int cc = 0; cc < BN / 32; ++cc) {
+        uint32_t r[32];
+        tmem_ld32(tmem + buf * BN + (static_cast<uint32_t>(32 * q) << 16) + cc * 32, r);
+        // transpose the warp's 32 x 32 block so each store instruction writes
+        // 32 consecutive columns of one row
+#pragma unroll
+        for (int j = 0; j < 32; ++j) stg[lane * 33 + j] = __uint_as_float(r[j]);
+        __syncwarp();
+        const int col = tr.z + cc * 32 + lane;
+        if (col < job.N) {
+#pragma unroll 4
+          for (int rr = 0; rr < 32; ++rr) {
+            const int row = row0 + rr;
+            if (row < job.M) store_value(job, row, col, stg[rr * 33 + lane]);
+          }
+        }
+        __syncwarp();
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(acce0 + 8 * buf)
+                                  : "memory");
     }
   }
-  tc_fence_before();
   __syncthreads();
   if (threadIdx.x == 0 && progress[1] < progress[0]) {
     // a failure left copies in flight: wait for them (bounded) before exiting
-    for (int kb = progress[1]; kb < progress[0]; ++kb)
-      mbar_wait(full0 + 8 * (kb % NSTAGE), (kb / NSTAGE) & 1, err, ERR_DRAIN);
+    for (int g = progress[1]; g < progress[0]; ++g)
+      mbar_wait(full0 + 8 * (g % NSTAGE), (g / NSTAGE) & 1, err, ERR_DRAIN);
   }
+  tc_fence_before();
   __syncthreads();
-  if (warp == 1) tmem_dealloc(tmem, BN);
+  tc_fence_after();
+  if (warp == 1) tmem_dealloc(tmem, 2 * BN);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -308,7 +355,8 @@ int launch(const TcJob* jobs_dev, const int4* tiles_dev, int n_tiles, int* err_d
     return AXI_ERR_CUDA;
   }
   if (n_tiles <= 0) return AXI_OK;
-  tf32x3_gemm_kernel<<<n_tiles, THREADS, SMEM_BYTES, s>>>(jobs_dev, tiles_dev, err_dev);
+  const int grid = n_tiles < axi::sm_count() ? n_tiles : axi::sm_count();
+  tf32x3_gemm_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(jobs_dev, tiles_dev, n_tiles, err_dev);
   return axi::launch_status("tf32x3_gemm");
 }
 

@@ -7,16 +7,19 @@
 // hi*hi + hi*lo + lo*hi in FP32 in tensor memory, which restores FP32-level
 // accuracy (the dropped lo*lo term is below FP32 rounding).
 //
-// One CTA computes a 128 x 128 output tile:
+// Persistent CTAs (one per SM) walk a list of 128 x 128 output tiles:
 //   warp 0, one thread   TMA producer: cp.async.bulk.tensor tiles (128 rows x
 //                        32 floats, 128-byte swizzle) of A_hi, A_lo, B_hi, B_lo
-//                        into a 3-stage shared-memory ring (mbarrier complete_tx)
+//                        into a 3-stage shared-memory ring (mbarrier complete_tx),
+//                        continuous across tiles
 //   warp 1, one thread   MMA issuer: 3 x 4 tcgen05.mma.kind::tf32 per stage into
-//                        a 128-lane x 128-column FP32 accumulator in TMEM;
-//                        tcgen05.commit releases the stage
-//   warps 0-3            epilogue: tcgen05.ld (warp w reads TMEM lanes 32w..32w+31)
-//                        and the stage-specific store (plain, hi/lo split, or
-//                        scaled by an elementwise factor then split)
+//                        one of two 128-lane x 128-column FP32 accumulators in
+//                        TMEM; tcgen05.commit releases stages and accumulators
+//   warps 2-5            epilogue: tcgen05.ld (warp w reads TMEM lanes
+//                        32 (w % 4) ..), a per-warp shared-memory transpose for
+//                        row-contiguous stores, and the stage-specific store
+//                        (plain, hi/lo split, or scaled then split); it drains
+//                        one accumulator while the MMAs fill the other
 // Every mbarrier wait is bounded by a 1 s wall-clock limit; on expiry the
 // kernel records an error code, drains its outstanding copies (bounded),
 // frees its TMEM and returns.
@@ -35,8 +38,9 @@ constexpr int BKF = 32;                         // K floats per stage (128-byte 
 constexpr int NSTAGE = 3;
 constexpr int TILE_BYTES = BM * BKF * 4;        // 16 KB per operand tile
 constexpr int STAGE_BYTES = 4 * TILE_BYTES;     // A_hi, A_lo, B_hi, B_lo
-constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 + 256;
-constexpr int THREADS = 128;
+constexpr int EPI_WARPS = 4;
+constexpr int THREADS = 32 * (2 + EPI_WARPS);   // TMA warp, MMA warp, 4 epilogue warps
+constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 + 256 + EPI_WARPS * 32 * 33 * 4;
 constexpr unsigned long long WAIT_NS = 1000000000ull;
 
 enum { MODE_PLAIN = 0, MODE_SPLIT = 1, MODE_SCALE_SPLIT = 2 };
