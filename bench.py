@@ -34,11 +34,12 @@ sys.path.insert(0, HERE)
 
 METRIC = "cell-updates/s on 1 GB300, batched FP32 vs plain FP64 at <=1e-5 L2; p50/p99 lat"
 UNIT = "cell-updates/s"
-PHASES = ("kill", "transform", "vel_max", "penalise", "adv_diff1", "diff2")
+PHASES = ("kill", "transform", "vel_max", "penalise", "advect_diffuse")
 # Algorithmic fields moved per cell by each stencil phase (reads + writes):
-# vel_max psi; penalise psi chi omega -> u_z u_r omega; adv_diff1 omega u_z
-# u_r -> w_adv w_tmp; diff2 w_adv w_tmp -> omega.
-PHASE_FIELDS = {"vel_max": 1, "penalise": 6, "adv_diff1": 5, "diff2": 3}
+# vel_max psi; penalise psi chi omega -> u_z u_r omega; advect_diffuse omega
+# u_z u_r -> omega (+ omega's TF32 hi / lo operand copy on the tensor-core
+# path, + the rebuilt mask of sedimenting bodies).
+PHASE_FIELDS = {"vel_max": 1, "penalise": 6, "advect_diffuse": 4}
 
 
 def ensemble_cases(workload, seed=4):
@@ -279,6 +280,10 @@ def run_gb300(args, world, rank, local):
     hbm, bf16, src = peaks()
     dom = max(ph_ms, key=ph_ms.get)
     esize = 8 if args.precision == "f64" else 4
+    if ens.tensor_cores:
+        PHASE_FIELDS["advect_diffuse"] += 2
+    if any(c.sediment for c in cases):
+        PHASE_FIELDS["advect_diffuse"] += 1
     if dom == "transform":
         flops = sum(4.0 * c.nr * c.nz * (c.nr + c.nz) for c in cases)
         achieved = flops / (ph_ms[dom] / 1000.0) / 1e12
@@ -296,7 +301,7 @@ def run_gb300(args, world, rank, local):
     roof["kernel"] = dom
     roof["frac"] = roof["achieved"] / roof["peak"]
     roof["traffic"] = None
-    stencil_bytes = sum(15 * esize * c.nr * c.nz for c in cases)
+    stencil_bytes = sum(sum(PHASE_FIELDS.values()) * esize * c.nr * c.nz for c in cases)
     stencil_ms = sum(ph_ms[p] for p in PHASE_FIELDS)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -315,7 +320,7 @@ def run_gb300(args, world, rank, local):
         "clocks": clocks.summary(),
         "status_ok": bool(np.all(status == 0)),
     }
-    n_launch = 1 + 4 + 4
+    n_launch = 1 + 4 + 3
     line["gpu_launches"] = n_launch * args.steps
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sample = cases[:2]

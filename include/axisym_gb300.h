@@ -345,8 +345,7 @@ typedef struct axi_case {
   void* u_z;
   void* u_r;
   void* chi;
-  void* w_adv;   /* scratch: advected vorticity */
-  void* w_tmp;   /* scratch: RK2 stage */
+  const double* kill_coef; /* 3 * kill_width sine-taper factors: z start, z end, outer r */
   const double* r;
   const double* z;
   const void* rinv2dx;   /* 1 / (2 dx r_i) */
@@ -409,9 +408,8 @@ int axi_rigid_step_f64(const axi_plan_info* info, const void* plan_dev, int n_st
 int axi_rigid_step_f32(const axi_plan_info* info, const void* plan_dev, int n_steps,
                        void* stream);
 /* One phase of a step (0 kill, 1 spectral transform, 2 velocity max and dt,
- * 3 penalisation and drag, 4 advection + diffusion stage 1, 5 diffusion stage
- * 2); running phases 0..5 in order equals one step. Lets a caller time each
- * kernel. */
+ * 3 penalisation and drag, 4 advection and both diffusion stages); running
+ * phases 0..4 in order equals one step. Lets a caller time each kernel. */
 int axi_rigid_phase_f64(const axi_plan_info* info, const void* plan_dev, int phase,
                         void* stream);
 int axi_rigid_phase_f32(const axi_plan_info* info, const void* plan_dev, int phase,

@@ -16,9 +16,9 @@
 //                it into dt and the dt-dependent constants of the step
 //   penalise     per tile: velocity + Brinkman + curl(u_pen - u) into omega,
 //                drag partials; the last tile of a case finalises the drag
-//   adv_diff1    per tile: ENO3 advection (axis mirror by index reflection,
-//                halo 3 in shared memory) + RK2 stage 1
-//   diff2        per tile: RK2 stage 2 into omega; advances the time
+//   advect_diffuse per tile: ENO3 advection (axis mirror by index reflection)
+//                and both RK2 stages in shared memory (halo 4); advances the
+//                time (sedimenting cases: mask rebuild, drag, body ODE)
 //
 // GB300 runs FP64 at 1/70 of its FP32 rate, so the FP32 engine keeps every
 // per-cell operation in FP32: per-row factors (1 / (2 dx r), 1 / r^2, r) are
@@ -81,7 +81,11 @@ __global__ void kill_reset_kernel(const axi_case* __restrict__ cases) {
   const axi_case& k = cases[blockIdx.x];
   T* w = F<T>(k.omega);
   const int nr = k.nr, nz = k.nz, wd = k.kill_width;
-  const double dx = k.dx, half_dx = 0.5 * k.dx;
+  // taper factors sin(pi (Z - dx/2) / 2 / (w - 1) / dx) etc., evaluated once on
+  // the host with the reference's own formula
+  const double* cz0 = k.kill_coef;
+  const double* cz1 = k.kill_coef + wd;
+  const double* cr = k.kill_coef + 2 * wd;
   if (threadIdx.x == 0) {
     *reinterpret_cast<unsigned long long*>(&k.state[AXI_ST_UMAX]) = 0ull;
     counter(k, 0)[0] = 0u;
@@ -92,24 +96,17 @@ __global__ void kill_reset_kernel(const axi_case* __restrict__ cases) {
     k.state[AXI_ST_UFREE] = k.U0 * prefac;
   }
   for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-    T* row = w + (long long)i * nz;
-    const double left = (double)row[wd - 1];
-    double nl[8];
-    for (int q = 0; q < wd; ++q) nl[q] = sin(kPi * (k.z[q] - half_dx) / 2 / (wd - 1) / dx) * left;
-    for (int q = 0; q < wd; ++q) store_omega<T>(k, (long long)i * nz + q, (T)nl[q]);
-    const double right = (double)row[nz - wd];
-    for (int q = 0; q < wd; ++q)
-      nl[q] = sin(kPi * (1 - k.z[nz - wd + q] - half_dx) / 2 / (wd - 1) / dx) * right;
-    for (int q = 0; q < wd; ++q) store_omega<T>(k, (long long)i * nz + nz - wd + q, (T)nl[q]);
+    const long long row = (long long)i * nz;
+    const double left = (double)w[row + wd - 1];
+    const double right = (double)w[row + nz - wd];
+    for (int q = 0; q < wd; ++q) store_omega<T>(k, row + q, (T)(cz0[q] * left));
+    for (int q = 0; q < wd; ++q) store_omega<T>(k, row + nz - wd + q, (T)(cz1[q] * right));
   }
   __syncthreads();
   for (int j = threadIdx.x; j < nz; j += blockDim.x) {
     const double src = (double)w[(long long)(nr - wd) * nz + j];
-    for (int q = 0; q < wd; ++q) {
-      const int i = nr - wd + q;
-      store_omega<T>(k, (long long)i * nz + j,
-                     (T)(sin(kPi * (1 - k.r[i] - half_dx) / 2 / (wd - 1) / dx) * src));
-    }
+    for (int q = 0; q < wd; ++q)
+      store_omega<T>(k, (long long)(nr - wd + q) * nz + j, (T)(cr[q] * src));
     store_omega<T>(k, j, T(0));
   }
 }
@@ -226,6 +223,7 @@ template <typename T>
 __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict__ cases,
                                                       const int4* __restrict__ tiles) {
   __shared__ T ps[TY + 4][TX + 4];
+  __shared__ T sc[TY + 2][TX + 2];
   __shared__ T duz[TY + 2][TX + 2];
   __shared__ T dur[TY + 2][TX + 2];
   __shared__ double red[NT / 32];
@@ -242,10 +240,25 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
   const bool sediment = (k.flags & AXI_CASE_SEDIMENTING) != 0;
   const T ubody = (T)(sediment ? k.state[AXI_ST_UBODY] : k.U_body);
   const T inv2dx = (T)k.inv_2dx;
+  // all global loads of the block are issued here: psi (halo 2), chi (halo 1)
+  // into shared memory, omega of the owned cells into registers
+  T* w = F<T>(k.omega);
+  T wown[CPT];
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) {
+    const int e = threadIdx.x + q * NT;
+    const int gi = i0 + e / TX, gj = j0 + e % TX;
+    wown[q] = (gi < nr && gj < nz) ? w[(long long)gi * nz + gj] : T(0);
+  }
   for (int e = threadIdx.x; e < (TY + 4) * (TX + 4); e += NT) {
     const int a = e / (TX + 4), b = e % (TX + 4);
     const int gi = i0 - 2 + a, gj = j0 - 2 + b;
     ps[a][b] = (gi >= 0 && gi < nr && gj >= 0 && gj < nz) ? psi[(long long)gi * nz + gj] : T(0);
+  }
+  for (int e = threadIdx.x; e < (TY + 2) * (TX + 2); e += NT) {
+    const int a = e / (TX + 2), b = e % (TX + 2);
+    const int gi = i0 - 1 + a, gj = j0 - 1 + b;
+    sc[a][b] = (gi >= 0 && gi < nr && gj >= 0 && gj < nz) ? chi[(long long)gi * nz + gj] : T(0);
   }
   __syncthreads();
   // every one-sided stencil of an edge cell stays inside the halo-2 tile
@@ -257,7 +270,7 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
     if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
       T uz, ur, pz, pr;
       velocity_at<T>(k, sp, gi, gj, rinv2dx[gi], ufree, uz, ur);
-      penalise_point<T>(uz, ur, lamdt * chi[(long long)gi * nz + gj], ubody, pz, pr);
+      penalise_point<T>(uz, ur, lamdt * sc[a][b], ubody, pz, pr);
       dz = pz - uz;
       dr = pr - ur;
     }
@@ -268,7 +281,6 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
   T cd_part = T(0);
   T* uzp = F<T>(k.u_z);
   T* urp = F<T>(k.u_r);
-  T* w = F<T>(k.omega);
   const T* rw = CF<T>(k.rw);
 #pragma unroll
   for (int q = 0; q < CPT; ++q) {
@@ -277,7 +289,7 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
     const int gi = i0 + a, gj = j0 + b;
     if (gi < nr && gj < nz) {
       const long long c = (long long)gi * nz + gj;
-      const T ch = chi[c];
+      const T ch = sc[a + 1][b + 1];
       T uz, ur, pz, pr;
       velocity_at<T>(k, sp, gi, gj, rinv2dx[gi], ufree, uz, ur);
       penalise_point<T>(uz, ur, lamdt * ch, ubody, pz, pr);
@@ -289,7 +301,7 @@ __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict
       if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
         const T pw = (dur[a + 1][b + 2] - dur[a + 1][b]) * inv2dx -
                      (duz[a + 2][b + 1] - duz[a][b + 1]) * inv2dx;
-        w[c] = w[c] + pw;
+        w[c] = wown[q] + pw;
       }
     }
   }
@@ -344,14 +356,47 @@ __device__ __forceinline__ T face_flux(T fm1, T f0, T f1, T f2, T um1, T u0, T u
   return third * f0 * u0 + five6 * f1 * u1 - sixth * f2 * u2;
 }
 
+// ---------------------------------------------------------------------------
+// advect_diffuse: ENO3 advection (kernels/advect_vorticity_via_eno3.py:28-42,
+// pyst_kernels/advection_flux.py:9-163, advection_timestep.py:37-54) followed
+// by both RK2 diffusion stages (kernels/diffusion_RK2.py:9-44), fused: the
+// block stages omega, u_z, u_r with a halo of 4, advects the tile plus a
+// halo of 2, applies stage 1 on the tile plus a halo of 1 and stage 2 on the
+// tile, all in shared memory, so omega is read and written once per step.
+// Sedimenting cases also rebuild the body mask here and close the step
+// (falling_rigid_sphere.py:156-181).
+// ---------------------------------------------------------------------------
+constexpr int AD_H = 4;
+constexpr int AD_LW = TX + 2 * AD_H, AD_LH = TY + 2 * AD_H;  // staged inputs
+constexpr int AD_AW = TX + 4, AD_AH = TY + 4;                // advected (halo 2)
+constexpr int AD_SW = TX + 2, AD_SH = TY + 2;                // stage 1 (halo 1)
 template <typename T>
-__global__ void __launch_bounds__(NT) adv_diff1_kernel(const axi_case* __restrict__ cases,
-                                                       const int4* __restrict__ tiles) {
-  constexpr int H = 3;
-  __shared__ T sw[TY + 2 * H][TX + 2 * H];
-  __shared__ T sz[TY + 2 * H][TX + 2 * H];
-  __shared__ T sr[TY + 2 * H][TX + 2 * H];
-  __shared__ T wa[TY + 2][TX + 2];
+constexpr int advect_diffuse_smem() {
+  return (int)sizeof(T) * (3 * AD_LH * AD_LW + AD_AH * AD_AW + AD_SH * AD_SW);
+}
+
+// Smoothed Heaviside of a sphere level set (kernels/smooth_Heaviside.py:10-14,
+// level set of falling_rigid_sphere.py:156).
+template <typename T>
+__device__ __forceinline__ T sphere_mask(T z, T r, T zc, T radius, T w) {
+  const T dz = z - zc;
+  const T phi = -sqrt(dz * dz + r * r) + radius;
+  T h = phi >= w ? T(1) : T(0);
+  if (fabs(phi) < w) h += T(0.5) * (T(1) + phi / w + dev_sin(Pi<T>::v * phi / w) / Pi<T>::v);
+  return h;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __restrict__ cases,
+                                                            const int4* __restrict__ tiles) {
+  extern __shared__ __align__(16) unsigned char ad_smem[];
+  T* sw = reinterpret_cast<T*>(ad_smem);
+  T* sz = sw + AD_LH * AD_LW;
+  T* sr = sz + AD_LH * AD_LW;
+  T* wa = sr + AD_LH * AD_LW;
+  T* tp = wa + AD_AH * AD_AW;
+  __shared__ double red[NT / 32];
+  __shared__ bool last;
   const int4 tr = tiles[blockIdx.x];
   const axi_case& k = cases[tr.x];
   const int nr = k.nr, nz = k.nz;
@@ -359,12 +404,15 @@ __global__ void __launch_bounds__(NT) adv_diff1_kernel(const axi_case* __restric
   const T* w = CF<T>(k.omega);
   const T* uz = CF<T>(k.u_z);
   const T* ur = CF<T>(k.u_r);
+  const T* rinv2dx = CF<T>(k.rinv2dx);
+  const T* rinv2 = CF<T>(k.rinv2);
   const T a = (T)k.state[AXI_ST_ADV];
   const T c1 = (T)k.state[AXI_ST_C1];
+  const T c2 = (T)k.state[AXI_ST_C2];
   const T inv_dx2 = (T)k.inv_dx2;
-  for (int e = threadIdx.x; e < (TY + 2 * H) * (TX + 2 * H); e += NT) {
-    const int p = e / (TX + 2 * H), q = e % (TX + 2 * H);
-    const int gi = i0 - H + p, gj = j0 - H + q;
+  for (int e = threadIdx.x; e < AD_LH * AD_LW; e += NT) {
+    const int p = e / AD_LW, q = e % AD_LW;
+    const int gi = i0 - AD_H + p, gj = j0 - AD_H + q;
     T vw = T(0), vz = T(0), vr = T(0);
     if (gj >= 0 && gj < nz && gi < nr) {
       if (gi >= 0) {
@@ -380,30 +428,32 @@ __global__ void __launch_bounds__(NT) adv_diff1_kernel(const axi_case* __restric
         vr = -ur[c];
       }
     }
-    sw[p][q] = vw;
-    sz[p][q] = vz;
-    sr[p][q] = vr;
+    sw[e] = vw;
+    sz[e] = vz;
+    sr[e] = vr;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < (TY + 2) * (TX + 2); e += NT) {
-    const int p = e / (TX + 2), q = e % (TX + 2);
-    const int gi = i0 - 1 + p, gj = j0 - 1 + q;
+  // advected omega on the tile + halo 2
+  for (int e = threadIdx.x; e < AD_AH * AD_AW; e += NT) {
+    const int p = e / AD_AW, q = e % AD_AW;
+    const int gi = i0 - 2 + p, gj = j0 - 2 + q;
     T val = T(0);
     if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
-      const int P = p + H - 1, Q = q + H - 1;
-      const T f0 = sw[P][Q];
+      const int c = (p + 2) * AD_LW + (q + 2);  // position in the staged tile
+      const T f0 = sw[c];
       T flux = T(0);
       // pystencils ghost layers: no flux in the last two rows and the first
       // and last two columns
       if (gi < nr - 2 && gj >= 2 && gj < nz - 2) {
-        const T xf = face_flux(sw[P][Q - 1], f0, sw[P][Q + 1], sw[P][Q + 2], sz[P][Q - 1],
-                               sz[P][Q], sz[P][Q + 1], sz[P][Q + 2]);
-        const T xb = face_flux(sw[P][Q - 2], sw[P][Q - 1], f0, sw[P][Q + 1], sz[P][Q - 2],
-                               sz[P][Q - 1], sz[P][Q], sz[P][Q + 1]);
-        const T yf = face_flux(sw[P - 1][Q], f0, sw[P + 1][Q], sw[P + 2][Q], sr[P - 1][Q],
-                               sr[P][Q], sr[P + 1][Q], sr[P + 2][Q]);
-        const T yb = face_flux(sw[P - 2][Q], sw[P - 1][Q], f0, sw[P + 1][Q], sr[P - 2][Q],
-                               sr[P - 1][Q], sr[P][Q], sr[P + 1][Q]);
+        const T xf = face_flux(sw[c - 1], f0, sw[c + 1], sw[c + 2], sz[c - 1], sz[c], sz[c + 1],
+                               sz[c + 2]);
+        const T xb = face_flux(sw[c - 2], sw[c - 1], f0, sw[c + 1], sz[c - 2], sz[c - 1], sz[c],
+                               sz[c + 1]);
+        const int L = AD_LW;
+        const T yf = face_flux(sw[c - L], f0, sw[c + L], sw[c + 2 * L], sr[c - L], sr[c],
+                               sr[c + L], sr[c + 2 * L]);
+        const T yb = face_flux(sw[c - 2 * L], sw[c - L], f0, sw[c + L], sr[c - 2 * L], sr[c - L],
+                               sr[c], sr[c + L]);
         flux = a * xf;
         flux = flux - a * xb;
         flux = flux + a * yf;
@@ -411,74 +461,43 @@ __global__ void __launch_bounds__(NT) adv_diff1_kernel(const axi_case* __restric
       }
       val = f0 + flux;
     }
-    wa[p][q] = val;
+    wa[e] = val;
   }
   __syncthreads();
-  const T* rinv2dx = CF<T>(k.rinv2dx);
-  const T* rinv2 = CF<T>(k.rinv2);
-  T* wadv = F<T>(k.w_adv);
-  T* wtmp = F<T>(k.w_tmp);
+  // RK2 stage 1 on the tile + halo 1
+  for (int e = threadIdx.x; e < AD_SH * AD_SW; e += NT) {
+    const int p = e / AD_SW, q = e % AD_SW;
+    const int gi = i0 - 1 + p, gj = j0 - 1 + q;
+    T tmp = T(0);
+    if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
+      const int c = (p + 1) * AD_AW + (q + 1);
+      const T c0 = wa[c];
+      tmp = c0;
+      if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
+        const T n = wa[c + AD_AW], s = wa[c - AD_AW], ee = wa[c + 1], ww = wa[c - 1];
+        const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rinv2dx[gi] -
+                      c0 * rinv2[gi];
+        tmp = c0 + c1 * lap;
+      }
+    }
+    tp[e] = tmp;
+  }
+  __syncthreads();
+  // RK2 stage 2 on the tile
+  const bool sediment = (k.flags & AXI_CASE_SEDIMENTING) != 0;
+  const T zc = (T)k.state[AXI_ST_ZCM];
+  T cd_part = T(0);
 #pragma unroll
   for (int qq = 0; qq < CPT; ++qq) {
     const int e = threadIdx.x + qq * NT;
     const int p = e / TX, q = e % TX;
     const int gi = i0 + p, gj = j0 + q;
     if (gi < nr && gj < nz) {
-      const T c0 = wa[p + 1][q + 1];
-      T tmp = c0;
-      if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
-        const T n = wa[p + 2][q + 1], s = wa[p][q + 1], ee = wa[p + 1][q + 2], ww = wa[p + 1][q];
-        const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rinv2dx[gi] -
-                      c0 * rinv2[gi];
-        tmp = c0 + c1 * lap;
-      }
       const long long c = (long long)gi * nz + gj;
-      wadv[c] = c0;
-      wtmp[c] = tmp;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// diff2: RK2 stage 2 (kernels/diffusion_RK2.py:27-44); advances the time
-// ---------------------------------------------------------------------------
-// Smoothed Heaviside of a sphere level set (kernels/smooth_Heaviside.py:10-14,
-// level set of falling_rigid_sphere.py:156).
-template <typename T>
-__device__ __forceinline__ T sphere_mask(T z, T r, T zc, T radius, T w) {
-  const T dz = z - zc;
-  const T phi = -sqrt(dz * dz + r * r) + radius;
-  T h = phi >= w ? T(1) : T(0);
-  if (fabs(phi) < w) h += T(0.5) * (T(1) + phi / w + dev_sin(Pi<T>::v * phi / w) / Pi<T>::v);
-  return h;
-}
-
-template <typename T>
-__global__ void __launch_bounds__(NT) diff2_kernel(const axi_case* __restrict__ cases,
-                                                   const int4* __restrict__ tiles) {
-  __shared__ double red[NT / 32];
-  __shared__ bool last;
-  const int4 tr = tiles[blockIdx.x];
-  const axi_case& k = cases[tr.x];
-  const int nr = k.nr, nz = k.nz;
-  const T* wa = CF<T>(k.w_adv);
-  const T* tm = CF<T>(k.w_tmp);
-  const T* rinv2dx = CF<T>(k.rinv2dx);
-  const T* rinv2 = CF<T>(k.rinv2);
-  const T inv_dx2 = (T)k.inv_dx2;
-  const T c2 = (T)k.state[AXI_ST_C2];
-  const bool sediment = (k.flags & AXI_CASE_SEDIMENTING) != 0;
-  const T zc = (T)k.state[AXI_ST_ZCM];
-  T cd_part = T(0);
-#pragma unroll
-  for (int q = 0; q < CPT; ++q) {
-    const int e = threadIdx.x + q * NT;
-    const int gi = tr.y + e / TX, gj = tr.z + e % TX;
-    if (gi < nr && gj < nz) {
-      const long long c = (long long)gi * nz + gj;
-      T v = wa[c];
+      T v = wa[(p + 2) * AD_AW + (q + 2)];
       if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
-        const T c0 = tm[c], n = tm[c + nz], s = tm[c - nz], ee = tm[c + 1], ww = tm[c - 1];
+        const int d = (p + 1) * AD_SW + (q + 1);
+        const T c0 = tp[d], n = tp[d + AD_SW], s = tp[d - AD_SW], ee = tp[d + 1], ww = tp[d - 1];
         const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rinv2dx[gi] -
                       c0 * rinv2[gi];
         v = v + c2 * lap;
@@ -490,7 +509,7 @@ __global__ void __launch_bounds__(NT) diff2_kernel(const axi_case* __restrict__ 
         const T ch = sphere_mask<T>(CF<T>(k.zw)[gj], CF<T>(k.rw)[gi], zc, (T)k.r_body,
                                     (T)k.blend_w);
         F<T>(k.chi)[c] = ch;
-        cd_part += CF<T>(k.rw)[gi] * ch * CF<T>(k.u_z)[c];
+        cd_part += CF<T>(k.rw)[gi] * ch * sz[(p + AD_H) * AD_LW + (q + AD_H)];
       }
     }
   }
@@ -767,8 +786,22 @@ inline int tc_tiles_of(const axi_case& k, int stage) {
   return ((M + axi_tc::BM - 1) / axi_tc::BM) * ((N + axi_tc::BN - 1) / axi_tc::BN);
 }
 
-enum { PH_KILL = 0, PH_TRANSFORM = 1, PH_VEL_MAX = 2, PH_PENALISE = 3, PH_ADV_DIFF1 = 4,
-       PH_DIFF2 = 5, PH_COUNT = 6 };
+enum { PH_KILL = 0, PH_TRANSFORM = 1, PH_VEL_MAX = 2, PH_PENALISE = 3, PH_ADVECT_DIFFUSE = 4,
+       PH_COUNT = 5 };
+
+template <typename T>
+int advect_diffuse_attr() {
+  static int status = -1;
+  if (status < 0) {
+    status = cudaFuncSetAttribute(advect_diffuse_kernel<T>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  advect_diffuse_smem<T>()) == cudaSuccess
+                 ? AXI_OK
+                 : AXI_ERR_CUDA;
+    if (status != AXI_OK) axi::set_error("advect_diffuse: cannot reserve shared memory");
+  }
+  return status;
+}
 
 template <typename T>
 int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStream_t s) {
@@ -794,11 +827,9 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
     case PH_PENALISE:
       penalise_kernel<T><<<nt, NT, 0, s>>>(v.cases, v.stencil);
       break;
-    case PH_ADV_DIFF1:
-      adv_diff1_kernel<T><<<nt, NT, 0, s>>>(v.cases, v.stencil);
-      break;
-    case PH_DIFF2:
-      diff2_kernel<T><<<nt, NT, 0, s>>>(v.cases, v.stencil);
+    case PH_ADVECT_DIFFUSE:
+      AXI_TRY(advect_diffuse_attr<T>());
+      advect_diffuse_kernel<T><<<nt, NT, advect_diffuse_smem<T>(), s>>>(v.cases, v.stencil);
       break;
     default:
       axi::set_error("rigid_phase: unknown phase %d", phase);
@@ -820,7 +851,7 @@ int validate(const axi_case* cases, int n_cases, const char* what) {
                      k.nz, k.kill_width);
       return AXI_ERR_INVALID;
     }
-    const void* ptrs[] = {k.omega, k.psi, k.u_z, k.u_r, k.chi, k.w_adv, k.w_tmp, k.r, k.z,
+    const void* ptrs[] = {k.omega, k.psi, k.u_z, k.u_r, k.chi, k.kill_coef, k.r, k.z,
                           k.rinv2dx, k.rinv2, k.rw, k.zw, k.Er, k.Er_inv_w, k.EzinvT, k.EzT,
                           k.inv_eig, k.gemm_work, k.state, k.partials};
     for (const void* p : ptrs) {

@@ -41,8 +41,7 @@ class AxiCase(ctypes.Structure):
         ("part_mass", ctypes.c_double), ("part_vol", ctypes.c_double),
         ("r_body", ctypes.c_double), ("blend_w", ctypes.c_double),
         ("omega", ctypes.c_void_p), ("psi", ctypes.c_void_p), ("u_z", ctypes.c_void_p),
-        ("u_r", ctypes.c_void_p), ("chi", ctypes.c_void_p), ("w_adv", ctypes.c_void_p),
-        ("w_tmp", ctypes.c_void_p),
+        ("u_r", ctypes.c_void_p), ("chi", ctypes.c_void_p), ("kill_coef", ctypes.c_void_p),
         ("r", ctypes.c_void_p), ("z", ctypes.c_void_p), ("rinv2dx", ctypes.c_void_p),
         ("rinv2", ctypes.c_void_p), ("rw", ctypes.c_void_p), ("zw", ctypes.c_void_p),
         ("Er", ctypes.c_void_p), ("Er_inv_w", ctypes.c_void_p), ("EzinvT", ctypes.c_void_p),
@@ -118,6 +117,16 @@ def grid(nz, nr, dx):
     z = np.linspace(dx / 2, nz * dx - dx / 2, nz)
     r = np.linspace(dx / 2, nr * dx - dx / 2, nr)
     return z, r
+
+
+def kill_coefficients(z, r, width, dx):
+    """Sine-taper factors of kernels/kill_boundary_vorticity_sine.py:9-26, with
+    the reference's own expression (literal 1 - Z, 1 - R): z start, z end,
+    outer r, each `width` long."""
+    zs = np.sin(np.pi * (z[:width] - 0.5 * dx) / 2 / (width - 1) / dx)
+    ze = np.sin(np.pi * (1 - z[-width:] - 0.5 * dx) / 2 / (width - 1) / dx)
+    rr = np.sin(np.pi * (1 - r[-width:] - 0.5 * dx) / 2 / (width - 1) / dx)
+    return np.concatenate([zs, ze, rr])
 
 
 class AxiPlanInfo(ctypes.Structure):
@@ -205,8 +214,7 @@ class RigidEnsemble:
                 u_z=torch.zeros((c.nr, c.nz), **f),
                 u_r=torch.zeros((c.nr, c.nz), **f),
                 chi=chi64.to(self.dtype),
-                w_adv=torch.zeros((c.nr, c.nz), **f),
-                w_tmp=torch.zeros((c.nr, c.nz), **f),
+                kill_coef=torch.tensor(kill_coefficients(z, r, c.kill_width, c.dx), **f64),
                 r=torch.tensor(r, **f64),
                 z=torch.tensor(z, **f64),
                 rinv2dx=torch.tensor(1.0 / (2 * c.dx * r), **f64).to(self.dtype),
@@ -246,7 +254,7 @@ class RigidEnsemble:
                 s.r_body = c.r_sphere
                 s.blend_w = c.moll_zone
                 self.state[k, ST_ZCM] = c.z_cm
-            for name in ("omega", "psi", "u_z", "u_r", "chi", "w_adv", "w_tmp", "r", "z",
+            for name in ("omega", "psi", "u_z", "u_r", "chi", "kill_coef", "r", "z",
                          "rinv2dx", "rinv2", "rw", "zw", "gemm_work", "partials"):
                 setattr(s, name, t[name].data_ptr())
             for name, v in b.t.items():
@@ -295,7 +303,7 @@ class RigidEnsemble:
         N.check(self._step_fn(ctypes.byref(self.info), ctypes.c_void_p(self.plan.data_ptr()),
                               int(n), ctypes.c_void_p(s.cuda_stream)), "rigid_step")
 
-    PHASES = ("kill", "transform", "vel_max", "penalise", "adv_diff1", "diff2")
+    PHASES = ("kill", "transform", "vel_max", "penalise", "advect_diffuse")
 
     def phase(self, ph, stream=None):
         """Run one phase of a step (see PHASES); all six in order = one step."""
