@@ -265,6 +265,59 @@ int axi_fd_transform_f64(double* out, int ld_out, const double* in, int ld_in,
 int64_t axi_tf32x3_gemm_work_bytes(int M, int N, int K);
 int axi_tf32x3_gemm(float* C, const float* A, const float* B, int M, int N, int K, void* work,
                     void* stream);
+/* ---------------------------------------------------------------------
+ * Spectral transform on the tcgen05 tensor cores (FP32 operands, 3xTF32
+ * products, FP32 accumulation): the same transform as axi_fd_transform_f64
+ * for any boundary-condition set, used by the FP32 solvers
+ * (kernels/FastDiagonalisationStokesSolver.py:130-156 and
+ * FastDiagonalisationPotentialSolver.py:119-145 with real_dtype float32).
+ * Operands are K-major row-major float; every basis matrix is given as a
+ * TF32 hi part and an FP32 remainder (lo). nr and nz multiples of 4.
+ * ------------------------------------------------------------------ */
+typedef struct axi_tc_transform {
+  int32_t nr, nz;
+  const float* basis[8]; /* E_z^-1 hi, lo (nz, nz); E_r^-1 W hi, lo (nr, nr);
+                            E_z hi, lo (nz, nz); E_r hi, lo (nr, nr) */
+  const float* inv_eig;  /* (nr, nz) */
+  float* in_hi;          /* (nr, nz) split input (axi_tc_split_*) */
+  float* in_lo;
+  float* work[4];        /* X hi, lo (nz, nr); Y hi, lo (nr, nz) */
+  float* out;            /* (nr, nz) */
+} axi_tc_transform;
+
+typedef struct axi_tc_plan_info {
+  int32_t n;             /* transforms in the plan */
+  int32_t n_tiles[4];    /* 128 x 128 output tiles per product stage */
+  int32_t reserved;
+  int64_t bytes;         /* device bytes of the plan */
+} axi_tc_plan_info;
+
+/* Plans n transforms (tensor maps encoded on the host). With plan_dev NULL
+ * only fills `info` (size query); else writes the plan (info->bytes) and
+ * synchronises the stream. */
+int axi_tc_transform_plan(const axi_tc_transform* t, int n, void* plan_dev,
+                          axi_tc_plan_info* info, void* stream);
+/* Runs every transform of the plan (four grouped tensor-core launches). */
+int axi_tc_transform_run(const axi_tc_plan_info* info, const void* plan_dev, void* stream);
+/* Pipeline status of the plan's launches (0 = healthy); synchronises. */
+int axi_tc_transform_status(const axi_tc_plan_info* info, const void* plan_dev, int* tc_error,
+                            void* stream);
+/* TF32 split of n values: hi = x with the low 13 mantissa bits cleared,
+ * lo = x - hi (from float) or fl32(x - hi) (from double). */
+int axi_tc_split_f32(float* hi, float* lo, const float* x, int64_t n, void* stream);
+int axi_tc_split_f64(float* hi, float* lo, const double* x, int64_t n, void* stream);
+/* Residual of one refinement step, in FP64: res = w_i rhs - L psi with
+ * L = A_r (x) I + I (x) A_z the discrete operator the solver inverts. ar, az
+ * hold the sub, main and super diagonal of each row (3 nr, 3 nz doubles);
+ * wrap0 = A_z[0, nz-1], wrap1 = A_z[nz-1, 0] (periodic z, else 0);
+ * row_weight may be NULL (w = 1). */
+int axi_fd_residual_f64(double* res, const double* rhs, const double* psi,
+                        const double* row_weight, const double* ar, const double* az, int nr,
+                        int nz, double wrap0, double wrap1, void* stream);
+/* y += x and y = x (float -> double), n values. */
+int axi_add_f32_to_f64(double* y, const float* x, int64_t n, void* stream);
+int axi_widen_f32_to_f64(double* y, const float* x, int64_t n, void* stream);
+
 /* Allocation-free form of axi_fd_transform_f64 (no counterpart in the
  * reference). For callers that cannot call cudaMalloc: code that captures its
  * time loop into a CUDA graph, or a host whose device memory is owned by

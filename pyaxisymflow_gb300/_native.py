@@ -53,6 +53,14 @@ def _signatures():
         "axi_fd_transform_static_f64": (I, [P, I, P, I, P, P, P, P, P, I, I, P]),
         "axi_dgemm_f64": (I, [P, I, P, I, P, I, P, I, I, I, P]),
         "axi_tf32x3_gemm_work_bytes": (I64, [I, I, I]),
+        "axi_tc_transform_plan": (I, [P, I, P, P, P]),
+        "axi_tc_transform_run": (I, [P, P, P]),
+        "axi_tc_transform_status": (I, [P, P, P, P]),
+        "axi_tc_split_f32": (I, [P, P, P, I64, P]),
+        "axi_tc_split_f64": (I, [P, P, P, I64, P]),
+        "axi_fd_residual_f64": (I, [P, P, P, P, P, P, I, I, D, D, P]),
+        "axi_add_f32_to_f64": (I, [P, P, I64, P]),
+        "axi_widen_f32_to_f64": (I, [P, P, I64, P]),
         "axi_tf32x3_gemm": (I, [P, P, P, I, I, I, P, P]),
         "axi_plan_init": (I, [P, I, I, I, P]),
         "axi_plan_tc_status": (I, [P, P, P, P]),

@@ -30,6 +30,7 @@
 
 #include "axi_common.cuh"
 
+
 namespace axi_tc {
 
 constexpr int BM = 128;

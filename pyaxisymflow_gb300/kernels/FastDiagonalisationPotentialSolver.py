@@ -10,7 +10,7 @@ class FastDiagonalisationPotentialSolver:
     """Solves psi_rr + psi_zz + psi_r / r = rhs by fast diagonalisation."""
 
     def __init__(self, grid_size_r, grid_size_z, dx, real_dtype=np.float64,
-                 bc_type=NEUMANN_ZR, device=None):
+                 bc_type=NEUMANN_ZR, device=None, refine=1):
         self.dx = dx
         self.grid_size_r = grid_size_r
         self.grid_size_z = grid_size_z
@@ -31,8 +31,10 @@ class FastDiagonalisationPotentialSolver:
         vr, er = eig_sorted_desc(pr + dr)
         vz, ez = eig_sorted_desc(pz)
         spectrum = vz.reshape(1, nz) + vr.reshape(nr, 1)
+        precision = "f32" if np.dtype(real_dtype) == np.float32 else "f64"
         self.engine = FastDiagonalisationEngine(vr, er, vz, ez, spectrum, row_weight=None,
-                                                device=device)
+                                                device=device, precision=precision,
+                                                op_r=pr + dr, op_z=pz, refine=refine)
 
     def solve(self, solution_field, rhs_field):
         """solution_field[...] = the potential for rhs_field (CUDA float64)."""

@@ -13,7 +13,7 @@ class FastDiagonalisationStokesSolver:
     -psi_rr - psi_zz + psi_r / r = r * omega by fast diagonalisation."""
 
     def __init__(self, grid_size_r, grid_size_z, dx, real_dtype=np.float64,
-                 bc_type=NEUMANN_ZR, device=None):
+                 bc_type=NEUMANN_ZR, device=None, refine=1):
         self.dx = dx
         self.grid_size_r = grid_size_r
         self.grid_size_z = grid_size_z
@@ -47,11 +47,18 @@ class FastDiagonalisationStokesSolver:
         vr, er = eig_sorted_desc(pr - dr)
         vz, ez = eig_sorted_desc(pz)
         spectrum = vz.reshape(1, nz) + vr.reshape(nr, 1)
+        precision = "f32" if np.dtype(real_dtype) == np.float32 else "f64"
         self.engine = FastDiagonalisationEngine(vr, er, vz, ez, spectrum,
                                                 row_weight=self.radial_coord.ravel(),
-                                                device=device)
+                                                device=device, precision=precision,
+                                                op_r=pr - dr, op_z=pz, refine=refine)
 
     def solve(self, solution_field, rhs_field):
-        """solution_field[...] = psi solving the pseudo Poisson for rhs_field
-        (CUDA float64 tensors; rows may be strided, e.g. field[:, g:-g])."""
+        """solution_field[...] = psi solving the pseudo Poisson for rhs_field.
+
+        real_dtype float64: FP64 products; CUDA float64 tensors, rows may be
+        strided (e.g. field[:, g:-g]). real_dtype float32: the products run on
+        the tcgen05 tensor cores (3xTF32, FP32 accumulation), followed by
+        `refine` steps of iterative refinement with an FP64 residual; fields
+        may be float32 or float64 (the refined result is kept in FP64)."""
         self.engine.transform(solution_field, rhs_field)

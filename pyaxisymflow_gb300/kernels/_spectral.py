@@ -11,6 +11,8 @@ numpy >= 2 returns complex eigenvectors even when all imaginary parts are
 zero (the numpy the reference pins returned real ones then); the imaginary
 parts are checked to be exactly zero and dropped.
 """
+import ctypes
+
 import numpy as np
 import torch
 
@@ -52,16 +54,59 @@ def _row_stride(t, nr, nz, name):
     return t.stride(0)
 
 
+def tf32_split(x):
+    """TF32 hi part (low 13 mantissa bits of fl32(x) cleared) and the FP32
+    remainder fl32(x - hi), from a float64 array."""
+    x32 = np.asarray(x, dtype=np.float32)
+    hi = (x32.view(np.uint32) & np.uint32(0xFFFFE000)).view(np.float32)
+    lo = (np.asarray(x, dtype=np.float64) - hi.astype(np.float64)).astype(np.float32)
+    return hi, lo
+
+
+def tridiagonals(mat):
+    """(sub, main, super) diagonal of each row of a tridiagonal matrix."""
+    n = mat.shape[0]
+    out = np.zeros((n, 3))
+    i = np.arange(n)
+    out[:, 1] = mat[i, i]
+    out[1:, 0] = mat[i[1:], i[1:] - 1]
+    out[:-1, 2] = mat[i[:-1], i[:-1] + 1]
+    return out
+
+
+class AxiTcTransform(ctypes.Structure):
+    """Mirror of ``axi_tc_transform`` in include/axisym_gb300.h."""
+    _fields_ = [("nr", ctypes.c_int32), ("nz", ctypes.c_int32),
+                ("basis", ctypes.c_void_p * 8), ("inv_eig", ctypes.c_void_p),
+                ("in_hi", ctypes.c_void_p), ("in_lo", ctypes.c_void_p),
+                ("work", ctypes.c_void_p * 4), ("out", ctypes.c_void_p)]
+
+
+class AxiTcPlanInfo(ctypes.Structure):
+    """Mirror of ``axi_tc_plan_info`` in include/axisym_gb300.h."""
+    _fields_ = [("n", ctypes.c_int32), ("n_tiles", ctypes.c_int32 * 4),
+                ("reserved", ctypes.c_int32), ("bytes", ctypes.c_int64)]
+
+
 class FastDiagonalisationEngine:
-    """Device copy of one eigenbasis set and the transform that applies it."""
+    """Device copy of one eigenbasis set and the transform that applies it.
+
+    precision "f64": four FP64 products (axi_fd_transform_f64).
+    precision "f32": four tcgen05 3xTF32 products (axi_tc_transform_run), then
+    `refine` steps of iterative refinement with the residual of the discrete
+    operator A_r (x) I + I (x) A_z computed in FP64 (op_r, op_z are those
+    1-D matrices, wrap entries included).
+    """
 
     def __init__(self, eig_vals_r, eig_vecs_r, eig_vals_z, eig_vecs_z, spectrum, row_weight,
-                 device=None):
+                 device=None, precision="f64", op_r=None, op_z=None, refine=1):
         nr, nz = spectrum.shape
         self.grid_size_r, self.grid_size_z = nr, nz
         dev = torch.device("cuda", torch.cuda.current_device()) if device is None \
             else torch.device(device)
         self.device = dev
+        self.precision = precision
+        self.refine = refine
         inv_r = np.linalg.inv(eig_vecs_r)
         if row_weight is not None:
             inv_r = inv_r * row_weight.reshape(1, nr)
@@ -74,15 +119,105 @@ class FastDiagonalisationEngine:
         )
         self.host = host
         self.eig_vals_r, self.eig_vals_z = eig_vals_r, eig_vals_z
-        self.dev = {k: torch.tensor(np.ascontiguousarray(v), dtype=torch.float64, device=dev)
-                    for k, v in host.items()}
-        self.work = torch.empty(2 * nr * nz, dtype=torch.float64, device=dev)
+        if precision == "f64":
+            self.dev = {k: torch.tensor(np.ascontiguousarray(v), dtype=torch.float64, device=dev)
+                        for k, v in host.items()}
+            self.work = torch.empty(2 * nr * nz, dtype=torch.float64, device=dev)
+        elif precision == "f32":
+            self._setup_tc(host, row_weight, op_r, op_z)
+        else:
+            raise ValueError("precision must be 'f64' or 'f32'")
+
+    def _setup_tc(self, host, row_weight, op_r, op_z):
+        nr, nz = self.grid_size_r, self.grid_size_z
+        if nr % 4 or nz % 4:
+            raise ValueError("the tensor-core solve needs nr and nz multiples of 4")
+        dev = self.device
+        f32 = dict(dtype=torch.float32, device=dev)
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.tc_basis = []
+        for m in (host["EzinvT"].T, host["Er_inv_w"], host["EzT"].T, host["Er"]):
+            hi, lo = tf32_split(np.ascontiguousarray(m))
+            self.tc_basis += [torch.tensor(hi, device=dev), torch.tensor(lo, device=dev)]
+        self.tc_inv_eig = torch.tensor(host["inv_eig"], **f32)
+        self.tc_in = [torch.empty((nr, nz), **f32) for _ in range(2)]
+        self.tc_work = [torch.empty(nr * nz, **f32) for _ in range(4)]
+        self.tc_out = torch.empty((nr, nz), **f32)
+        self.tc_psi = torch.empty((nr, nz), **f64)
+        self.tc_res = torch.empty((nr, nz), **f64)
+        self.weight = (torch.tensor(np.ascontiguousarray(row_weight), **f64)
+                       if row_weight is not None else None)
+        self.op_r = torch.tensor(tridiagonals(op_r), **f64) if op_r is not None else None
+        self.op_z = torch.tensor(tridiagonals(op_z), **f64) if op_z is not None else None
+        self.wrap = (float(op_z[0, -1]), float(op_z[-1, 0])) if op_z is not None else (0.0, 0.0)
+        t = AxiTcTransform()
+        t.nr, t.nz = nr, nz
+        for q in range(8):
+            t.basis[q] = self.tc_basis[q].data_ptr()
+        t.inv_eig = self.tc_inv_eig.data_ptr()
+        t.in_hi, t.in_lo = self.tc_in[0].data_ptr(), self.tc_in[1].data_ptr()
+        for q in range(4):
+            t.work[q] = self.tc_work[q].data_ptr()
+        t.out = self.tc_out.data_ptr()
+        self.tc_t = t
+        self.tc_info = AxiTcPlanInfo()
+        s = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        N.call("axi_tc_transform_plan", ctypes.byref(t), 1, None, ctypes.byref(self.tc_info), s)
+        self.tc_plan = torch.empty(int(self.tc_info.bytes), dtype=torch.uint8, device=dev)
+        N.call("axi_tc_transform_plan", ctypes.byref(t), 1, N.ptr(self.tc_plan),
+               ctypes.byref(self.tc_info), s)
+
+    def _tc_run(self, s):
+        N.call("axi_tc_transform_run", ctypes.byref(self.tc_info), N.ptr(self.tc_plan), s)
+
+    def tc_status(self):
+        err = ctypes.c_int(0)
+        N.call("axi_tc_transform_status", ctypes.byref(self.tc_info), N.ptr(self.tc_plan),
+               ctypes.byref(err), ctypes.c_void_p(torch.cuda.current_stream(
+                   self.device).cuda_stream))
+        return err.value
 
     def transform(self, out, inp):
         nr, nz = self.grid_size_r, self.grid_size_z
+        if self.precision == "f32":
+            self._transform_tc(out, inp)
+            return
         ld_in = _row_stride(inp, nr, nz, "rhs_field")
         ld_out = _row_stride(out, nr, nz, "solution_field")
         d = self.dev
         N.call("axi_fd_transform_f64", N.ptr(out), ld_out, N.ptr(inp), ld_in,
                N.ptr(d["Er_inv_w"]), N.ptr(d["EzinvT"]), N.ptr(d["inv_eig"]), N.ptr(d["Er"]),
                N.ptr(d["EzT"]), N.ptr(self.work), nr, nz, N.stream_of(out))
+
+    def _transform_tc(self, out, inp):
+        nr, nz = self.grid_size_r, self.grid_size_z
+        for t, name in ((inp, "rhs_field"), (out, "solution_field")):
+            if not isinstance(t, torch.Tensor) or not t.is_cuda:
+                raise ValueError(f"{name} must be a CUDA tensor (there is no CPU path)")
+            if tuple(t.shape) != (nr, nz) or t.dtype not in (torch.float32, torch.float64):
+                raise ValueError(f"{name} must be a float32 / float64 tensor of shape {(nr, nz)}")
+        s = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        x = inp.contiguous()
+        n = nr * nz
+        hi, lo = self.tc_in
+        if x.dtype == torch.float64:
+            N.call("axi_tc_split_f64", N.ptr(hi), N.ptr(lo), N.ptr(x), n, s)
+        else:
+            N.call("axi_tc_split_f32", N.ptr(hi), N.ptr(lo), N.ptr(x), n, s)
+        self._tc_run(s)
+        if not self.refine:
+            out.copy_(self.tc_out)
+            return
+        if self.op_r is None:
+            raise ValueError("refinement needs the discrete operator")
+        psi, res = self.tc_psi, self.tc_res
+        N.call("axi_widen_f32_to_f64", N.ptr(psi), N.ptr(self.tc_out), n, s)
+        x64 = x if x.dtype == torch.float64 else x.double()
+        for _ in range(self.refine):
+            N.call("axi_fd_residual_f64", N.ptr(res), N.ptr(x64), N.ptr(psi),
+                   N.ptr(self.weight) if self.weight is not None else None, N.ptr(self.op_r),
+                   N.ptr(self.op_z), nr, nz, self.wrap[0], self.wrap[1], s)
+            N.call("axi_tc_split_f64", N.ptr(hi), N.ptr(lo), N.ptr(res), n, s)
+            self._tc_run(s)
+            N.call("axi_add_f32_to_f64", N.ptr(psi), N.ptr(self.tc_out), n, s)
+        out.copy_(psi)

@@ -8,7 +8,7 @@ class ImplicitEulerDiffusionStepper:
     """Implicit Euler step (I - nu dt L)^-1 of axisymmetric vorticity diffusion."""
 
     def __init__(self, time_step, kinematic_viscosity, grid_size_r, grid_size_z, dx,
-                 real_dtype=np.float64, device=None):
+                 real_dtype=np.float64, device=None, refine=1):
         self.time_step = time_step
         self.nu_times_dt = time_step * kinematic_viscosity
         self.dx = dx
@@ -26,8 +26,12 @@ class ImplicitEulerDiffusionStepper:
         vr, er = eig_sorted_desc(pr + npr)
         vz, ez = eig_sorted_desc(pz)
         spectrum = 1.0 - self.nu_times_dt * (vz.reshape(1, nz) + vr.reshape(nr, 1))
-        self.engine = FastDiagonalisationEngine(vr, er, vz, ez, spectrum, row_weight=None,
-                                                device=device)
+        precision = "f32" if np.dtype(real_dtype) == np.float32 else "f64"
+        # the operator inverted: (I - nu dt A_r) (x) I + I (x) (-nu dt A_z)
+        self.engine = FastDiagonalisationEngine(
+            vr, er, vz, ez, spectrum, row_weight=None, device=device, precision=precision,
+            op_r=np.identity(nr) - self.nu_times_dt * (pr + npr), op_z=-self.nu_times_dt * pz,
+            refine=refine)
 
     def step(self, vorticity_field, dt):
         """Performs an implicit Euler timestep for diffusion in axisym

@@ -48,3 +48,18 @@ def test_rigid_sphere_full_size_against_oracle(steps):
         err = rel_l2(t.cpu().numpy(), ref)
         assert err < 1e-12, (f, err)
     assert abs(s.Cd - st.Cd) <= 1e-10 * abs(st.Cd)
+
+
+def test_soft_sphere_loop_against_golden(golden):
+    """Elasto path end to end: eta advection, level-set pinning, least-squares
+    extrapolation, neo-Hookean stress and its curl, tether penalisation."""
+    from pyaxisymflow_gb300.simulation import SoftSphereSimulation
+    g = golden("soft")
+    case = sim.SoftSphereCase(nz=64, nr=32, dx=1.0 / 64, r_ball=0.15, lam=1e6)
+    s = SoftSphereSimulation(case, device="cuda")
+    s.run(12)
+    for f, t in (("omega", s.vorticity), ("eta1", s.eta1), ("eta2", s.eta2),
+                 ("phi", s.ball_phi), ("chi", s.ball_char_func)):
+        err = rel_l2(t.cpu().numpy(), g[f"soft/{f}_12"])
+        assert err < 1e-12, (f, err)
+    assert abs(s.t - float(g["soft/t_12"])) <= 1e-13 * float(g["soft/t_12"])
