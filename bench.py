@@ -13,6 +13,10 @@ Workloads (synthetic, seeded; there is no dataset):
               [10, 1000] (velocity scale 1), sphere radius uniform in
               [0.04, 0.12], density ratio uniform in [1.5, 4], seed 4
   sphere512   one 512 x 256 rigid sphere, Re 100, radius 0.0625 at z = 0.5
+  poisson2048 isolated streamfunction solves, 2048 x 1024, periodic z, a sum
+              of 32 Gaussian vortex rings (seed 3); FP32 tensor-core solve +
+              one FP64 refinement step vs plain FP64
+  serve       continuous-batching server on a Poisson request stream
 
 --impl reference times the reference's CPU path restated by the oracle
 (numpy FP64, all host cores for BLAS) on a bounded sample of the same
@@ -224,19 +228,20 @@ def run_gb300(args, world, rank, local):
     with ClockSampler(local) as clocks:
         torch.cuda.synchronize(dev)
         barrier(world)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
+        evs_t = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+        evs_t[0].record(stream)
+        for k in range(args.steps):
             ens.replay()
-        e1.record(stream)
+            evs_t[k + 1].record(stream)
         torch.cuda.synchronize(dev)
         barrier(world)
-    ms = e0.elapsed_time(e1)
+    step_ms = [evs_t[k].elapsed_time(evs_t[k + 1]) for k in range(args.steps)]
+    ms = evs_t[0].elapsed_time(evs_t[-1])
     ms = max_over_ranks(world, ms)
     ms_per_step = ms / args.steps
     value = cells * world / (ms_per_step / 1000.0)
     status = ens.status()
+    uses_tc = ens.tensor_cores
     # ---- per-phase device times (same stream, same step sequence) -------------
     ph_ms = {p: 0.0 for p in PHASES}
     nph = max(3, min(args.steps, 10))
@@ -276,11 +281,48 @@ def run_gb300(args, world, rank, local):
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_s = max_over_ranks(world, e2e_s)
     e2e_value = cells * world / e2e_s
+    # ---- plain FP64 GPU path on the same workload, and the FP32 error -------------
+    fp64 = None
+    if args.precision == "f32" and not args.no_fp64_compare:
+        del ens
+        torch.cuda.empty_cache()
+        e64 = RigidEnsemble(cases, precision="f64", device=dev)
+        e64.step(1)
+        torch.cuda.synchronize(dev)
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        nf = 3
+        f0.record(stream)
+        e64.step(nf)
+        f1.record(stream)
+        torch.cuda.synchronize(dev)
+        fp64_ms = f0.elapsed_time(f1) / nf
+        del e64
+        torch.cuda.empty_cache()
+        # accuracy of the FP32 engine against the FP64 engine (itself within
+        # 1e-12 of the FP64 oracle) after many steps on one case of each size
+        errs = {}
+        nsteps = 300
+        for nz in sorted({c.nz for c in cases}):
+            c = next(c for c in cases if c.nz == nz)
+            a = RigidEnsemble([c], precision="f64", device=dev)
+            b = RigidEnsemble([c], precision="f32", device=dev)
+            a.step(nsteps)
+            b.step(nsteps)
+            torch.cuda.synchronize(dev)
+            for f in ("omega", "psi", "u_z", "u_r"):
+                x = b.fields[0][f].double()
+                y = a.fields[0][f]
+                e = float(torch.linalg.norm(x - y) / torch.linalg.norm(y))
+                errs[f] = max(errs.get(f, 0.0), e)
+        fp64 = {"value": cells * world / (fp64_ms / 1000.0), "ms_per_step": fp64_ms,
+                "speedup_fp32_over_fp64": fp64_ms / ms_per_step,
+                "rel_l2_fp32_vs_fp64_max_over_sizes": errs, "accuracy_steps": nsteps}
     # ---- roofline of the dominant kernel ---------------------------------------
     hbm, bf16, src = peaks()
     dom = max(ph_ms, key=ph_ms.get)
     esize = 8 if args.precision == "f64" else 4
-    if ens.tensor_cores:
+    if uses_tc:
         PHASE_FIELDS["advect_diffuse"] += 2
     if any(c.sediment for c in cases):
         PHASE_FIELDS["advect_diffuse"] += 1
@@ -288,11 +330,14 @@ def run_gb300(args, world, rank, local):
         flops = sum(4.0 * c.nr * c.nz * (c.nr + c.nz) for c in cases)
         achieved = flops / (ph_ms[dom] / 1000.0) / 1e12
         if args.precision == "f64":
-            roof = {"bound": "fp64", "achieved": achieved, "peak": 1.05, "unit": "TFLOP/s",
-                    "peak_source": "DMMA/DFMA throughput probe on this pool's GB300"}
+            roof = {"bound": "fp64", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
+                    "peak_source": "nominal GB300 FP64 (DFMA probe on this pool: 1.0)"}
         else:
-            roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-                    "peak_source": f"{src} bf16"}
+            # 3xTF32: three tensor products per useful product; the TF32 dense
+            # rate is half the BF16 rate
+            roof = {"bound": "tensor", "achieved": 3 * achieved, "peak": bf16 / 2,
+                    "unit": "TFLOP/s", "useful_tflops": achieved,
+                    "peak_source": f"{src} bf16 / 2 (TF32 dense rate)"}
     else:
         nbytes = sum(PHASE_FIELDS[dom] * esize * c.nr * c.nz for c in cases)
         achieved = nbytes / (ph_ms[dom] / 1000.0) / 1e9
@@ -313,6 +358,9 @@ def run_gb300(args, world, rank, local):
                    "parallelism": f"case-parallel replicas x{world}"},
         "roofline": roof,
         "phase_ms": ph_ms,
+        "step_latency_ms": {"p50": float(np.percentile(step_ms, 50)),
+                            "p99": float(np.percentile(step_ms, 99))},
+        "plain_fp64": fp64,
         "stencil_hbm_gbs": stencil_bytes / (stencil_ms / 1000.0) / 1e9,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
@@ -334,21 +382,194 @@ def run_gb300(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def vortex_rings(nr, nz, dx, seed=3, n=32):
+    """Seeded sum of axisymmetric Gaussian vortex rings: centres z ~ U(0, Lz),
+    r ~ U(0.1, 0.9) Lr, radii U[0.02, 0.2], strengths N(0, 1)."""
+    rng = np.random.default_rng(seed)
+    z = (np.arange(nz) + 0.5) * dx
+    r = (np.arange(nr) + 0.5) * dx
+    Z, R = np.meshgrid(z, r)
+    w = np.zeros((nr, nz))
+    for _ in range(n):
+        zc, rc = rng.uniform(0, nz * dx), rng.uniform(0.1, 0.9) * nr * dx
+        rad, st = rng.uniform(0.02, 0.2), rng.standard_normal()
+        w += st * np.exp(-((Z - zc) ** 2 + (R - rc) ** 2) / rad ** 2)
+    return w, Z, R
+
+
+def run_poisson(args, world, rank, local):
+    """Isolated streamfunction solves, 2048 x 1024 (nz x nr), periodic z,
+    Neumann r: FP32 tensor-core solve + one FP64-residual refinement vs the
+    plain FP64 solve, with errors of psi and velocity."""
+    import torch
+    from pyaxisymflow_gb300.kernels.compute_velocity_from_psi import \
+        compute_velocity_from_psi_unb
+    from pyaxisymflow_gb300.kernels.FastDiagonalisationStokesSolver import \
+        FastDiagonalisationStokesSolver
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nz, nr = 2048, 1024
+    dx = 1.0 / nr
+    bc = "homogenous_neumann_along_r_and_periodic_along_z"
+    w, Z, R = vortex_rings(nr, nz, dx)
+    tw = torch.tensor(w, dtype=torch.float64, device=dev)
+    tR = torch.tensor(R, dtype=torch.float64, device=dev)
+    s64 = FastDiagonalisationStokesSolver(nr, nz, dx, bc_type=bc, device=dev)
+    s32 = FastDiagonalisationStokesSolver(nr, nz, dx, bc_type=bc, device=dev,
+                                          real_dtype=np.float32, refine=1)
+    psi64, psi32 = torch.zeros_like(tw), torch.zeros_like(tw)
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn, k):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize(dev)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(k + 1)]
+        ev[0].record(stream)
+        for q in range(k):
+            fn()
+            ev[q + 1].record(stream)
+        torch.cuda.synchronize(dev)
+        return [ev[q].elapsed_time(ev[q + 1]) for q in range(k)]
+
+    with ClockSampler(local) as clocks:
+        t32 = timed(lambda: s32.solve(psi32, tw), args.steps)
+    t64 = timed(lambda: s64.solve(psi64, tw), max(3, args.steps // 4))
+    tc_ms = timed(lambda: s32.engine._tc_run(ctypes_stream(stream)), args.steps)
+    uz64, ur64, uz32, ur32 = (torch.zeros_like(tw) for _ in range(4))
+    compute_velocity_from_psi_unb(uz64, ur64, psi64, tR, dx)
+    compute_velocity_from_psi_unb(uz32, ur32, psi32, tR, dx)
+
+    def rel(a, b):
+        return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+
+    s_norefine = FastDiagonalisationStokesSolver(nr, nz, dx, bc_type=bc, device=dev,
+                                                 real_dtype=np.float32, refine=0)
+    p0 = torch.zeros_like(tw)
+    s_norefine.solve(p0, tw)
+    cells = nr * nz
+    ms32 = float(np.mean(t32))
+    ms64 = float(np.mean(t64))
+    flops = 4.0 * nr * nz * (nr + nz)
+    tcm = float(np.mean(tc_ms))
+    hbm, bf16, src = peaks()
+    # e2e: host rhs in (pinned), solve, psi out
+    host_in = torch.tensor(w, dtype=torch.float64).pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        tw.copy_(host_in, non_blocking=True)
+        s32.solve(psi32, tw)
+        host_out.copy_(psi32, non_blocking=True)
+        torch.cuda.synchronize(dev)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    line = {
+        "metric": METRIC, "value": cells / (ms32 / 1000.0), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "poisson2048", "grid": "nz 2048 x nr 1024", "bc": bc,
+                   "rhs": "32 Gaussian vortex rings, seed 3", "step": "one streamfunction solve",
+                   "refinement_steps": 1},
+        "roofline": {"bound": "tensor", "kernel": "tf32x3_gemm (4 products)",
+                     "achieved": 3 * flops / (tcm / 1000.0) / 1e12, "peak": bf16 / 2,
+                     "unit": "TFLOP/s", "useful_tflops": flops / (tcm / 1000.0) / 1e12,
+                     "peak_source": f"{src} bf16 / 2 (TF32 dense rate)", "traffic": None},
+        "step_latency_ms": {"p50": float(np.percentile(t32, 50)),
+                            "p99": float(np.percentile(t32, 99))},
+        "plain_fp64": {"value": cells / (ms64 / 1000.0), "ms_per_step": ms64,
+                       "speedup_fp32_over_fp64": ms64 / ms32},
+        "rel_l2_vs_fp64": {"psi": rel(psi32, psi64), "u_z": rel(uz32, uz64),
+                           "u_r": rel(ur32, ur64), "psi_without_refinement": rel(p0, psi64)},
+        "e2e": {"value": cells / e2e_s, "unit": UNIT, "h2d_bytes_per_step": cells * 8,
+                "d2h_bytes_per_step": cells * 8},
+        "gpu_launches": args.steps * (2 + 4 + 4 + 3),
+        "clocks": clocks.summary(),
+        "status_ok": s32.engine.tc_status() == 0,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def ctypes_stream(stream):
+    import ctypes
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def run_serve(args, world, rank, local):
+    """Continuous-batching server on a Poisson stream of requests (mean 20/s):
+    grids 256 x 128 .. 2048 x 1024, sphere / torus / spheroid, 500-5000 steps,
+    Re log-uniform in [10, 500], 80% HBM budget."""
+    import torch
+    from pyaxisymflow_gb300.engine import RigidEnsemble
+    from pyaxisymflow_gb300.serving import SimulationServer, poisson_requests
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    reqs = poisson_requests(args.requests, rate_per_s=20.0, seed=5)
+    server = SimulationServer(precision=args.precision, device=dev, hbm_budget=0.8)
+    server.prepare([r.case for r in reqs])
+    with ClockSampler(local) as clocks:
+        report = server.run(reqs)
+    summ = report.summary()
+    # plain sequential FP64 on the same GPU: per-size step time of one case
+    # alone, applied to the same request list
+    per_size = {}
+    for r in reqs:
+        key = (r.case.nz, r.case.nr)
+        if key in per_size:
+            continue
+        e = RigidEnsemble([r.case], precision="f64", device=dev)
+        e.step(2)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        e.step(5)
+        torch.cuda.synchronize(dev)
+        per_size[key] = (time.perf_counter() - t0) / 5
+        del e
+    seq_s = sum(per_size[(r.case.nz, r.case.nr)] * r.steps for r in reqs)
+    seq_cells = sum(r.case.nz * r.case.nr * r.steps for r in reqs)
+    line = {
+        "metric": METRIC, "value": summ["cell_updates_per_s"], "unit": UNIT, "n_gpus": world,
+        "steps": sum(len(report.step_latency_s) for _ in [0]), "warmup": 0,
+        "ms_per_step": summ["step_p50_ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.precision, "data": "synthetic",
+        "config": {"workload": "serve", "requests": len(reqs), "arrival_rate_per_s": 20.0,
+                   "grids": "nz in {256, 512, 1024, 2048}, nr = nz / 2",
+                   "bodies": "sphere / torus / spheroid (aspect U[0.5, 2])",
+                   "steps_per_request": "U{500..5000}", "hbm_budget": 0.8, "seed": 5},
+        "serving": summ,
+        "plain_fp64_sequential": {"value": seq_cells / seq_s, "wall_s_estimate": seq_s,
+                                  "speedup_served_over_sequential_fp64":
+                                      summ["cell_updates_per_s"] / (seq_cells / seq_s)},
+        "clocks": clocks.summary(),
+        "gpu_launches": 8 * len(report.step_latency_s),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="ensemble64", choices=["ensemble64", "sphere512"])
+    ap.add_argument("--workload", default="ensemble64",
+                    choices=["ensemble64", "sphere512", "poisson2048", "serve"])
+    ap.add_argument("--requests", type=int, default=40)
     ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-compare", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "poisson2048":
+        run_poisson(args, world, rank, local)
+    elif args.workload == "serve":
+        run_serve(args, world, rank, local)
     else:
         run_gb300(args, world, rank, local)
 

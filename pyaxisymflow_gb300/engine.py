@@ -168,11 +168,110 @@ class _Bases:
                 self.tc.append(torch.tensor(lo, device=device))
 
 
+class CaseState:
+    """Device-resident fields and per-case state of one case of an ensemble.
+
+    It survives re-planning, so cases can join and leave an ensemble between
+    steps (continuous batching) without disturbing the others."""
+
+    def __init__(self, ens, case, slot, history_steps=0, initial_vorticity=None):
+        self.case = c = case
+        self.slot = slot
+        dev = ens.device
+        dtype = ens.dtype
+        f = dict(dtype=dtype, device=dev)
+        f64 = dict(dtype=torch.float64, device=dev)
+        z, r = grid(c.nz, c.nr, c.dx)
+        Z, R = np.meshgrid(z, r)
+        b = ens._bases_for(c)
+        self.bases = b
+        if initial_vorticity is not None:
+            w0 = np.asarray(initial_vorticity, dtype=np.float64)
+        else:
+            w0 = c.noise * np.random.default_rng(c.seed).standard_normal((c.nr, c.nz))
+        chi64 = torch.zeros((c.nr, c.nz), **f64)
+        smooth_Heaviside(chi64, torch.tensor(c.level_set(Z, R), **f64), c.moll_zone)
+        t = dict(
+            omega=torch.tensor(w0, **f64).to(dtype),
+            psi=torch.zeros((c.nr, c.nz), **f),
+            u_z=torch.zeros((c.nr, c.nz), **f),
+            u_r=torch.zeros((c.nr, c.nz), **f),
+            chi=chi64.to(dtype),
+            kill_coef=torch.tensor(kill_coefficients(z, r, c.kill_width, c.dx), **f64),
+            r=torch.tensor(r, **f64),
+            z=torch.tensor(z, **f64),
+            rinv2dx=torch.tensor(1.0 / (2 * c.dx * r), **f64).to(dtype),
+            rinv2=torch.tensor(1.0 / (r * r), **f64).to(dtype),
+            rw=torch.tensor(r, **f64).to(dtype),
+            zw=torch.tensor(z, **f64).to(dtype),
+            gemm_work=torch.zeros(2 * c.nr * c.nz, **f),
+            partials=torch.zeros(2 * ((c.nr + 15) // 16) * ((c.nz + 63) // 64) + 8, **f64),
+        )
+        if ens.tensor_cores:
+            whi, wlo = tf32_split(w0)
+            t["omega_hi"] = torch.tensor(whi, device=dev)
+            t["omega_lo"] = torch.tensor(wlo, device=dev)
+            t["tc_work"] = [torch.zeros(c.nr * c.nz, dtype=torch.float32, device=dev)
+                            for _ in range(4)]
+        self.fields = t
+        self.history = (torch.zeros((history_steps, 2), **f64) if history_steps else None)
+        st = ens.state_arena[slot]
+        st.zero_()
+        s = AxiCase()
+        s.nr, s.nz, s.kill_width = c.nr, c.nz, c.kill_width
+        s.dx, s.nu, s.lam, s.U0 = c.dx, c.nu, c.lam, c.U0
+        s.t_ramp = c.t_ramp if c.ramp else 0.0
+        s.cfl, s.U_body = c.cfl, c.U_body
+        s.cd_scale = 2 * 2 * math.pi * c.dx * c.dx * c.lam / (math.pi * c.r_sphere ** 2)
+        s.dt_diff = 0.9 * c.dx ** 2 / 4 / c.nu
+        s.eps = float(np.finfo(float).eps)
+        s.inv_dx2 = 1.0 / (c.dx * c.dx)
+        s.inv_2dx = 0.5 / c.dx
+        if c.sediment:
+            if c.body != "sphere":
+                raise ValueError("sedimenting bodies are spheres")
+            # falling_rigid_sphere.py:71-73 (mass and volume from the initial mask)
+            chi_h = chi64.cpu().numpy()
+            s.flags = CASE_SEDIMENTING
+            s.rho_f, s.rho_s = c.rho_f, c.rho_s
+            s.grav = (c.rho_s - c.rho_f) * c.gravity
+            s.part_mass = 2 * np.pi * c.dx * c.dx * c.rho_s * np.sum(chi_h * R)
+            s.part_vol = 2 * np.pi * c.dx * c.dx * np.sum(chi_h * R)
+            s.r_body = c.r_sphere
+            s.blend_w = c.moll_zone
+            st[ST_ZCM] = c.z_cm
+        for name in ("omega", "psi", "u_z", "u_r", "chi", "kill_coef", "r", "z",
+                     "rinv2dx", "rinv2", "rw", "zw", "gemm_work", "partials"):
+            setattr(s, name, t[name].data_ptr())
+        for name, v in b.t.items():
+            setattr(s, name, v.data_ptr())
+        if ens.tensor_cores:
+            s.omega_hi = t["omega_hi"].data_ptr()
+            s.omega_lo = t["omega_lo"].data_ptr()
+            for q in range(8):
+                s.tc_basis[q] = b.tc[q].data_ptr()
+            for q in range(4):
+                s.tc_work[q] = t["tc_work"][q].data_ptr()
+        s.state = st.data_ptr()
+        if self.history is not None:
+            s.history = self.history.data_ptr()
+            s.history_len = history_steps
+        self.struct = s
+
+    def nbytes(self):
+        n = 0
+        for v in self.fields.values():
+            for x in (v if isinstance(v, list) else [v]):
+                n += x.numel() * x.element_size()
+        return n
+
+
 class RigidEnsemble:
-    """All cases resident on one GPU, advanced together."""
+    """Cases resident on one GPU, advanced together by one launch sequence per
+    step. Cases may join (add_case) and leave (remove_case) between steps."""
 
     def __init__(self, cases, precision="f64", device="cuda", history_steps=0,
-                 initial_vorticity=None, tensor_cores=None):
+                 initial_vorticity=None, tensor_cores=None, capacity=None):
         if precision not in ("f64", "f32"):
             raise ValueError("precision must be 'f64' or 'f32'")
         if tensor_cores is None:
@@ -183,102 +282,51 @@ class RigidEnsemble:
         self.precision = precision
         self.dtype = torch.float64 if precision == "f64" else torch.float32
         self.device = torch.device(device)
-        self.cases = list(cases)
-        self._keep = []
-        bases = {}
-        n = len(self.cases)
-        self.structs = (AxiCase * n)()
-        self.fields = []
-        self.state = torch.zeros((n, ST_WORDS), dtype=torch.float64, device=self.device)
-        self.history = (torch.zeros((n, max(history_steps, 1), 2), dtype=torch.float64,
-                                    device=self.device) if history_steps else None)
-        f = dict(dtype=self.dtype, device=self.device)
-        f64 = dict(dtype=torch.float64, device=self.device)
-        for k, c in enumerate(self.cases):
-            z, r = grid(c.nz, c.nr, c.dx)
-            Z, R = np.meshgrid(z, r)
-            key = (c.nr, c.nz, c.dx)
-            if key not in bases:
-                bases[key] = _Bases(c.nr, c.nz, c.dx, self.dtype, self.device,
-                                    tensor_cores=tensor_cores)
-            b = bases[key]
-            if initial_vorticity is not None and initial_vorticity[k] is not None:
-                w0 = np.asarray(initial_vorticity[k], dtype=np.float64)
-            else:
-                w0 = c.noise * np.random.default_rng(c.seed).standard_normal((c.nr, c.nz))
-            chi64 = torch.zeros((c.nr, c.nz), **f64)
-            smooth_Heaviside(chi64, torch.tensor(c.level_set(Z, R), **f64), c.moll_zone)
-            t = dict(
-                omega=torch.tensor(w0, **f64).to(self.dtype),
-                psi=torch.zeros((c.nr, c.nz), **f),
-                u_z=torch.zeros((c.nr, c.nz), **f),
-                u_r=torch.zeros((c.nr, c.nz), **f),
-                chi=chi64.to(self.dtype),
-                kill_coef=torch.tensor(kill_coefficients(z, r, c.kill_width, c.dx), **f64),
-                r=torch.tensor(r, **f64),
-                z=torch.tensor(z, **f64),
-                rinv2dx=torch.tensor(1.0 / (2 * c.dx * r), **f64).to(self.dtype),
-                rinv2=torch.tensor(1.0 / (r * r), **f64).to(self.dtype),
-                rw=torch.tensor(r, **f64).to(self.dtype),
-                zw=torch.tensor(z, **f64).to(self.dtype),
-                gemm_work=torch.zeros(2 * c.nr * c.nz, **f),
-                partials=torch.zeros(2 * ((c.nr + 15) // 16) * ((c.nz + 63) // 64) + 8, **f64),
-            )
-            if tensor_cores:
-                whi, wlo = tf32_split(w0)
-                t["omega_hi"] = torch.tensor(whi, device=self.device)
-                t["omega_lo"] = torch.tensor(wlo, device=self.device)
-                t["tc_work"] = [torch.zeros(c.nr * c.nz, dtype=torch.float32, device=self.device)
-                                for _ in range(4)]
-            self.fields.append(t)
-            s = self.structs[k]
-            s.nr, s.nz, s.kill_width = c.nr, c.nz, c.kill_width
-            s.dx, s.nu, s.lam, s.U0 = c.dx, c.nu, c.lam, c.U0
-            s.t_ramp = c.t_ramp if c.ramp else 0.0
-            s.cfl, s.U_body = c.cfl, c.U_body
-            s.cd_scale = 2 * 2 * math.pi * c.dx * c.dx * c.lam / (math.pi * c.r_sphere ** 2)
-            s.dt_diff = 0.9 * c.dx ** 2 / 4 / c.nu
-            s.eps = float(np.finfo(float).eps)
-            s.inv_dx2 = 1.0 / (c.dx * c.dx)
-            s.inv_2dx = 0.5 / c.dx
-            if c.sediment:
-                if c.body != "sphere":
-                    raise ValueError("sedimenting bodies are spheres")
-                # falling_rigid_sphere.py:71-73 (mass and volume from the initial mask)
-                chi_h = chi64.cpu().numpy()
-                s.flags = CASE_SEDIMENTING
-                s.rho_f, s.rho_s = c.rho_f, c.rho_s
-                s.grav = (c.rho_s - c.rho_f) * c.gravity
-                s.part_mass = 2 * np.pi * c.dx * c.dx * c.rho_s * np.sum(chi_h * R)
-                s.part_vol = 2 * np.pi * c.dx * c.dx * np.sum(chi_h * R)
-                s.r_body = c.r_sphere
-                s.blend_w = c.moll_zone
-                self.state[k, ST_ZCM] = c.z_cm
-            for name in ("omega", "psi", "u_z", "u_r", "chi", "kill_coef", "r", "z",
-                         "rinv2dx", "rinv2", "rw", "zw", "gemm_work", "partials"):
-                setattr(s, name, t[name].data_ptr())
-            for name, v in b.t.items():
-                setattr(s, name, v.data_ptr())
-            if tensor_cores:
-                s.omega_hi = t["omega_hi"].data_ptr()
-                s.omega_lo = t["omega_lo"].data_ptr()
-                for q in range(8):
-                    s.tc_basis[q] = b.tc[q].data_ptr()
-                for q in range(4):
-                    s.tc_work[q] = t["tc_work"][q].data_ptr()
-            s.state = self.state[k].data_ptr()
-            if self.history is not None:
-                s.history = self.history[k].data_ptr()
-                s.history_len = history_steps
-            else:
-                s.history = None
-                s.history_len = 0
-        self._bases = bases
+        cases = list(cases)
+        capacity = max(capacity or 0, len(cases), 1)
+        self.state_arena = torch.zeros((capacity, ST_WORDS), dtype=torch.float64,
+                                       device=self.device)
+        self._free = list(range(capacity - 1, -1, -1))
+        self._bases = {}
+        self.members = []
+        self.graph = None
         lib = N.lib()
+        self._step_fn = getattr(lib, f"axi_rigid_step_{precision}")
+        self._phase_fn = getattr(lib, f"axi_rigid_phase_{precision}")
+        for k, c in enumerate(cases):
+            w0 = initial_vorticity[k] if initial_vorticity is not None else None
+            self._admit(c, history_steps, w0)
+        self._replan()
+
+    def _bases_for(self, c):
+        key = (c.nr, c.nz, c.dx)
+        if key not in self._bases:
+            self._bases[key] = _Bases(c.nr, c.nz, c.dx, self.dtype, self.device,
+                                      tensor_cores=self.tensor_cores)
+        return self._bases[key]
+
+    def _admit(self, case, history_steps=0, initial_vorticity=None):
+        if not self._free:
+            raise RuntimeError("ensemble is at capacity")
+        m = CaseState(self, case, self._free.pop(), history_steps, initial_vorticity)
+        self.members.append(m)
+        return m
+
+    def _replan(self):
+        self.graph = None
+        n = len(self.members)
+        self.structs = (AxiCase * max(n, 1))()
+        for k, m in enumerate(self.members):
+            self.structs[k] = m.struct
         self.info = AxiPlanInfo()
-        esize = 8 if precision == "f64" else 4
+        if n == 0:
+            self.plan = None
+            self.n_tiles = 0
+            return
+        lib = N.lib()
+        esize = 8 if self.precision == "f64" else 4
         N.check(lib.axi_plan_init(ctypes.addressof(self.structs), n, esize,
-                                  PLAN_TENSOR_CORES if tensor_cores else 0,
+                                  PLAN_TENSOR_CORES if self.tensor_cores else 0,
                                   ctypes.byref(self.info)), "plan_init")
         self.n_tiles = self.info.n_stencil_tiles
         self.plan = torch.empty(int(self.info.bytes), dtype=torch.uint8, device=self.device)
@@ -286,13 +334,44 @@ class RigidEnsemble:
                                     ctypes.c_void_p(self.plan.data_ptr()),
                                     ctypes.c_void_p(torch.cuda.current_stream(
                                         self.device).cuda_stream)), "plan_upload")
-        self._step_fn = getattr(lib, f"axi_rigid_step_{precision}")
-        self._phase_fn = getattr(lib, f"axi_rigid_phase_{precision}")
-        self.graph = None
+
+    def add_case(self, case, history_steps=0, initial_vorticity=None):
+        """Admit a case between steps; returns its CaseState."""
+        m = self._admit(case, history_steps, initial_vorticity)
+        self._replan()
+        return m
+
+    def remove_case(self, member):
+        """Retire a case between steps (its device memory is released)."""
+        self.members.remove(member)
+        self._free.append(member.slot)
+        member.fields = None
+        self._replan()
+
+    @property
+    def cases(self):
+        return [m.case for m in self.members]
+
+    @property
+    def fields(self):
+        return [m.fields for m in self.members]
+
+    @property
+    def history(self):
+        if not self.members or self.members[0].history is None:
+            return None
+        return torch.stack([m.history for m in self.members])
+
+    @property
+    def state(self):
+        idx = [m.slot for m in self.members]
+        if idx == list(range(len(idx))):
+            return self.state_arena[:len(idx)]
+        return self.state_arena[idx]
 
     @property
     def n_cases(self):
-        return len(self.cases)
+        return len(self.members)
 
     def cells(self):
         return sum(c.nr * c.nz for c in self.cases)
