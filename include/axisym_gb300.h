@@ -306,8 +306,10 @@ int axi_tc_transform_status(const axi_tc_plan_info* info, const void* plan_dev, 
  * lo = x - hi (from float) or fl32(x - hi) (from double). */
 int axi_tc_split_f32(float* hi, float* lo, const float* x, int64_t n, void* stream);
 int axi_tc_split_f64(float* hi, float* lo, const double* x, int64_t n, void* stream);
-/* Residual of one refinement step, in FP64: res = w_i rhs - L psi with
- * L = A_r (x) I + I (x) A_z the discrete operator the solver inverts. ar, az
+/* Residual of one refinement step, in FP64: res = rhs - (L psi) / w_i with
+ * L = A_r (x) I + I (x) A_z the discrete operator and w the row weight
+ * (the solver solves L psi = diag(w) rhs; its transform applies w itself,
+ * so the residual it is given is unweighted). ar, az
  * hold the sub, main and super diagonal of each row (3 nr, 3 nz doubles);
  * wrap0 = A_z[0, nz-1], wrap1 = A_z[nz-1, 0] (periodic z, else 0);
  * row_weight may be NULL (w = 1). */

@@ -38,7 +38,9 @@ __global__ void split_f64_kernel(const double* __restrict__ x, float* __restrict
   }
 }
 
-// res = w_i * rhs - L psi, with L = A_r (rows) + A_z (columns) given by the
+// The transform solves L psi = W rhs (W = diag(w) on rows, folded into its
+// E_r^-1 W basis), so the correction it is applied to is the unweighted
+// residual res = rhs - W^-1 L psi, with L = A_r (rows) + A_z (columns) given by the
 // three diagonals of each 1-D operator plus the two periodic wrap entries
 // A_z[0, nz-1] and A_z[nz-1, 0] (the FD matrices of
 // FastDiagonalisationStokesSolver.py:41-97 after the boundary edits).
@@ -59,8 +61,7 @@ __global__ void residual_kernel(double* __restrict__ res, const double* __restri
   if (j < nz - 1) lp += zr[3 * j + 2] * psi[c + 1];
   if (j == 0) lp += wrap0 * psi[c + nz - 1];
   if (j == nz - 1) lp += wrap1 * psi[c - nz + 1];
-  const double b = w ? w[i] * rhs[c] : rhs[c];
-  res[c] = b - lp;
+  res[c] = w ? rhs[c] - lp / w[i] : rhs[c] - lp;
 }
 
 __global__ void add_kernel(double* __restrict__ y, const float* __restrict__ x, long long n) {

@@ -57,14 +57,10 @@ def test_tensor_core_stokes_solve_with_refinement(bc, nr, nz):
         K.compute_velocity_from_psi_unb(uz, ur, p, R, dx)
         errs[refine] = (rel_l2(p, ref), rel_l2(uz, uz_ref), rel_l2(ur, ur_ref))
     print(bc, nr, nz, "rel L2 (psi, u_z, u_r) without / with refinement:", errs)
-    # The FP32 (hi + lo TF32) eigenbases perturb the inverse by ~1e-7 per
-    # entry; composed with the discrete operator that error is amplified by its
-    # spectral condition number, so one refinement step contracts the error by
-    # a few times rather than to FP64 level. The target is 1e-5 on psi and
-    # velocity.
-    assert max(errs[0]) < 3e-5, errs
-    assert max(errs[1]) < 1e-5, errs
-    assert max(errs[1]) < max(errs[0]), errs
+    # One FP64-residual refinement step squares the relative error of the
+    # 3xTF32 transform (~1e-5 on velocity at these sizes).
+    assert max(errs[0]) < 2e-4, errs
+    assert max(errs[1]) < 1e-8, errs
 
 
 def test_tensor_core_solve_float32_fields_and_potential():
@@ -83,11 +79,11 @@ def test_tensor_core_solve_float32_fields_and_potential():
     s.solve(psi32, t32)
     ref32 = np.zeros_like(w)
     K.FastDiagonalisationStokesSolver(nr, nz, dx).solve(ref32, w.astype(np.float32).astype(np.float64))
-    assert rel_l2(psi32.double().cpu().numpy(), ref32) < 1e-5
+    assert rel_l2(psi32.double().cpu().numpy(), ref32) < 5e-7
     dt = 0.5 * dx * dx / 1e-2
     st = ImplicitEulerDiffusionStepper(dt, 1e-2, nr, nz, dx, real_dtype=np.float32)
     x = torch.tensor(w, dtype=torch.float64, device="cuda")
     st.step(x, dt)
     refd = w.copy()
     K.ImplicitEulerDiffusionStepper(dt, 1e-2, nr, nz, dx).step(refd, dt)
-    assert rel_l2(x.cpu().numpy(), refd) < 1e-6
+    assert rel_l2(x.cpu().numpy(), refd) < 1e-8
