@@ -372,16 +372,22 @@ enum {
   AXI_ST_UBODY = 14,   /* sedimenting body: velocity along z */
   AXI_ST_DIFF = 15,    /* sedimenting body: last velocity increment (unsteady force) */
   AXI_ST_FTOTAL = 16,  /* sedimenting body: last total force */
+  AXI_ST_F32 = 17,     /* words 17-23: float copies of the step scalars that
+                          the float engine's per-cell code reads (internal) */
   AXI_ST_WORDS = 24
 };
 
 enum { AXI_CASE_SEDIMENTING = 1 };
 
+/* Stencil tiles of the engine: AXI_TILE_NR rows x AXI_TILE_NZ columns. A
+ * case has ceil(nr / AXI_TILE_NR) * ceil(nz / AXI_TILE_NZ) of them. */
+enum { AXI_TILE_NR = 32, AXI_TILE_NZ = 64 };
+
 /* One flow-past-rigid-body case. Fields are (nr, nz) row-major in the engine
  * precision (double for _f64, float for _f32); rinv2dx, rinv2 and rw are
  * per-row vectors (length nr) and zw a per-column vector (length nz) in the
  * engine precision; r and z are double vectors of length nr and nz. partials
- * holds 2 doubles per stencil tile of the case. */
+ * holds 2 doubles per stencil tile of the case. nr * nz < 2^31. */
 typedef struct axi_case {
   int32_t nr, nz;
   int32_t kill_width;

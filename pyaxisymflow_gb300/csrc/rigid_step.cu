@@ -31,13 +31,56 @@
 
 namespace {
 
-// Stencil tiles: 64 x 16 cells per 256-thread block (4 cells per thread,
-// warps along the contiguous z axis).
-constexpr int TX = 64;
-constexpr int TY = 16;
+// Stencil tiles: 64 x 32 cells per 256-thread block (8 cells per thread,
+// warps along the contiguous z axis). Thread t owns column t % 64 of the tile
+// and rows t / 64 + 4 m (m < 8); vel_max gives each thread 8 consecutive rows
+// instead. Cell indices are 32-bit (a case has fewer than 2^31 cells).
+constexpr int TX = AXI_TILE_NZ;
+constexpr int TY = AXI_TILE_NR;
 constexpr int NT = 256;
 constexpr int CPT = TX * TY / NT;
+constexpr int RG = NT / TX;  // row groups
+static_assert(TX == 64 && TY % RG == 0, "tile shape");
 constexpr double kPi = 3.141592653589793;
+
+// Per-step scalars as the per-cell code reads them. The double engine reads
+// the state words and case fields directly; the float engine reads float
+// copies that kill_reset and vel_max write once per case and step, so no
+// thread converts from double (GB300 issues FP64 conversions at the FP64
+// rate).
+enum {
+  SF_UFREE, SF_LAMDT, SF_ADV, SF_C1, SF_C2, SF_UBODY, SF_ZCM, SF_INV2DX, SF_INVDX2, SF_RBODY,
+  SF_BLENDW, SF_COUNT
+};
+static_assert(SF_COUNT <= 2 * (AXI_ST_WORDS - AXI_ST_F32), "float scalar slots");
+
+__device__ __forceinline__ float* fslots(const axi_case& k) {
+  return reinterpret_cast<float*>(&k.state[AXI_ST_F32]);
+}
+
+template <typename T>
+__device__ __forceinline__ T scalar(const axi_case& k, int f);
+template <>
+__device__ __forceinline__ float scalar<float>(const axi_case& k, int f) {
+  return fslots(k)[f];
+}
+template <>
+__device__ __forceinline__ double scalar<double>(const axi_case& k, int f) {
+  switch (f) {
+    case SF_UFREE: return k.state[AXI_ST_UFREE];
+    case SF_LAMDT: return k.state[AXI_ST_LAMDT];
+    case SF_ADV: return k.state[AXI_ST_ADV];
+    case SF_C1: return k.state[AXI_ST_C1];
+    case SF_C2: return k.state[AXI_ST_C2];
+    case SF_UBODY:
+      return (k.flags & AXI_CASE_SEDIMENTING) ? k.state[AXI_ST_UBODY] : k.U_body;
+    case SF_ZCM: return k.state[AXI_ST_ZCM];
+    case SF_INV2DX: return k.inv_2dx;
+    case SF_INVDX2: return k.inv_dx2;
+    case SF_RBODY: return k.r_body;
+    default: return k.blend_w;
+  }
+}
 
 template <typename T>
 __device__ __forceinline__ T* F(void* p) {
@@ -55,7 +98,7 @@ __device__ __forceinline__ unsigned int* counter(const axi_case& k, int which) {
 // Keeps the TF32 hi / lo copy of omega (operand of the tensor-core products)
 // in step with omega in the FP32 engine.
 template <typename T>
-__device__ __forceinline__ void store_omega(const axi_case& k, long long c, T v) {
+__device__ __forceinline__ void store_omega(const axi_case& k, int c, T v) {
   F<T>(k.omega)[c] = v;
   if constexpr (sizeof(T) == 4) {
     if (k.omega_hi) {
@@ -94,9 +137,18 @@ __global__ void kill_reset_kernel(const axi_case* __restrict__ cases) {
     double prefac = 1.0;
     if (k.t_ramp > 0.0 && t < k.t_ramp) prefac = sin(0.5 * kPi * t / k.t_ramp);
     k.state[AXI_ST_UFREE] = k.U0 * prefac;
+    float* f = fslots(k);
+    f[SF_UFREE] = (float)(k.U0 * prefac);
+    f[SF_UBODY] =
+        (float)((k.flags & AXI_CASE_SEDIMENTING) ? k.state[AXI_ST_UBODY] : k.U_body);
+    f[SF_ZCM] = (float)k.state[AXI_ST_ZCM];
+    f[SF_INV2DX] = (float)k.inv_2dx;
+    f[SF_INVDX2] = (float)k.inv_dx2;
+    f[SF_RBODY] = (float)k.r_body;
+    f[SF_BLENDW] = (float)k.blend_w;
   }
   for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-    const long long row = (long long)i * nz;
+    const int row = i * nz;
     const double left = (double)w[row + wd - 1];
     const double right = (double)w[row + nz - wd];
     for (int q = 0; q < wd; ++q) store_omega<T>(k, row + q, (T)(cz0[q] * left));
@@ -104,39 +156,52 @@ __global__ void kill_reset_kernel(const axi_case* __restrict__ cases) {
   }
   __syncthreads();
   for (int j = threadIdx.x; j < nz; j += blockDim.x) {
-    const double src = (double)w[(long long)(nr - wd) * nz + j];
+    const double src = (double)w[(nr - wd) * nz + j];
     for (int q = 0; q < wd; ++q)
-      store_omega<T>(k, (long long)(nr - wd + q) * nz + j, (T)(cr[q] * src));
+      store_omega<T>(k, (nr - wd + q) * nz + j, (T)(cr[q] * src));
     store_omega<T>(k, j, T(0));
   }
 }
 
 // ---------------------------------------------------------------------------
 // velocity from psi (kernels/compute_velocity_from_psi.py:9-17) plus the free
-// stream. psi(a, b) is an accessor; interior cells run in T, the one-sided
-// rows / columns at the grid edges in double.
+// stream. psi(a, b) is an accessor; rinv = 1 / (2 dx r_i). The one-sided rows
+// and columns at the grid edges run in double in the double engine (the
+// reference's expression) and in float in the float engine.
 // ---------------------------------------------------------------------------
 template <typename T, typename Acc>
 __device__ __forceinline__ void velocity_at(const axi_case& k, Acc psi, int i, int j, T rinv,
                                             T ufree, T& uz, T& ur) {
   const int nr = k.nr, nz = k.nz;
   if (i == 0 || i == nr - 1) {
-    double d;
-    if (i == 0)
-      d = -(double)psi(2, j) + 4.0 * (double)psi(1, j) - 3.0 * (double)psi(0, j);
-    else
-      d = (double)psi(nr - 3, j) - 4.0 * (double)psi(nr - 2, j) + 3.0 * (double)psi(nr - 1, j);
-    uz = (T)(d * (0.5 / k.dx) / k.r[i]) + ufree;
+    if constexpr (sizeof(T) == 8) {
+      double d;
+      if (i == 0)
+        d = -(double)psi(2, j) + 4.0 * (double)psi(1, j) - 3.0 * (double)psi(0, j);
+      else
+        d = (double)psi(nr - 3, j) - 4.0 * (double)psi(nr - 2, j) + 3.0 * (double)psi(nr - 1, j);
+      uz = (T)(d * (0.5 / k.dx) / k.r[i]) + ufree;
+    } else {
+      const T d = (i == 0) ? -psi(2, j) + T(4) * psi(1, j) - T(3) * psi(0, j)
+                           : psi(nr - 3, j) - T(4) * psi(nr - 2, j) + T(3) * psi(nr - 1, j);
+      uz = d * rinv + ufree;
+    }
   } else {
     uz = (psi(i + 1, j) - psi(i - 1, j)) * rinv + ufree;
   }
   if (j == 0 || j == nz - 1) {
-    double d;
-    if (j == 0)
-      d = -(double)psi(i, 2) + 4.0 * (double)psi(i, 1) - 3.0 * (double)psi(i, 0);
-    else
-      d = (double)psi(i, nz - 3) - 4.0 * (double)psi(i, nz - 2) + 3.0 * (double)psi(i, nz - 1);
-    ur = (T)(-d) * rinv;
+    if constexpr (sizeof(T) == 8) {
+      double d;
+      if (j == 0)
+        d = -(double)psi(i, 2) + 4.0 * (double)psi(i, 1) - 3.0 * (double)psi(i, 0);
+      else
+        d = (double)psi(i, nz - 3) - 4.0 * (double)psi(i, nz - 2) + 3.0 * (double)psi(i, nz - 1);
+      ur = (T)(-d) * rinv;
+    } else {
+      const T d = (j == 0) ? -psi(i, 2) + T(4) * psi(i, 1) - T(3) * psi(i, 0)
+                           : psi(i, nz - 3) - T(4) * psi(i, nz - 2) + T(3) * psi(i, nz - 1);
+      ur = -d * rinv;
+    }
   } else {
     ur = -(psi(i, j + 1) - psi(i, j - 1)) * rinv;
   }
@@ -161,18 +226,40 @@ __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict_
   const int4 tr = tiles[blockIdx.x];
   const axi_case& k = cases[tr.x];
   const int nr = k.nr, nz = k.nz;
-  const T* psi = CF<T>(k.psi);
-  const T* rinv2dx = CF<T>(k.rinv2dx);
-  const T ufree = (T)k.state[AXI_ST_UFREE];
-  auto acc = [&](int a, int b) { return psi[(long long)a * nz + b]; };
+  const T* __restrict__ psi = CF<T>(k.psi);
+  const T* __restrict__ rinv2dx = CF<T>(k.rinv2dx);
+  const T ufree = scalar<T>(k, SF_UFREE);
+  // this thread: column j, rows ib .. ib + CPT - 1; the column (with one row
+  // above and below) and the two neighbouring columns are loaded up front
+  const int j = tr.z + (threadIdx.x % TX);
+  const int ib = tr.y + (threadIdx.x / TX) * CPT;
+  T col[CPT + 2], lf[CPT], rt[CPT];
+  const bool jin = j < nz;
+#pragma unroll
+  for (int m = 0; m < CPT + 2; ++m) {
+    const int ii = ib - 1 + m;
+    col[m] = (jin && ii >= 0 && ii < nr) ? psi[ii * nz + j] : T(0);
+  }
+#pragma unroll
+  for (int m = 0; m < CPT; ++m) {
+    const int ii = ib + m;
+    lf[m] = (ii < nr && j >= 1 && jin) ? psi[ii * nz + j - 1] : T(0);
+    rt[m] = (ii < nr && j + 1 < nz) ? psi[ii * nz + j + 1] : T(0);
+  }
+  auto acc = [&](int a, int b) { return psi[a * nz + b]; };
   unsigned long long bits = 0;
 #pragma unroll
-  for (int q = 0; q < CPT; ++q) {
-    const int e = threadIdx.x + q * NT;
-    const int i = tr.y + e / TX, j = tr.z + e % TX;
-    if (i < nr && j < nz) {
+  for (int m = 0; m < CPT; ++m) {
+    const int i = ib + m;
+    if (jin && i < nr) {
+      const T rv = rinv2dx[i];
       T uz, ur;
-      velocity_at<T>(k, acc, i, j, rinv2dx[i], ufree, uz, ur);
+      if (i == 0 || i == nr - 1 || j == 0 || j == nz - 1) {
+        velocity_at<T>(k, acc, i, j, rv, ufree, uz, ur);
+      } else {
+        uz = (col[m + 2] - col[m]) * rv + ufree;
+        ur = -(rt[m] - lf[m]) * rv;
+      }
       const unsigned long long b = order_bits<T>(fabs(uz) + fabs(ur));
       bits = b > bits ? b : bits;
     }
@@ -205,6 +292,11 @@ __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict_
     k.state[AXI_ST_ADV] = -dt / k.dx;
     k.state[AXI_ST_C1] = 0.5 * k.nu * dt;
     k.state[AXI_ST_C2] = k.nu * dt;
+    float* f = fslots(k);
+    f[SF_LAMDT] = (float)(k.lam * dt);
+    f[SF_ADV] = (float)(-dt / k.dx);
+    f[SF_C1] = (float)(0.5 * k.nu * dt);
+    f[SF_C2] = (float)(k.nu * dt);
   }
 }
 
@@ -219,90 +311,98 @@ __device__ __forceinline__ void penalise_point(T uz, T ur, T lc, T ubody, T& pz,
   pr = ur * inv;
 }
 
+constexpr int PN_PW = TX + 4, PN_PH = TY + 4;  // psi, halo 2
+constexpr int PN_SW = TX + 2, PN_SH = TY + 2;  // chi and u_pen - u, halo 1
+template <typename T>
+constexpr int penalise_smem() {
+  return (int)sizeof(T) * (PN_PH * PN_PW + 3 * PN_SH * PN_SW);
+}
+
+// Velocity, penalised velocity and their difference are evaluated once per
+// point of the tile + halo 1 (owned points also store u_pen and add to the
+// drag integrand); the curl of the difference then updates omega of the
+// owned cells.
 template <typename T>
 __global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict__ cases,
                                                       const int4* __restrict__ tiles) {
-  __shared__ T ps[TY + 4][TX + 4];
-  __shared__ T sc[TY + 2][TX + 2];
-  __shared__ T duz[TY + 2][TX + 2];
-  __shared__ T dur[TY + 2][TX + 2];
+  extern __shared__ __align__(16) unsigned char pn_smem[];
+  T* ps = reinterpret_cast<T*>(pn_smem);
+  T* sc = ps + PN_PH * PN_PW;
+  T* duz = sc + PN_SH * PN_SW;
+  T* dur = duz + PN_SH * PN_SW;
   __shared__ double red[NT / 32];
   __shared__ bool last;
   const int4 tr = tiles[blockIdx.x];
   const axi_case& k = cases[tr.x];
   const int nr = k.nr, nz = k.nz;
   const int i0 = tr.y, j0 = tr.z;
-  const T* psi = CF<T>(k.psi);
-  const T* chi = CF<T>(k.chi);
-  const T* rinv2dx = CF<T>(k.rinv2dx);
-  const T ufree = (T)k.state[AXI_ST_UFREE];
-  const T lamdt = (T)k.state[AXI_ST_LAMDT];
+  const T* __restrict__ psi = CF<T>(k.psi);
+  const T* __restrict__ chi = CF<T>(k.chi);
+  const T* __restrict__ rinv2dx = CF<T>(k.rinv2dx);
+  const T* __restrict__ rw = CF<T>(k.rw);
+  const T ufree = scalar<T>(k, SF_UFREE);
+  const T lamdt = scalar<T>(k, SF_LAMDT);
+  const T ubody = scalar<T>(k, SF_UBODY);
+  const T inv2dx = scalar<T>(k, SF_INV2DX);
   const bool sediment = (k.flags & AXI_CASE_SEDIMENTING) != 0;
-  const T ubody = (T)(sediment ? k.state[AXI_ST_UBODY] : k.U_body);
-  const T inv2dx = (T)k.inv_2dx;
   // all global loads of the block are issued here: psi (halo 2), chi (halo 1)
   // into shared memory, omega of the owned cells into registers
   T* w = F<T>(k.omega);
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
   T wown[CPT];
 #pragma unroll
   for (int q = 0; q < CPT; ++q) {
-    const int e = threadIdx.x + q * NT;
-    const int gi = i0 + e / TX, gj = j0 + e % TX;
-    wown[q] = (gi < nr && gj < nz) ? w[(long long)gi * nz + gj] : T(0);
+    const int gi = i0 + ty + RG * q, gj = j0 + tx;
+    wown[q] = (gi < nr && gj < nz) ? w[gi * nz + gj] : T(0);
   }
-  for (int e = threadIdx.x; e < (TY + 4) * (TX + 4); e += NT) {
-    const int a = e / (TX + 4), b = e % (TX + 4);
+  for (int e = threadIdx.x; e < PN_PH * PN_PW; e += NT) {
+    const int a = e / PN_PW, b = e - a * PN_PW;
     const int gi = i0 - 2 + a, gj = j0 - 2 + b;
-    ps[a][b] = (gi >= 0 && gi < nr && gj >= 0 && gj < nz) ? psi[(long long)gi * nz + gj] : T(0);
+    ps[e] = (gi >= 0 && gi < nr && gj >= 0 && gj < nz) ? psi[gi * nz + gj] : T(0);
   }
-  for (int e = threadIdx.x; e < (TY + 2) * (TX + 2); e += NT) {
-    const int a = e / (TX + 2), b = e % (TX + 2);
+  for (int e = threadIdx.x; e < PN_SH * PN_SW; e += NT) {
+    const int a = e / PN_SW, b = e - a * PN_SW;
     const int gi = i0 - 1 + a, gj = j0 - 1 + b;
-    sc[a][b] = (gi >= 0 && gi < nr && gj >= 0 && gj < nz) ? chi[(long long)gi * nz + gj] : T(0);
+    sc[e] = (gi >= 0 && gi < nr && gj >= 0 && gj < nz) ? chi[gi * nz + gj] : T(0);
   }
   __syncthreads();
   // every one-sided stencil of an edge cell stays inside the halo-2 tile
-  auto sp = [&](int gi, int gj) { return ps[gi - i0 + 2][gj - j0 + 2]; };
-  for (int e = threadIdx.x; e < (TY + 2) * (TX + 2); e += NT) {
-    const int a = e / (TX + 2), b = e % (TX + 2);
+  auto sp = [&](int gi, int gj) { return ps[(gi - i0 + 2) * PN_PW + (gj - j0 + 2)]; };
+  T* uzp = F<T>(k.u_z);
+  T* urp = F<T>(k.u_r);
+  T cd_part = T(0);
+  for (int e = threadIdx.x; e < PN_SH * PN_SW; e += NT) {
+    const int a = e / PN_SW, b = e - a * PN_SW;
     const int gi = i0 - 1 + a, gj = j0 - 1 + b;
     T dz = T(0), dr = T(0);
     if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
-      T uz, ur, pz, pr;
-      velocity_at<T>(k, sp, gi, gj, rinv2dx[gi], ufree, uz, ur);
-      penalise_point<T>(uz, ur, lamdt * sc[a][b], ubody, pz, pr);
-      dz = pz - uz;
-      dr = pr - ur;
-    }
-    duz[a][b] = dz;
-    dur[a][b] = dr;
-  }
-  __syncthreads();
-  T cd_part = T(0);
-  T* uzp = F<T>(k.u_z);
-  T* urp = F<T>(k.u_r);
-  const T* rw = CF<T>(k.rw);
-#pragma unroll
-  for (int q = 0; q < CPT; ++q) {
-    const int e = threadIdx.x + q * NT;
-    const int a = e / TX, b = e % TX;
-    const int gi = i0 + a, gj = j0 + b;
-    if (gi < nr && gj < nz) {
-      const long long c = (long long)gi * nz + gj;
-      const T ch = sc[a + 1][b + 1];
+      const T ch = sc[e];
       T uz, ur, pz, pr;
       velocity_at<T>(k, sp, gi, gj, rinv2dx[gi], ufree, uz, ur);
       penalise_point<T>(uz, ur, lamdt * ch, ubody, pz, pr);
-      uzp[c] = pz;
-      urp[c] = pr;
-      // drag / penalisation force integrand r chi (u_z - U_body)
-      // (flow_past_sphere.py:173, compute_forces.py:14)
-      cd_part += rw[gi] * ch * (pz - ubody);
-      if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
-        const T pw = (dur[a + 1][b + 2] - dur[a + 1][b]) * inv2dx -
-                     (duz[a + 2][b + 1] - duz[a][b + 1]) * inv2dx;
-        w[c] = wown[q] + pw;
+      dz = pz - uz;
+      dr = pr - ur;
+      if (a >= 1 && a <= TY && b >= 1 && b <= TX) {
+        const int c = gi * nz + gj;
+        uzp[c] = pz;
+        urp[c] = pr;
+        // drag / penalisation force integrand r chi (u_z - U_body)
+        // (flow_past_sphere.py:173, compute_forces.py:14)
+        cd_part += rw[gi] * ch * (pz - ubody);
       }
+    }
+    duz[e] = dz;
+    dur[e] = dr;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) {
+    const int a = ty + RG * q, b = tx;
+    const int gi = i0 + a, gj = j0 + b;
+    if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
+      const int d = (a + 1) * PN_SW + (b + 1);
+      const T pw = (dur[d + 1] - dur[d - 1]) * inv2dx - (duz[d + PN_SW] - duz[d - PN_SW]) * inv2dx;
+      w[gi * nz + gj] = wown[q] + pw;
     }
   }
   // drag: thread and warp sums in T, then warps and tiles in double, fixed order
@@ -406,23 +506,23 @@ __global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __re
   const T* ur = CF<T>(k.u_r);
   const T* rinv2dx = CF<T>(k.rinv2dx);
   const T* rinv2 = CF<T>(k.rinv2);
-  const T a = (T)k.state[AXI_ST_ADV];
-  const T c1 = (T)k.state[AXI_ST_C1];
-  const T c2 = (T)k.state[AXI_ST_C2];
-  const T inv_dx2 = (T)k.inv_dx2;
+  const T a = scalar<T>(k, SF_ADV);
+  const T c1 = scalar<T>(k, SF_C1);
+  const T c2 = scalar<T>(k, SF_C2);
+  const T inv_dx2 = scalar<T>(k, SF_INVDX2);
   for (int e = threadIdx.x; e < AD_LH * AD_LW; e += NT) {
-    const int p = e / AD_LW, q = e % AD_LW;
+    const int p = e / AD_LW, q = e - p * AD_LW;
     const int gi = i0 - AD_H + p, gj = j0 - AD_H + q;
     T vw = T(0), vz = T(0), vr = T(0);
     if (gj >= 0 && gj < nz && gi < nr) {
       if (gi >= 0) {
-        const long long c = (long long)gi * nz + gj;
+        const int c = gi * nz + gj;
         vw = w[c];
         vz = uz[c];
         vr = ur[c];
       } else if (-1 - gi < nr) {
         // rows below the axis: omega odd, u_z even, u_r odd
-        const long long c = (long long)(-1 - gi) * nz + gj;
+        const int c = (-1 - gi) * nz + gj;
         vw = -w[c];
         vz = uz[c];
         vr = -ur[c];
@@ -435,7 +535,7 @@ __global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __re
   __syncthreads();
   // advected omega on the tile + halo 2
   for (int e = threadIdx.x; e < AD_AH * AD_AW; e += NT) {
-    const int p = e / AD_AW, q = e % AD_AW;
+    const int p = e / AD_AW, q = e - p * AD_AW;
     const int gi = i0 - 2 + p, gj = j0 - 2 + q;
     T val = T(0);
     if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
@@ -466,7 +566,7 @@ __global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __re
   __syncthreads();
   // RK2 stage 1 on the tile + halo 1
   for (int e = threadIdx.x; e < AD_SH * AD_SW; e += NT) {
-    const int p = e / AD_SW, q = e % AD_SW;
+    const int p = e / AD_SW, q = e - p * AD_SW;
     const int gi = i0 - 1 + p, gj = j0 - 1 + q;
     T tmp = T(0);
     if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
@@ -485,15 +585,16 @@ __global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __re
   __syncthreads();
   // RK2 stage 2 on the tile
   const bool sediment = (k.flags & AXI_CASE_SEDIMENTING) != 0;
-  const T zc = (T)k.state[AXI_ST_ZCM];
+  const T zc = scalar<T>(k, SF_ZCM);
+  const T rbody = scalar<T>(k, SF_RBODY);
+  const T blendw = scalar<T>(k, SF_BLENDW);
   T cd_part = T(0);
 #pragma unroll
   for (int qq = 0; qq < CPT; ++qq) {
-    const int e = threadIdx.x + qq * NT;
-    const int p = e / TX, q = e % TX;
+    const int p = threadIdx.x / TX + RG * qq, q = threadIdx.x % TX;
     const int gi = i0 + p, gj = j0 + q;
     if (gi < nr && gj < nz) {
-      const long long c = (long long)gi * nz + gj;
+      const int c = gi * nz + gj;
       T v = wa[(p + 2) * AD_AW + (q + 2)];
       if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
         const int d = (p + 1) * AD_SW + (q + 1);
@@ -506,8 +607,7 @@ __global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __re
       if (sediment) {
         // mask at the body position of this step (falling_rigid_sphere.py:156-157),
         // then the drag integrand with the new mask (:164-173)
-        const T ch = sphere_mask<T>(CF<T>(k.zw)[gj], CF<T>(k.rw)[gi], zc, (T)k.r_body,
-                                    (T)k.blend_w);
+        const T ch = sphere_mask<T>(CF<T>(k.zw)[gj], CF<T>(k.rw)[gi], zc, rbody, blendw);
         F<T>(k.chi)[c] = ch;
         cd_part += CF<T>(k.rw)[gi] * ch * sz[(p + AD_H) * AD_LW + (q + AD_H)];
       }
@@ -571,7 +671,7 @@ __global__ void __launch_bounds__(NT) refresh_split_kernel(const axi_case* __res
     const int e = threadIdx.x + q * NT;
     const int gi = tr.y + e / TX, gj = tr.z + e % TX;
     if (gi < k.nr && gj < k.nz) {
-      const long long c = (long long)gi * k.nz + gj;
+      const int c = gi * k.nz + gj;
       store_omega<float>(k, c, static_cast<const float*>(k.omega)[c]);
     }
   }
@@ -789,16 +889,21 @@ inline int tc_tiles_of(const axi_case& k, int stage) {
 enum { PH_KILL = 0, PH_TRANSFORM = 1, PH_VEL_MAX = 2, PH_PENALISE = 3, PH_ADVECT_DIFFUSE = 4,
        PH_COUNT = 5 };
 
+// Both stencil kernels with a dynamic shared-memory tile reserve it once per
+// process (the double engine's tiles exceed the 48 KB default).
 template <typename T>
-int advect_diffuse_attr() {
+int stencil_attrs() {
   static int status = -1;
   if (status < 0) {
-    status = cudaFuncSetAttribute(advect_diffuse_kernel<T>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  advect_diffuse_smem<T>()) == cudaSuccess
+    status = (cudaFuncSetAttribute(advect_diffuse_kernel<T>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   advect_diffuse_smem<T>()) == cudaSuccess &&
+              cudaFuncSetAttribute(penalise_kernel<T>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   penalise_smem<T>()) == cudaSuccess)
                  ? AXI_OK
                  : AXI_ERR_CUDA;
-    if (status != AXI_OK) axi::set_error("advect_diffuse: cannot reserve shared memory");
+    if (status != AXI_OK) axi::set_error("rigid_step: cannot reserve shared memory");
   }
   return status;
 }
@@ -825,10 +930,11 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
       vel_max_kernel<T><<<nt, NT, 0, s>>>(v.cases, v.stencil);
       break;
     case PH_PENALISE:
-      penalise_kernel<T><<<nt, NT, 0, s>>>(v.cases, v.stencil);
+      AXI_TRY(stencil_attrs<T>());
+      penalise_kernel<T><<<nt, NT, penalise_smem<T>(), s>>>(v.cases, v.stencil);
       break;
     case PH_ADVECT_DIFFUSE:
-      AXI_TRY(advect_diffuse_attr<T>());
+      AXI_TRY(stencil_attrs<T>());
       advect_diffuse_kernel<T><<<nt, NT, advect_diffuse_smem<T>(), s>>>(v.cases, v.stencil);
       break;
     default:
@@ -846,7 +952,7 @@ int validate(const axi_case* cases, int n_cases, const char* what) {
   for (int c = 0; c < n_cases; ++c) {
     const axi_case& k = cases[c];
     if (k.nr < 8 || k.nz < 8 || k.kill_width < 2 || k.kill_width > 8 || 2 * k.kill_width > k.nz ||
-        k.kill_width > k.nr) {
+        k.kill_width > k.nr || (int64_t)k.nr * k.nz >= ((int64_t)1 << 31)) {
       axi::set_error("%s: case %d has an unsupported grid %d x %d / kill width %d", what, c, k.nr,
                      k.nz, k.kill_width);
       return AXI_ERR_INVALID;

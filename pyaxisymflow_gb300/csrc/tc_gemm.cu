@@ -127,13 +127,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// v already carries the elementwise factor of MODE_SCALE_SPLIT.
 __device__ __forceinline__ void store_value(const TcJob& job, int row, int col, float v) {
   const long long idx = (long long)row * job.ldc + col;
   if (job.mode == MODE_PLAIN) {
     job.c[idx] = v;
     return;
   }
-  if (job.mode == MODE_SCALE_SPLIT) v *= job.scale[(long long)row * job.N + col];
   float hi, lo;
   tf32_split(v, hi, lo);
   job.c[idx] = hi;
@@ -265,8 +265,23 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (!__all_sync(0xffffffffu, ok && *reinterpret_cast<volatile int*>(err) == 0)) break;
       tc_fence_after();
       const int row0 = tr.y + 32 * q;
+      const bool scaled = job.mode == MODE_SCALE_SPLIT;
 #pragma unroll 1
       for (int cc = 0; cc < BN / 32; ++cc) {
+        const int col = tr.z + cc * 32 + lane;
+        // the elementwise factors of this 32 x 32 block are fetched before the
+        // accumulator is read, all 32 loads in flight at once (one load per
+        // row in the store loop left the epilogue waiting on L2 latency)
+        float sv[32];
+        if (scaled) {
+#pragma unroll
+          for (int rr = 0; rr < 32; ++rr) {
+            const int row = row0 + rr;
+            sv[rr] = (col < job.N && row < job.M)
+                         ? __ldg(job.scale + (long long)row * job.N + col)
+                         : 0.0f;
+          }
+        }
         uint32_t r[32];
         tmem_ld32(tmem + buf * BN + (static_cast<uint32_t>(32 * q) << 16) + cc * 32, r);
         // transpose the warp's 32 x 32 block so each store instruction writes
@@ -274,12 +289,13 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
         for (int j = 0; j < 32; ++j) stg[lane * 33 + j] = __uint_as_float(r[j]);
         __syncwarp();
-        const int col = tr.z + cc * 32 + lane;
         if (col < job.N) {
-#pragma unroll 4
+#pragma unroll
           for (int rr = 0; rr < 32; ++rr) {
             const int row = row0 + rr;
-            if (row < job.M) store_value(job, row, col, stg[rr * 33 + lane]);
+            float v = stg[rr * 33 + lane];
+            if (scaled) v *= sv[rr];
+            if (row < job.M) store_value(job, row, col, v);
           }
         }
         __syncwarp();

@@ -23,6 +23,7 @@ from .kernels.smooth_Heaviside import smooth_Heaviside
 ST_T, ST_DT, ST_CD, ST_STEPS, ST_UMAX, ST_COUNT, ST_STATUS, ST_FORCE = range(8)
 ST_UFREE, ST_LAMDT, ST_ADV, ST_C1, ST_C2, ST_ZCM, ST_UBODY, ST_DIFF, ST_FTOTAL = range(8, 17)
 ST_WORDS = 24
+TILE_NR, TILE_NZ = 32, 64       # stencil tile of the engine (rows x columns)
 CASE_SEDIMENTING = 1
 
 
@@ -205,7 +206,8 @@ class CaseState:
             rw=torch.tensor(r, **f64).to(dtype),
             zw=torch.tensor(z, **f64).to(dtype),
             gemm_work=torch.zeros(2 * c.nr * c.nz, **f),
-            partials=torch.zeros(2 * ((c.nr + 15) // 16) * ((c.nz + 63) // 64) + 8, **f64),
+            partials=torch.zeros(2 * ((c.nr + TILE_NR - 1) // TILE_NR)
+                                 * ((c.nz + TILE_NZ - 1) // TILE_NZ) + 8, **f64),
         )
         if ens.tensor_cores:
             whi, wlo = tf32_split(w0)
