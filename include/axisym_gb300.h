@@ -455,8 +455,10 @@ int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, int flags, axi_p
 /* Tensor-core plans: recompute the TF32 operand copy of omega (omega_hi,
  * omega_lo) of every case after the caller overwrote omega. */
 int axi_rigid_refresh_operands(const axi_plan_info* info, const void* plan_dev, void* stream);
-/* Pipeline status of the tensor-core products since the plan was uploaded
- * (0 = healthy; otherwise a wait timed out). Synchronises the stream. */
+/* Pipeline status of the plan's asynchronous copies (tensor-core products
+ * and the stencil kernels' TMA boxes) since the plan was uploaded: 0 =
+ * healthy; 1-4 a tensor-core wait, 5-6 a stencil wait timed out.
+ * Synchronises the stream. */
 int axi_plan_tc_status(const axi_plan_info* info, const void* plan_dev, int* tc_error,
                        void* stream);
 /* Copies the case table and tile tables into plan_dev (caller-allocated,

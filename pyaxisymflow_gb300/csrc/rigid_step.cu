@@ -28,6 +28,7 @@
 // step, time and the drag sums across warps and tiles.
 #include "axi_common.cuh"
 #include "tc_gemm.cuh"
+#include "tma.cuh"
 
 namespace {
 
@@ -53,6 +54,11 @@ enum {
   SF_BLENDW, SF_COUNT
 };
 static_assert(SF_COUNT <= 2 * (AXI_ST_WORDS - AXI_ST_F32), "float scalar slots");
+
+// Tensor maps of a case's fields (the stencil kernels' TMA boxes) and the
+// error codes of their bounded waits (plan error word).
+enum { MAP_PSI = 0, MAP_CHI = 1, MAP_W = 2, MAP_UZ = 3, MAP_UR = 4, MAP_COUNT = 5 };
+enum { ERR_STENCIL_WAIT = 5, ERR_STENCIL_DRAIN = 6 };
 
 __device__ __forceinline__ float* fslots(const axi_case& k) {
   return reinterpret_cast<float*>(&k.state[AXI_ST_F32]);
@@ -208,6 +214,81 @@ __device__ __forceinline__ void velocity_at(const axi_case& k, Acc psi, int i, i
 }
 
 // ---------------------------------------------------------------------------
+// Persistent stencil kernels. Each block walks the tile table with stride
+// gridDim.x. Thread 0 keeps a ring of NBUF shared-memory box sets: the boxes
+// of the tile NBUF - 1 iterations ahead are requested by TMA
+// (cp.async.bulk.tensor.2d, zero fill outside the grid) while the current
+// tile is computed, so global latency overlaps the arithmetic. Every box is
+// BOXW = TX + 8 columns wide starting at column j0 - 4 (a 16-byte aligned
+// origin) and HALO rows above the tile. The per-case reductions keep the
+// "last tile of the case finalises" pattern: only thread 0 acts on it, so the
+// block moves on to its next tile without waiting for the atomics.
+// ---------------------------------------------------------------------------
+constexpr int BOXW = TX + 8;
+constexpr int PSI_ROWS = TY + 4;  // psi and chi boxes: rows i0 - 2 .. i0 + TY + 1
+constexpr int ADV_ROWS = TY + 8;  // omega, u_z, u_r boxes: rows i0 - 4 .. i0 + TY + 3
+// vel_max is light on arithmetic and runs persistent with a 3-deep ring;
+// penalise and advect_diffuse are bound by instruction issue, so they run one
+// tile per block (ring depth 1) to keep more blocks resident per SM.
+constexpr int VM_NBUF = 3, PN_NBUF = 1, AD_NBUF = 1;
+
+// Ring of box sets in dynamic shared memory (128-byte aligned) and its
+// mbarriers (one per slot, one arrival + the boxes' bytes).
+template <typename T, int NBUF, int NBOX, int ROWS>
+struct BoxRing {
+  static constexpr int BOX = ROWS * BOXW;                   // elements per box
+  static constexpr uint32_t SET_BYTES = NBOX * BOX * sizeof(T);
+  static constexpr int BYTES = NBUF * (int)SET_BYTES;
+  T* base;
+  uint32_t bar0;
+  __device__ T* box(int slot, int which) const { return base + (slot * NBOX + which) * BOX; }
+  __device__ void init() const {
+    for (int b = 0; b < NBUF; ++b) axi_tma::mbar_init(bar0 + 8 * b, 1);
+    axi_tma::fence_mbar_init();
+  }
+  // thread 0: request the boxes of tile tr into slot `slot`
+  __device__ void issue(const CUtensorMap* maps, const int4& tr, const int (&which)[NBOX],
+                        int row0, int slot) const {
+    const uint32_t bar = bar0 + 8 * slot;
+    axi_tma::fence_proxy_async_smem();
+    axi_tma::mbar_expect_tx(bar, SET_BYTES);
+    for (int q = 0; q < NBOX; ++q)
+      axi_tma::tma_load_2d(axi_tma::smem_u32(box(slot, q)), maps + MAP_COUNT * tr.x + which[q],
+                           tr.z - 4, tr.y + row0, bar);
+  }
+  __device__ bool wait(int it, int* err) const {
+    return axi_tma::mbar_wait(bar0 + 8 * (it % NBUF), (it / NBUF) & 1, err, ERR_STENCIL_WAIT);
+  }
+  // thread 0, after a failure: wait (bounded) for the copies still in flight
+  __device__ void drain(int consumed, int issued, int* err) const {
+    for (int g = consumed; g < issued; ++g)
+      if (!axi_tma::mbar_wait_drain(bar0 + 8 * (g % NBUF), (g / NBUF) & 1))
+        atomicCAS(err, 0, ERR_STENCIL_DRAIN);
+  }
+};
+
+__device__ __forceinline__ unsigned char* align_smem(unsigned char* p) {
+  return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 127) &
+                                          ~static_cast<uintptr_t>(127));
+}
+
+// Issues the prologue of a block's ring; returns how many tiles were issued.
+template <typename Ring, int NBUF, int NBOX>
+__device__ __forceinline__ int ring_prologue(const Ring& ring, const CUtensorMap* maps,
+                                             const int4* tiles, int n_tiles,
+                                             const int (&which)[NBOX], int row0) {
+  int issued = 0;
+  for (int b = 0; b < NBUF - 1; ++b) {
+    const int t = blockIdx.x + b * gridDim.x;
+    if (t < n_tiles) {
+      ring.issue(maps, tiles[t], which, row0, b);
+      ++issued;
+    }
+  }
+  return issued;
+}
+
+// ---------------------------------------------------------------------------
 // vel_max: max over the case of |u_z| + |u_r| (flow_past_sphere.py:150-153);
 // the last tile of the case derives dt and the per-step constants.
 // ---------------------------------------------------------------------------
@@ -219,90 +300,117 @@ __device__ __forceinline__ unsigned long long order_bits(T v) {
 }
 
 template <typename T>
+using VmRing = BoxRing<T, VM_NBUF, 1, PSI_ROWS>;
+template <typename T>
+constexpr int vel_max_smem() {
+  return VmRing<T>::BYTES + 128;
+}
+
+template <typename T>
 __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict__ cases,
-                                                     const int4* __restrict__ tiles) {
-  __shared__ unsigned long long wm[NT / 32];
-  __shared__ bool last;
-  const int4 tr = tiles[blockIdx.x];
-  const axi_case& k = cases[tr.x];
-  const int nr = k.nr, nz = k.nz;
-  const T* __restrict__ psi = CF<T>(k.psi);
-  const T* __restrict__ rinv2dx = CF<T>(k.rinv2dx);
-  const T ufree = scalar<T>(k, SF_UFREE);
-  // this thread: column j, rows ib .. ib + CPT - 1; the column (with one row
-  // above and below) and the two neighbouring columns are loaded up front
-  const int j = tr.z + (threadIdx.x % TX);
-  const int ib = tr.y + (threadIdx.x / TX) * CPT;
-  T col[CPT + 2], lf[CPT], rt[CPT];
-  const bool jin = j < nz;
-#pragma unroll
-  for (int m = 0; m < CPT + 2; ++m) {
-    const int ii = ib - 1 + m;
-    col[m] = (jin && ii >= 0 && ii < nr) ? psi[ii * nz + j] : T(0);
+                                                     const int4* __restrict__ tiles, int n_tiles,
+                                                     const CUtensorMap* __restrict__ maps,
+                                                     int* __restrict__ err) {
+  extern __shared__ unsigned char vm_raw[];
+  __shared__ __align__(8) uint64_t bars[VM_NBUF];
+  __shared__ unsigned long long wm[2][NT / 32];
+  VmRing<T> ring{reinterpret_cast<T*>(align_smem(vm_raw)), axi_tma::smem_u32(bars)};
+  constexpr int which[1] = {MAP_PSI};
+  int issued = 0;
+  if (threadIdx.x == 0) {
+    ring.init();
+    issued = ring_prologue<VmRing<T>, VM_NBUF, 1>(ring, maps, tiles, n_tiles, which, -2);
   }
-#pragma unroll
-  for (int m = 0; m < CPT; ++m) {
-    const int ii = ib + m;
-    lf[m] = (ii < nr && j >= 1 && jin) ? psi[ii * nz + j - 1] : T(0);
-    rt[m] = (ii < nr && j + 1 < nz) ? psi[ii * nz + j + 1] : T(0);
-  }
-  auto acc = [&](int a, int b) { return psi[a * nz + b]; };
-  unsigned long long bits = 0;
-#pragma unroll
-  for (int m = 0; m < CPT; ++m) {
-    const int i = ib + m;
-    if (jin && i < nr) {
-      const T rv = rinv2dx[i];
-      T uz, ur;
-      if (i == 0 || i == nr - 1 || j == 0 || j == nz - 1) {
-        velocity_at<T>(k, acc, i, j, rv, ufree, uz, ur);
-      } else {
-        uz = (col[m + 2] - col[m]) * rv + ufree;
-        ur = -(rt[m] - lf[m]) * rv;
+  __syncthreads();
+  // this thread: column tx, rows ty * CPT .. ty * CPT + CPT - 1 of the tile
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  int it = 0;
+  bool ok = true;
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
+    if (threadIdx.x == 0) {
+      const int tn = t + (VM_NBUF - 1) * gridDim.x;
+      if (tn < n_tiles) {
+        ring.issue(maps, tiles[tn], which, -2, (it + VM_NBUF - 1) % VM_NBUF);
+        ++issued;
       }
-      const unsigned long long b = order_bits<T>(fabs(uz) + fabs(ur));
-      bits = b > bits ? b : bits;
+    }
+    const int4 tr = tiles[t];
+    const axi_case& k = cases[tr.x];
+    const int nr = k.nr, nz = k.nz;
+    const T* __restrict__ rinv2dx = CF<T>(k.rinv2dx);
+    const T ufree = scalar<T>(k, SF_UFREE);
+    if (!__syncthreads_and(ring.wait(it, err))) {
+      ok = false;
+      break;
+    }
+    const T* bx = ring.box(it % VM_NBUF, 0);
+    const int i0 = tr.y, j0 = tr.z;
+    auto bp = [&](int gi, int gj) { return bx[(gi - i0 + 2) * BOXW + (gj - j0 + 4)]; };
+    const int j = j0 + tx;
+    const int ib = i0 + ty * CPT;
+    unsigned long long bits = 0;
+    if (j < nz) {
+#pragma unroll
+      for (int m = 0; m < CPT; ++m) {
+        const int i = ib + m;
+        if (i < nr) {
+          const T rv = rinv2dx[i];
+          T uz, ur;
+          if (i == 0 || i == nr - 1 || j == 0 || j == nz - 1) {
+            velocity_at<T>(k, bp, i, j, rv, ufree, uz, ur);
+          } else {
+            uz = (bp(i + 1, j) - bp(i - 1, j)) * rv + ufree;
+            ur = -(bp(i, j + 1) - bp(i, j - 1)) * rv;
+          }
+          const unsigned long long b = order_bits<T>(fabs(uz) + fabs(ur));
+          bits = b > bits ? b : bits;
+        }
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long other = __shfl_down_sync(0xffffffffu, bits, o);
+      bits = other > bits ? other : bits;
+    }
+    if ((threadIdx.x & 31) == 0) wm[it & 1][threadIdx.x >> 5] = bits;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long m = 0;
+      for (int q = 0; q < NT / 32; ++q) m = wm[it & 1][q] > m ? wm[it & 1][q] : m;
+      atomicMax(reinterpret_cast<unsigned long long*>(&k.state[AXI_ST_UMAX]), m);
+      __threadfence();
+      if (atomicAdd(counter(k, 0), 1u) == dev_tiles_of(k) - 1) {
+        __threadfence();
+        const unsigned long long mb =
+            atomicAdd(reinterpret_cast<unsigned long long*>(&k.state[AXI_ST_UMAX]), 0ull);
+        const double umax = sizeof(T) == 8 ? __longlong_as_double((long long)mb)
+                                           : (double)__uint_as_float((unsigned int)mb);
+        if (!(umax <= 1.7976931348623157e308))
+          atomicOr(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_STATUS]),
+                   1u << AXI_ERR_NONFINITE);
+        const double dt = fmin(k.dt_diff, (k.cfl * k.dx) / (umax + k.eps));
+        k.state[AXI_ST_DT] = dt;
+        k.state[AXI_ST_LAMDT] = k.lam * dt;
+        k.state[AXI_ST_ADV] = -dt / k.dx;
+        k.state[AXI_ST_C1] = 0.5 * k.nu * dt;
+        k.state[AXI_ST_C2] = k.nu * dt;
+        float* f = fslots(k);
+        f[SF_LAMDT] = (float)(k.lam * dt);
+        f[SF_ADV] = (float)(-dt / k.dx);
+        f[SF_C1] = (float)(0.5 * k.nu * dt);
+        f[SF_C2] = (float)(k.nu * dt);
+      }
     }
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long other = __shfl_down_sync(0xffffffffu, bits, o);
-    bits = other > bits ? other : bits;
-  }
-  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = bits;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long m = 0;
-    for (int q = 0; q < NT / 32; ++q) m = wm[q] > m ? wm[q] : m;
-    atomicMax(reinterpret_cast<unsigned long long*>(&k.state[AXI_ST_UMAX]), m);
-    __threadfence();
-    last = (atomicAdd(counter(k, 0), 1u) == dev_tiles_of(k) - 1);
-  }
-  __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    const unsigned long long mb =
-        atomicAdd(reinterpret_cast<unsigned long long*>(&k.state[AXI_ST_UMAX]), 0ull);
-    const double umax = sizeof(T) == 8 ? __longlong_as_double((long long)mb)
-                                       : (double)__uint_as_float((unsigned int)mb);
-    if (!(umax <= 1.7976931348623157e308))
-      atomicOr(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_STATUS]), 1u << AXI_ERR_NONFINITE);
-    const double dt = fmin(k.dt_diff, (k.cfl * k.dx) / (umax + k.eps));
-    k.state[AXI_ST_DT] = dt;
-    k.state[AXI_ST_LAMDT] = k.lam * dt;
-    k.state[AXI_ST_ADV] = -dt / k.dx;
-    k.state[AXI_ST_C1] = 0.5 * k.nu * dt;
-    k.state[AXI_ST_C2] = k.nu * dt;
-    float* f = fslots(k);
-    f[SF_LAMDT] = (float)(k.lam * dt);
-    f[SF_ADV] = (float)(-dt / k.dx);
-    f[SF_C1] = (float)(0.5 * k.nu * dt);
-    f[SF_C2] = (float)(k.nu * dt);
-  }
+  if (!ok && threadIdx.x == 0) ring.drain(it, issued, err);
 }
 
 // ---------------------------------------------------------------------------
 // penalise: flow_past_sphere.py:156-175 (kernels/brinkmann_penalize.py:11-16,
-// kernels/compute_vorticity_from_velocity.py:11-13 on u_pen - u, drag)
+// kernels/compute_vorticity_from_velocity.py:11-13 on u_pen - u, drag).
+// Velocity, penalised velocity and their difference are evaluated once per
+// point of the tile + halo 1 (owned points also store u_pen and add to the
+// drag integrand); the curl of the difference then updates omega of the
+// owned cells.
 // ---------------------------------------------------------------------------
 template <typename T>
 __device__ __forceinline__ void penalise_point(T uz, T ur, T lc, T ubody, T& pz, T& pr) {
@@ -311,168 +419,155 @@ __device__ __forceinline__ void penalise_point(T uz, T ur, T lc, T ubody, T& pz,
   pr = ur * inv;
 }
 
-constexpr int PN_PW = TX + 4, PN_PH = TY + 4;  // psi, halo 2
-constexpr int PN_SW = TX + 2, PN_SH = TY + 2;  // chi and u_pen - u, halo 1
+constexpr int PN_SW = TX + 2, PN_SH = TY + 2;  // u_pen - u, halo 1
+template <typename T>
+using PnRing = BoxRing<T, PN_NBUF, 2, PSI_ROWS>;
 template <typename T>
 constexpr int penalise_smem() {
-  return (int)sizeof(T) * (PN_PH * PN_PW + 3 * PN_SH * PN_SW);
+  return PnRing<T>::BYTES + 2 * PN_SH * PN_SW * (int)sizeof(T) + 128;
 }
 
-// Velocity, penalised velocity and their difference are evaluated once per
-// point of the tile + halo 1 (owned points also store u_pen and add to the
-// drag integrand); the curl of the difference then updates omega of the
-// owned cells.
 template <typename T>
-__global__ void __launch_bounds__(NT) penalise_kernel(const axi_case* __restrict__ cases,
-                                                      const int4* __restrict__ tiles) {
-  extern __shared__ __align__(16) unsigned char pn_smem[];
-  T* ps = reinterpret_cast<T*>(pn_smem);
-  T* sc = ps + PN_PH * PN_PW;
-  T* duz = sc + PN_SH * PN_SW;
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 2) penalise_kernel(const axi_case* __restrict__ cases,
+                                                      const int4* __restrict__ tiles, int n_tiles,
+                                                      const CUtensorMap* __restrict__ maps,
+                                                      int* __restrict__ err) {
+  extern __shared__ unsigned char pn_raw[];
+  __shared__ __align__(8) uint64_t bars[PN_NBUF];
+  __shared__ double red[2][NT / 32];
+  PnRing<T> ring{reinterpret_cast<T*>(align_smem(pn_raw)), axi_tma::smem_u32(bars)};
+  T* duz = ring.base + PnRing<T>::BYTES / sizeof(T);
   T* dur = duz + PN_SH * PN_SW;
-  __shared__ double red[NT / 32];
-  __shared__ bool last;
-  const int4 tr = tiles[blockIdx.x];
-  const axi_case& k = cases[tr.x];
-  const int nr = k.nr, nz = k.nz;
-  const int i0 = tr.y, j0 = tr.z;
-  const T* __restrict__ psi = CF<T>(k.psi);
-  const T* __restrict__ chi = CF<T>(k.chi);
-  const T* __restrict__ rinv2dx = CF<T>(k.rinv2dx);
-  const T* __restrict__ rw = CF<T>(k.rw);
-  const T ufree = scalar<T>(k, SF_UFREE);
-  const T lamdt = scalar<T>(k, SF_LAMDT);
-  const T ubody = scalar<T>(k, SF_UBODY);
-  const T inv2dx = scalar<T>(k, SF_INV2DX);
-  const bool sediment = (k.flags & AXI_CASE_SEDIMENTING) != 0;
-  // all global loads of the block are issued here: psi (halo 2), chi (halo 1)
-  // into shared memory, omega of the owned cells into registers
-  T* w = F<T>(k.omega);
-  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
-  T wown[CPT];
-#pragma unroll
-  for (int q = 0; q < CPT; ++q) {
-    const int gi = i0 + ty + RG * q, gj = j0 + tx;
-    wown[q] = (gi < nr && gj < nz) ? w[gi * nz + gj] : T(0);
-  }
-  for (int e = threadIdx.x; e < PN_PH * PN_PW; e += NT) {
-    const int a = e / PN_PW, b = e - a * PN_PW;
-    const int gi = i0 - 2 + a, gj = j0 - 2 + b;
-    ps[e] = (gi >= 0 && gi < nr && gj >= 0 && gj < nz) ? psi[gi * nz + gj] : T(0);
-  }
-  for (int e = threadIdx.x; e < PN_SH * PN_SW; e += NT) {
-    const int a = e / PN_SW, b = e - a * PN_SW;
-    const int gi = i0 - 1 + a, gj = j0 - 1 + b;
-    sc[e] = (gi >= 0 && gi < nr && gj >= 0 && gj < nz) ? chi[gi * nz + gj] : T(0);
-  }
-  __syncthreads();
-  // every one-sided stencil of an edge cell stays inside the halo-2 tile
-  auto sp = [&](int gi, int gj) { return ps[(gi - i0 + 2) * PN_PW + (gj - j0 + 2)]; };
-  T* uzp = F<T>(k.u_z);
-  T* urp = F<T>(k.u_r);
-  T cd_part = T(0);
-  for (int e = threadIdx.x; e < PN_SH * PN_SW; e += NT) {
-    const int a = e / PN_SW, b = e - a * PN_SW;
-    const int gi = i0 - 1 + a, gj = j0 - 1 + b;
-    T dz = T(0), dr = T(0);
-    if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
-      const T ch = sc[e];
-      T uz, ur, pz, pr;
-      velocity_at<T>(k, sp, gi, gj, rinv2dx[gi], ufree, uz, ur);
-      penalise_point<T>(uz, ur, lamdt * ch, ubody, pz, pr);
-      dz = pz - uz;
-      dr = pr - ur;
-      if (a >= 1 && a <= TY && b >= 1 && b <= TX) {
-        const int c = gi * nz + gj;
-        uzp[c] = pz;
-        urp[c] = pr;
-        // drag / penalisation force integrand r chi (u_z - U_body)
-        // (flow_past_sphere.py:173, compute_forces.py:14)
-        cd_part += rw[gi] * ch * (pz - ubody);
-      }
-    }
-    duz[e] = dz;
-    dur[e] = dr;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int q = 0; q < CPT; ++q) {
-    const int a = ty + RG * q, b = tx;
-    const int gi = i0 + a, gj = j0 + b;
-    if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
-      const int d = (a + 1) * PN_SW + (b + 1);
-      const T pw = (dur[d + 1] - dur[d - 1]) * inv2dx - (duz[d + PN_SW] - duz[d - PN_SW]) * inv2dx;
-      w[gi * nz + gj] = wown[q] + pw;
-    }
-  }
-  // drag: thread and warp sums in T, then warps and tiles in double, fixed order
-  T x = cd_part;
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)x;
-  __syncthreads();
-  const unsigned int ntiles = dev_tiles_of(k);
+  constexpr int which[2] = {MAP_PSI, MAP_CHI};
+  int issued = 0;
   if (threadIdx.x == 0) {
-    double sum = 0.0;
-    for (int q = 0; q < NT / 32; ++q) sum += red[q];
-    k.partials[tr.w] = sum;
-    __threadfence();
-    last = (atomicAdd(counter(k, 1), 1u) == ntiles - 1);
+    ring.init();
+    issued = ring_prologue<PnRing<T>, PN_NBUF, 2>(ring, maps, tiles, n_tiles, which, -2);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    double sum = 0.0;
-    for (unsigned int q = 0; q < ntiles; ++q) sum += ((volatile double*)k.partials)[q];
-    const double dt = k.state[AXI_ST_DT];
-    if (!(sum == sum) || !(fabs(sum) <= 1.7976931348623157e308))
-      atomicOr(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_STATUS]), 1u << AXI_ERR_NONFINITE);
-    k.state[AXI_ST_FORCE] = sum;
-    if (sediment) {
-      // compute_forces.py:14-15 and falling_rigid_sphere.py:155
-      const double f_pen = k.rho_f * k.lam * sum;
-      const double f_un = (k.state[AXI_ST_DIFF] * k.part_vol) / dt;
-      k.state[AXI_ST_FTOTAL] = 2.0 * kPi * k.dx * k.dx * f_pen + f_un;
-    } else {
-      const double cd = k.cd_scale * sum;
-      const long long step = (long long)k.state[AXI_ST_STEPS];
-      if (k.history && step < k.history_len) {
-        k.history[2 * step] = dt;
-        k.history[2 * step + 1] = cd;
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  int it = 0;
+  bool ok = true;
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
+    if (threadIdx.x == 0) {
+      const int tn = t + (PN_NBUF - 1) * gridDim.x;
+      if (tn < n_tiles) {
+        ring.issue(maps, tiles[tn], which, -2, (it + PN_NBUF - 1) % PN_NBUF);
+        ++issued;
       }
-      k.state[AXI_ST_CD] = cd;
+    }
+    const int4 tr = tiles[t];
+    const axi_case& k = cases[tr.x];
+    const int nr = k.nr, nz = k.nz;
+    const int i0 = tr.y, j0 = tr.z;
+    const T* __restrict__ rinv2dx = CF<T>(k.rinv2dx);
+    const T* __restrict__ rw = CF<T>(k.rw);
+    const T ufree = scalar<T>(k, SF_UFREE);
+    const T lamdt = scalar<T>(k, SF_LAMDT);
+    const T ubody = scalar<T>(k, SF_UBODY);
+    const T inv2dx = scalar<T>(k, SF_INV2DX);
+    T* w = F<T>(k.omega);
+    if (!__syncthreads_and(ring.wait(it, err))) {
+      ok = false;
+      break;
+    }
+    const T* ps = ring.box(it % PN_NBUF, 0);
+    const T* sc = ring.box(it % PN_NBUF, 1);
+    // every one-sided stencil of an edge cell stays inside the box
+    auto sp = [&](int gi, int gj) { return ps[(gi - i0 + 2) * BOXW + (gj - j0 + 4)]; };
+    T* uzp = F<T>(k.u_z);
+    T* urp = F<T>(k.u_r);
+    T cd_part = T(0);
+    for (int e = threadIdx.x; e < PN_SH * PN_SW; e += NT) {
+      const int a = e / PN_SW, b = e - a * PN_SW;
+      const int gi = i0 - 1 + a, gj = j0 - 1 + b;
+      T dz = T(0), dr = T(0);
+      if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
+        const T ch = sc[(a + 1) * BOXW + (b + 3)];
+        T uz, ur, pz, pr;
+        velocity_at<T>(k, sp, gi, gj, rinv2dx[gi], ufree, uz, ur);
+        penalise_point<T>(uz, ur, lamdt * ch, ubody, pz, pr);
+        dz = pz - uz;
+        dr = pr - ur;
+        if (a >= 1 && a <= TY && b >= 1 && b <= TX) {
+          const int c = gi * nz + gj;
+          uzp[c] = pz;
+          urp[c] = pr;
+          // drag / penalisation force integrand r chi (u_z - U_body)
+          // (flow_past_sphere.py:173, compute_forces.py:14)
+          cd_part += rw[gi] * ch * (pz - ubody);
+        }
+      }
+      duz[e] = dz;
+      dur[e] = dr;
+    }
+    // omega of the owned cells: all loads issued before the first use
+    T wown[CPT];
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) {
+      const int gi = i0 + ty + RG * q, gj = j0 + tx;
+      wown[q] = (gi < nr && gj < nz) ? w[gi * nz + gj] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) {
+      const int a = ty + RG * q, b = tx;
+      const int gi = i0 + a, gj = j0 + b;
+      if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
+        const int d = (a + 1) * PN_SW + (b + 1);
+        const T pw =
+            (dur[d + 1] - dur[d - 1]) * inv2dx - (duz[d + PN_SW] - duz[d - PN_SW]) * inv2dx;
+        w[gi * nz + gj] = wown[q] + pw;
+      }
+    }
+    // drag: thread and warp sums in T, then warps and tiles in double, fixed order
+    T x = cd_part;
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) red[it & 1][threadIdx.x >> 5] = (double)x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const unsigned int ntiles = dev_tiles_of(k);
+      double sum = 0.0;
+      for (int q = 0; q < NT / 32; ++q) sum += red[it & 1][q];
+      k.partials[tr.w] = sum;
+      __threadfence();
+      if (atomicAdd(counter(k, 1), 1u) == ntiles - 1) {
+        __threadfence();
+        double tot = 0.0;
+        for (unsigned int q = 0; q < ntiles; ++q) tot += ((volatile double*)k.partials)[q];
+        const double dt = k.state[AXI_ST_DT];
+        if (!(tot == tot) || !(fabs(tot) <= 1.7976931348623157e308))
+          atomicOr(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_STATUS]),
+                   1u << AXI_ERR_NONFINITE);
+        k.state[AXI_ST_FORCE] = tot;
+        if (k.flags & AXI_CASE_SEDIMENTING) {
+          // compute_forces.py:14-15 and falling_rigid_sphere.py:155
+          const double f_pen = k.rho_f * k.lam * tot;
+          const double f_un = (k.state[AXI_ST_DIFF] * k.part_vol) / dt;
+          k.state[AXI_ST_FTOTAL] = 2.0 * kPi * k.dx * k.dx * f_pen + f_un;
+        } else {
+          const double cd = k.cd_scale * tot;
+          const long long step = (long long)k.state[AXI_ST_STEPS];
+          if (k.history && step < k.history_len) {
+            k.history[2 * step] = dt;
+            k.history[2 * step + 1] = cd;
+          }
+          k.state[AXI_ST_CD] = cd;
+        }
+      }
     }
   }
+  if (!ok && threadIdx.x == 0) ring.drain(it, issued, err);
 }
 
 // ---------------------------------------------------------------------------
-// adv_diff1: ENO3 advection (kernels/advect_vorticity_via_eno3.py:28-42,
-// pyst_kernels/advection_flux.py:9-163, advection_timestep.py:37-54) and RK2
-// stage 1 (kernels/diffusion_RK2.py:9-26)
+// ENO3 face flux (pyst_kernels/advection_flux.py:9-163)
 // ---------------------------------------------------------------------------
 template <typename T>
 __device__ __forceinline__ T face_flux(T fm1, T f0, T f1, T f2, T um1, T u0, T u1, T u2) {
   const T third = T(1) / T(3), five6 = T(5) / T(6), sixth = T(1) / T(6);
   if (u0 > -u1) return third * f1 * u1 + five6 * f0 * u0 - sixth * fm1 * um1;
   return third * f0 * u0 + five6 * f1 * u1 - sixth * f2 * u2;
-}
-
-// ---------------------------------------------------------------------------
-// advect_diffuse: ENO3 advection (kernels/advect_vorticity_via_eno3.py:28-42,
-// pyst_kernels/advection_flux.py:9-163, advection_timestep.py:37-54) followed
-// by both RK2 diffusion stages (kernels/diffusion_RK2.py:9-44), fused: the
-// block stages omega, u_z, u_r with a halo of 4, advects the tile plus a
-// halo of 2, applies stage 1 on the tile plus a halo of 1 and stage 2 on the
-// tile, all in shared memory, so omega is read and written once per step.
-// Sedimenting cases also rebuild the body mask here and close the step
-// (falling_rigid_sphere.py:156-181).
-// ---------------------------------------------------------------------------
-constexpr int AD_H = 4;
-constexpr int AD_LW = TX + 2 * AD_H, AD_LH = TY + 2 * AD_H;  // staged inputs
-constexpr int AD_AW = TX + 4, AD_AH = TY + 4;                // advected (halo 2)
-constexpr int AD_SW = TX + 2, AD_SH = TY + 2;                // stage 1 (halo 1)
-template <typename T>
-constexpr int advect_diffuse_smem() {
-  return (int)sizeof(T) * (3 * AD_LH * AD_LW + AD_AH * AD_AW + AD_SH * AD_SW);
 }
 
 // Smoothed Heaviside of a sphere level set (kernels/smooth_Heaviside.py:10-14,
@@ -486,158 +581,198 @@ __device__ __forceinline__ T sphere_mask(T z, T r, T zc, T radius, T w) {
   return h;
 }
 
+// ---------------------------------------------------------------------------
+// advect_diffuse: ENO3 advection (kernels/advect_vorticity_via_eno3.py:28-42,
+// pyst_kernels/advection_flux.py:9-163, advection_timestep.py:37-54) followed
+// by both RK2 diffusion stages (kernels/diffusion_RK2.py:9-44), fused: the
+// boxes of omega, u_z, u_r (halo 4) arrive by TMA; the block advects the
+// tile plus a halo of 2, applies stage 1 on the tile plus a halo of 1 and
+// stage 2 on the tile, all in shared memory, so omega is read and written
+// once per step. Rows below the axis are the mirror images of rows 0..3
+// (omega and u_r odd, u_z even). Sedimenting cases also rebuild the body mask
+// here and close the step (falling_rigid_sphere.py:156-181).
+// ---------------------------------------------------------------------------
+constexpr int AD_H = 4;
+constexpr int AD_LW = BOXW;                      // staged inputs: the TMA boxes
+constexpr int AD_AW = TX + 4, AD_AH = TY + 4;    // advected (halo 2)
+constexpr int AD_SW = TX + 2, AD_SH = TY + 2;    // stage 1 (halo 1)
+template <typename T>
+using AdRing = BoxRing<T, AD_NBUF, 3, ADV_ROWS>;
+template <typename T>
+constexpr int advect_diffuse_smem() {
+  return AdRing<T>::BYTES + (int)sizeof(T) * AD_AH * AD_AW + 128;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __restrict__ cases,
-                                                            const int4* __restrict__ tiles) {
-  extern __shared__ __align__(16) unsigned char ad_smem[];
-  T* sw = reinterpret_cast<T*>(ad_smem);
-  T* sz = sw + AD_LH * AD_LW;
-  T* sr = sz + AD_LH * AD_LW;
-  T* wa = sr + AD_LH * AD_LW;
-  T* tp = wa + AD_AH * AD_AW;
-  __shared__ double red[NT / 32];
-  __shared__ bool last;
-  const int4 tr = tiles[blockIdx.x];
-  const axi_case& k = cases[tr.x];
-  const int nr = k.nr, nz = k.nz;
-  const int i0 = tr.y, j0 = tr.z;
-  const T* w = CF<T>(k.omega);
-  const T* uz = CF<T>(k.u_z);
-  const T* ur = CF<T>(k.u_r);
-  const T* rinv2dx = CF<T>(k.rinv2dx);
-  const T* rinv2 = CF<T>(k.rinv2);
-  const T a = scalar<T>(k, SF_ADV);
-  const T c1 = scalar<T>(k, SF_C1);
-  const T c2 = scalar<T>(k, SF_C2);
-  const T inv_dx2 = scalar<T>(k, SF_INVDX2);
-  for (int e = threadIdx.x; e < AD_LH * AD_LW; e += NT) {
-    const int p = e / AD_LW, q = e - p * AD_LW;
-    const int gi = i0 - AD_H + p, gj = j0 - AD_H + q;
-    T vw = T(0), vz = T(0), vr = T(0);
-    if (gj >= 0 && gj < nz && gi < nr) {
-      if (gi >= 0) {
-        const int c = gi * nz + gj;
-        vw = w[c];
-        vz = uz[c];
-        vr = ur[c];
-      } else if (-1 - gi < nr) {
-        // rows below the axis: omega odd, u_z even, u_r odd
-        const int c = (-1 - gi) * nz + gj;
-        vw = -w[c];
-        vz = uz[c];
-        vr = -ur[c];
-      }
-    }
-    sw[e] = vw;
-    sz[e] = vz;
-    sr[e] = vr;
-  }
-  __syncthreads();
-  // advected omega on the tile + halo 2
-  for (int e = threadIdx.x; e < AD_AH * AD_AW; e += NT) {
-    const int p = e / AD_AW, q = e - p * AD_AW;
-    const int gi = i0 - 2 + p, gj = j0 - 2 + q;
-    T val = T(0);
-    if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
-      const int c = (p + 2) * AD_LW + (q + 2);  // position in the staged tile
-      const T f0 = sw[c];
-      T flux = T(0);
-      // pystencils ghost layers: no flux in the last two rows and the first
-      // and last two columns
-      if (gi < nr - 2 && gj >= 2 && gj < nz - 2) {
-        const T xf = face_flux(sw[c - 1], f0, sw[c + 1], sw[c + 2], sz[c - 1], sz[c], sz[c + 1],
-                               sz[c + 2]);
-        const T xb = face_flux(sw[c - 2], sw[c - 1], f0, sw[c + 1], sz[c - 2], sz[c - 1], sz[c],
-                               sz[c + 1]);
-        const int L = AD_LW;
-        const T yf = face_flux(sw[c - L], f0, sw[c + L], sw[c + 2 * L], sr[c - L], sr[c],
-                               sr[c + L], sr[c + 2 * L]);
-        const T yb = face_flux(sw[c - 2 * L], sw[c - L], f0, sw[c + L], sr[c - 2 * L], sr[c - L],
-                               sr[c], sr[c + L]);
-        flux = a * xf;
-        flux = flux - a * xb;
-        flux = flux + a * yf;
-        flux = flux - a * yb;
-      }
-      val = f0 + flux;
-    }
-    wa[e] = val;
-  }
-  __syncthreads();
-  // RK2 stage 1 on the tile + halo 1
-  for (int e = threadIdx.x; e < AD_SH * AD_SW; e += NT) {
-    const int p = e / AD_SW, q = e - p * AD_SW;
-    const int gi = i0 - 1 + p, gj = j0 - 1 + q;
-    T tmp = T(0);
-    if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
-      const int c = (p + 1) * AD_AW + (q + 1);
-      const T c0 = wa[c];
-      tmp = c0;
-      if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
-        const T n = wa[c + AD_AW], s = wa[c - AD_AW], ee = wa[c + 1], ww = wa[c - 1];
-        const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rinv2dx[gi] -
-                      c0 * rinv2[gi];
-        tmp = c0 + c1 * lap;
-      }
-    }
-    tp[e] = tmp;
-  }
-  __syncthreads();
-  // RK2 stage 2 on the tile
-  const bool sediment = (k.flags & AXI_CASE_SEDIMENTING) != 0;
-  const T zc = scalar<T>(k, SF_ZCM);
-  const T rbody = scalar<T>(k, SF_RBODY);
-  const T blendw = scalar<T>(k, SF_BLENDW);
-  T cd_part = T(0);
-#pragma unroll
-  for (int qq = 0; qq < CPT; ++qq) {
-    const int p = threadIdx.x / TX + RG * qq, q = threadIdx.x % TX;
-    const int gi = i0 + p, gj = j0 + q;
-    if (gi < nr && gj < nz) {
-      const int c = gi * nz + gj;
-      T v = wa[(p + 2) * AD_AW + (q + 2)];
-      if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
-        const int d = (p + 1) * AD_SW + (q + 1);
-        const T c0 = tp[d], n = tp[d + AD_SW], s = tp[d - AD_SW], ee = tp[d + 1], ww = tp[d - 1];
-        const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rinv2dx[gi] -
-                      c0 * rinv2[gi];
-        v = v + c2 * lap;
-      }
-      store_omega<T>(k, c, v);
-      if (sediment) {
-        // mask at the body position of this step (falling_rigid_sphere.py:156-157),
-        // then the drag integrand with the new mask (:164-173)
-        const T ch = sphere_mask<T>(CF<T>(k.zw)[gj], CF<T>(k.rw)[gi], zc, rbody, blendw);
-        F<T>(k.chi)[c] = ch;
-        cd_part += CF<T>(k.rw)[gi] * ch * sz[(p + AD_H) * AD_LW + (q + AD_H)];
-      }
-    }
-  }
-  if (!sediment) {
-    if (tr.w == 0 && threadIdx.x == 0) {
-      k.state[AXI_ST_T] += k.state[AXI_ST_DT];
-      k.state[AXI_ST_STEPS] += 1.0;
-    }
-    return;
-  }
-  T x = cd_part;
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)x;
-  __syncthreads();
-  const unsigned int ntiles = dev_tiles_of(k);
+                                                            const int4* __restrict__ tiles,
+                                                            int n_tiles,
+                                                            const CUtensorMap* __restrict__ maps,
+                                                            int* __restrict__ err) {
+  extern __shared__ unsigned char ad_raw[];
+  __shared__ __align__(8) uint64_t bars[AD_NBUF];
+  __shared__ double red[2][NT / 32];
+  AdRing<T> ring{reinterpret_cast<T*>(align_smem(ad_raw)), axi_tma::smem_u32(bars)};
+  T* wa = ring.base + AdRing<T>::BYTES / sizeof(T);
+  constexpr int which[3] = {MAP_W, MAP_UZ, MAP_UR};
+  int issued = 0;
   if (threadIdx.x == 0) {
+    ring.init();
+    issued = ring_prologue<AdRing<T>, AD_NBUF, 3>(ring, maps, tiles, n_tiles, which, -AD_H);
+  }
+  __syncthreads();
+  int it = 0;
+  bool ok = true;
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
+    if (threadIdx.x == 0) {
+      const int tn = t + (AD_NBUF - 1) * gridDim.x;
+      if (tn < n_tiles) {
+        ring.issue(maps, tiles[tn], which, -AD_H, (it + AD_NBUF - 1) % AD_NBUF);
+        ++issued;
+      }
+    }
+    const int4 tr = tiles[t];
+    const axi_case& k = cases[tr.x];
+    const int nr = k.nr, nz = k.nz;
+    const int i0 = tr.y, j0 = tr.z;
+    const T* __restrict__ rinv2dx = CF<T>(k.rinv2dx);
+    const T* __restrict__ rinv2 = CF<T>(k.rinv2);
+    const T a = scalar<T>(k, SF_ADV);
+    const T c1 = scalar<T>(k, SF_C1);
+    const T c2 = scalar<T>(k, SF_C2);
+    const T inv_dx2 = scalar<T>(k, SF_INVDX2);
+    if (!__syncthreads_and(ring.wait(it, err))) {
+      ok = false;
+      break;
+    }
+    T* sw = ring.box(it % AD_NBUF, 0);
+    T* sz = ring.box(it % AD_NBUF, 1);
+    T* sr = ring.box(it % AD_NBUF, 2);
+    // RK2 stage 1 reuses the omega box once the advected values are in wa
+    T* tp = sw;
+    static_assert(AD_SH * AD_SW <= ADV_ROWS * BOXW, "stage-1 tile fits the omega box");
+    if (i0 == 0) {
+      // box rows 0..3 (global rows -4..-1) mirror box rows 7..4 (rows 3..0)
+      for (int e = threadIdx.x; e < AD_H * BOXW; e += NT) {
+        const int p = e / BOXW, q = e - p * BOXW;
+        const int gj = j0 - AD_H + q;
+        if (gj >= 0 && gj < nz) {
+          const int src = (2 * AD_H - 1 - p) * BOXW + q;
+          sw[e] = -sw[src];
+          sz[e] = sz[src];
+          sr[e] = -sr[src];
+        }
+      }
+      __syncthreads();
+    }
+    // advected omega on the tile + halo 2
+    for (int e = threadIdx.x; e < AD_AH * AD_AW; e += NT) {
+      const int p = e / AD_AW, q = e - p * AD_AW;
+      const int gi = i0 - 2 + p, gj = j0 - 2 + q;
+      T val = T(0);
+      if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
+        const int c = (p + 2) * AD_LW + (q + 2);  // position in the staged boxes
+        const T f0 = sw[c];
+        T flux = T(0);
+        // pystencils ghost layers: no flux in the last two rows and the first
+        // and last two columns
+        if (gi < nr - 2 && gj >= 2 && gj < nz - 2) {
+          const T xf = face_flux(sw[c - 1], f0, sw[c + 1], sw[c + 2], sz[c - 1], sz[c], sz[c + 1],
+                                 sz[c + 2]);
+          const T xb = face_flux(sw[c - 2], sw[c - 1], f0, sw[c + 1], sz[c - 2], sz[c - 1], sz[c],
+                                 sz[c + 1]);
+          const int L = AD_LW;
+          const T yf = face_flux(sw[c - L], f0, sw[c + L], sw[c + 2 * L], sr[c - L], sr[c],
+                                 sr[c + L], sr[c + 2 * L]);
+          const T yb = face_flux(sw[c - 2 * L], sw[c - L], f0, sw[c + L], sr[c - 2 * L],
+                                 sr[c - L], sr[c], sr[c + L]);
+          flux = a * xf;
+          flux = flux - a * xb;
+          flux = flux + a * yf;
+          flux = flux - a * yb;
+        }
+        val = f0 + flux;
+      }
+      wa[e] = val;
+    }
+    __syncthreads();
+    // RK2 stage 1 on the tile + halo 1
+    for (int e = threadIdx.x; e < AD_SH * AD_SW; e += NT) {
+      const int p = e / AD_SW, q = e - p * AD_SW;
+      const int gi = i0 - 1 + p, gj = j0 - 1 + q;
+      T tmp = T(0);
+      if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
+        const int c = (p + 1) * AD_AW + (q + 1);
+        const T c0 = wa[c];
+        tmp = c0;
+        if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
+          const T n = wa[c + AD_AW], s = wa[c - AD_AW], ee = wa[c + 1], ww = wa[c - 1];
+          const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rinv2dx[gi] -
+                        c0 * rinv2[gi];
+          tmp = c0 + c1 * lap;
+        }
+      }
+      tp[e] = tmp;
+    }
+    __syncthreads();
+    // RK2 stage 2 on the tile
+    const bool sediment = (k.flags & AXI_CASE_SEDIMENTING) != 0;
+    T cd_part = T(0);
+    {
+      const T zc = scalar<T>(k, SF_ZCM);
+      const T rbody = scalar<T>(k, SF_RBODY);
+      const T blendw = scalar<T>(k, SF_BLENDW);
+#pragma unroll
+      for (int qq = 0; qq < CPT; ++qq) {
+        const int p = threadIdx.x / TX + RG * qq, q = threadIdx.x % TX;
+        const int gi = i0 + p, gj = j0 + q;
+        if (gi < nr && gj < nz) {
+          const int c = gi * nz + gj;
+          T v = wa[(p + 2) * AD_AW + (q + 2)];
+          if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
+            const int d = (p + 1) * AD_SW + (q + 1);
+            const T c0 = tp[d], n = tp[d + AD_SW], s = tp[d - AD_SW], ee = tp[d + 1],
+                    ww = tp[d - 1];
+            const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rinv2dx[gi] -
+                          c0 * rinv2[gi];
+            v = v + c2 * lap;
+          }
+          store_omega<T>(k, c, v);
+          if (sediment) {
+            // mask at the body position of this step (falling_rigid_sphere.py:156-157),
+            // then the drag integrand with the new mask (:164-173)
+            const T ch = sphere_mask<T>(CF<T>(k.zw)[gj], CF<T>(k.rw)[gi], zc, rbody, blendw);
+            F<T>(k.chi)[c] = ch;
+            cd_part += CF<T>(k.rw)[gi] * ch * sz[(p + AD_H) * AD_LW + (q + AD_H)];
+          }
+        }
+      }
+    }
+    if (sediment) {
+      T x = cd_part;
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if ((threadIdx.x & 31) == 0) red[it & 1][threadIdx.x >> 5] = (double)x;
+    }
+    // end of tile: the boxes and wa / tp may be reused from here on
+    __syncthreads();
+    if (threadIdx.x != 0) continue;
+    if (!sediment) {
+      if (tr.w == 0) {
+        k.state[AXI_ST_T] += k.state[AXI_ST_DT];
+        k.state[AXI_ST_STEPS] += 1.0;
+      }
+      continue;
+    }
+    const unsigned int ntiles = dev_tiles_of(k);
     double sum = 0.0;
-    for (int q = 0; q < NT / 32; ++q) sum += red[q];
+    for (int q = 0; q < NT / 32; ++q) sum += red[it & 1][q];
     k.partials[ntiles + tr.w] = sum;
     __threadfence();
-    last = (atomicAdd(counter(k, 1), 1u) == 2 * ntiles - 1);
-  }
-  __syncthreads();
-  if (last && threadIdx.x == 0) {
+    if (atomicAdd(counter(k, 1), 1u) != 2 * ntiles - 1) continue;
     __threadfence();
-    double sum = 0.0;
-    for (unsigned int q = 0; q < ntiles; ++q) sum += ((volatile double*)k.partials)[ntiles + q];
-    const double cd = k.cd_scale * sum;
+    double tot = 0.0;
+    for (unsigned int q = 0; q < ntiles; ++q) tot += ((volatile double*)k.partials)[ntiles + q];
+    const double cd = k.cd_scale * tot;
     const double dt = k.state[AXI_ST_DT];
     // body ODE, falling_rigid_sphere.py:176-181 (FP64)
     const double ft = k.state[AXI_ST_FTOTAL];
@@ -657,6 +792,7 @@ __global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __re
     k.state[AXI_ST_T] += dt;
     k.state[AXI_ST_STEPS] += 1.0;
   }
+  if (!ok && threadIdx.x == 0) ring.drain(it, issued, err);
 }
 
 // Recomputes the TF32 hi / lo operand copy of omega from omega (after the
@@ -786,23 +922,28 @@ struct PlanView {
   const axi_case* cases;
   const int4* stencil;
   const int4* gemm;
+  const CUtensorMap* maps;
   const axi_tc::TcJob* jobs;
   const int4* tc_tiles[4];
-  int* tc_err;
+  int* err;
 };
 
 inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 inline size_t align128(size_t x) { return (x + 127) & ~size_t(127); }
 
 struct PlanOffsets {
-  size_t stencil, gemm, jobs, tc_tiles[4], err, total;
+  size_t stencil, gemm, maps, jobs, tc_tiles[4], err, total;
 };
 
+// Plan buffer: cases | stencil tiles | SIMT GEMM tiles | stencil tensor maps
+// (MAP_COUNT per case) | [tensor-core jobs | tensor-core tiles x 4] | error word
 inline PlanOffsets plan_offsets(const axi_plan_info* info) {
   PlanOffsets o;
   o.stencil = align16(info->n_cases * sizeof(axi_case));
   o.gemm = o.stencil + (size_t)info->n_stencil_tiles * sizeof(int4);
   size_t end = o.gemm + (size_t)info->n_gemm_tiles * sizeof(int4);
+  o.maps = align128(end);
+  end = o.maps + (size_t)MAP_COUNT * info->n_cases * sizeof(CUtensorMap);
   if (info->flags & AXI_PLAN_TENSOR_CORES) {
     o.jobs = align128(end);
     end = o.jobs + (size_t)4 * info->n_cases * sizeof(axi_tc::TcJob);
@@ -810,12 +951,12 @@ inline PlanOffsets plan_offsets(const axi_plan_info* info) {
       o.tc_tiles[st] = align16(end);
       end = o.tc_tiles[st] + (size_t)info->n_tc_tiles[st] * sizeof(int4);
     }
-    o.err = align16(end);
-    end = o.err + 16;
   } else {
-    o.jobs = o.err = 0;
+    o.jobs = 0;
     for (int st = 0; st < 4; ++st) o.tc_tiles[st] = 0;
   }
+  o.err = align16(end);
+  end = o.err + 16;
   o.total = align16(end);
   return o;
 }
@@ -827,11 +968,12 @@ inline PlanView plan_view(const void* plan_dev, const axi_plan_info* info) {
   v.cases = reinterpret_cast<const axi_case*>(base);
   v.stencil = reinterpret_cast<const int4*>(base + o.stencil);
   v.gemm = reinterpret_cast<const int4*>(base + o.gemm);
+  v.maps = reinterpret_cast<const CUtensorMap*>(base + o.maps);
   const bool tc = (info->flags & AXI_PLAN_TENSOR_CORES) != 0;
   v.jobs = tc ? reinterpret_cast<const axi_tc::TcJob*>(base + o.jobs) : nullptr;
   for (int st = 0; st < 4; ++st)
     v.tc_tiles[st] = tc ? reinterpret_cast<const int4*>(base + o.tc_tiles[st]) : nullptr;
-  v.tc_err = tc ? reinterpret_cast<int*>(const_cast<char*>(base) + o.err) : nullptr;
+  v.err = reinterpret_cast<int*>(const_cast<char*>(base) + o.err);
   return v;
 }
 
@@ -889,24 +1031,57 @@ inline int tc_tiles_of(const axi_case& k, int stage) {
 enum { PH_KILL = 0, PH_TRANSFORM = 1, PH_VEL_MAX = 2, PH_PENALISE = 3, PH_ADVECT_DIFFUSE = 4,
        PH_COUNT = 5 };
 
-// Both stencil kernels with a dynamic shared-memory tile reserve it once per
-// process (the double engine's tiles exceed the 48 KB default).
+// The persistent stencil kernels reserve their dynamic shared memory once per
+// process and run as many blocks as fit on every SM (at most one block per
+// tile).
 template <typename T>
 int stencil_attrs() {
   static int status = -1;
   if (status < 0) {
-    status = (cudaFuncSetAttribute(advect_diffuse_kernel<T>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   advect_diffuse_smem<T>()) == cudaSuccess &&
+    status = (cudaFuncSetAttribute(vel_max_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   vel_max_smem<T>()) == cudaSuccess &&
               cudaFuncSetAttribute(penalise_kernel<T>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   penalise_smem<T>()) == cudaSuccess)
+                                   penalise_smem<T>()) == cudaSuccess &&
+              cudaFuncSetAttribute(advect_diffuse_kernel<T>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   advect_diffuse_smem<T>()) == cudaSuccess)
                  ? AXI_OK
                  : AXI_ERR_CUDA;
     if (status != AXI_OK) axi::set_error("rigid_step: cannot reserve shared memory");
   }
   return status;
 }
+
+template <typename T>
+struct StencilGrid {
+  // blocks per SM of each stencil phase, measured once
+  static int per_sm(int phase) {
+    static int n[PH_COUNT] = {0};
+    if (n[phase] == 0) {
+      int b = 0;
+      cudaError_t e = cudaErrorInvalidValue;
+      if (phase == PH_VEL_MAX)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, vel_max_kernel<T>, NT,
+                                                          vel_max_smem<T>());
+      else if (phase == PH_PENALISE)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, penalise_kernel<T>, NT,
+                                                          penalise_smem<T>());
+      else if (phase == PH_ADVECT_DIFFUSE)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, advect_diffuse_kernel<T>, NT,
+                                                          advect_diffuse_smem<T>());
+      n[phase] = (e == cudaSuccess && b > 0) ? b : 1;
+    }
+    return n[phase];
+  }
+  static int get(int phase, int n_tiles) {
+    // ring depth 1: one block per tile
+    if ((phase == PH_PENALISE && PN_NBUF == 1) || (phase == PH_ADVECT_DIFFUSE && AD_NBUF == 1))
+      return n_tiles;
+    const int g = per_sm(phase) * axi::sm_count();
+    return n_tiles < g ? n_tiles : g;
+  }
+};
 
 template <typename T>
 int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStream_t s) {
@@ -918,7 +1093,7 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
     case PH_TRANSFORM:
       if (v.jobs) {
         for (int st = 0; st < 4; ++st)
-          AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[st], info->n_tc_tiles[st], v.tc_err, s));
+          AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[st], info->n_tc_tiles[st], v.err, s));
         break;
       }
       grouped_gemm_kernel<T, 0><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
@@ -927,15 +1102,20 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
       grouped_gemm_kernel<T, 3><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
       break;
     case PH_VEL_MAX:
-      vel_max_kernel<T><<<nt, NT, 0, s>>>(v.cases, v.stencil);
+      AXI_TRY(stencil_attrs<T>());
+      vel_max_kernel<T><<<StencilGrid<T>::get(PH_VEL_MAX, nt), NT, vel_max_smem<T>(), s>>>(
+          v.cases, v.stencil, nt, v.maps, v.err);
       break;
     case PH_PENALISE:
       AXI_TRY(stencil_attrs<T>());
-      penalise_kernel<T><<<nt, NT, penalise_smem<T>(), s>>>(v.cases, v.stencil);
+      penalise_kernel<T><<<StencilGrid<T>::get(PH_PENALISE, nt), NT, penalise_smem<T>(), s>>>(
+          v.cases, v.stencil, nt, v.maps, v.err);
       break;
     case PH_ADVECT_DIFFUSE:
       AXI_TRY(stencil_attrs<T>());
-      advect_diffuse_kernel<T><<<nt, NT, advect_diffuse_smem<T>(), s>>>(v.cases, v.stencil);
+      advect_diffuse_kernel<T>
+          <<<StencilGrid<T>::get(PH_ADVECT_DIFFUSE, nt), NT, advect_diffuse_smem<T>(), s>>>(
+              v.cases, v.stencil, nt, v.maps, v.err);
       break;
     default:
       axi::set_error("rigid_phase: unknown phase %d", phase);
@@ -952,9 +1132,9 @@ int validate(const axi_case* cases, int n_cases, const char* what) {
   for (int c = 0; c < n_cases; ++c) {
     const axi_case& k = cases[c];
     if (k.nr < 8 || k.nz < 8 || k.kill_width < 2 || k.kill_width > 8 || 2 * k.kill_width > k.nz ||
-        k.kill_width > k.nr || (int64_t)k.nr * k.nz >= ((int64_t)1 << 31)) {
-      axi::set_error("%s: case %d has an unsupported grid %d x %d / kill width %d", what, c, k.nr,
-                     k.nz, k.kill_width);
+        k.kill_width > k.nr || (int64_t)k.nr * k.nz >= ((int64_t)1 << 31) || (k.nz % 4) != 0) {
+      axi::set_error("%s: case %d has an unsupported grid %d x %d / kill width %d (nz must be a "
+                     "multiple of 4)", what, c, k.nr, k.nz, k.kill_width);
       return AXI_ERR_INVALID;
     }
     const void* ptrs[] = {k.omega, k.psi, k.u_z, k.u_r, k.chi, k.kill_coef, k.r, k.z,
@@ -1086,8 +1266,20 @@ extern "C" int axi_plan_upload(const axi_case* cases, const axi_plan_info* info,
     axi::set_error("plan_upload: cases changed since plan_init");
     return AXI_ERR_INVALID;
   }
+  const PlanOffsets po = plan_offsets(info);
+  CUtensorMap* maps = reinterpret_cast<CUtensorMap*>(&buf[po.maps]);
+  for (int c = 0; c < n; ++c) {
+    const axi_case& k = cases[c];
+    const int eb = info->elem_bytes;
+    CUtensorMap* m = maps + MAP_COUNT * c;
+    AXI_TRY(axi_tma::encode_box(m + MAP_PSI, k.psi, eb, k.nr, k.nz, PSI_ROWS, BOXW));
+    AXI_TRY(axi_tma::encode_box(m + MAP_CHI, k.chi, eb, k.nr, k.nz, PSI_ROWS, BOXW));
+    AXI_TRY(axi_tma::encode_box(m + MAP_W, k.omega, eb, k.nr, k.nz, ADV_ROWS, BOXW));
+    AXI_TRY(axi_tma::encode_box(m + MAP_UZ, k.u_z, eb, k.nr, k.nz, ADV_ROWS, BOXW));
+    AXI_TRY(axi_tma::encode_box(m + MAP_UR, k.u_r, eb, k.nr, k.nz, ADV_ROWS, BOXW));
+  }
   if (info->flags & AXI_PLAN_TENSOR_CORES) {
-    const PlanOffsets o = plan_offsets(info);
+    const PlanOffsets& o = po;
     axi_tc::TcJob* jobs = reinterpret_cast<axi_tc::TcJob*>(&buf[o.jobs]);
     for (int c = 0; c < n; ++c) AXI_TRY(build_tc_jobs(cases[c], jobs + 4 * c));
     for (int st = 0; st < 4; ++st) {
@@ -1131,10 +1323,9 @@ extern "C" int axi_plan_tc_status(const axi_plan_info* info, const void* plan_de
   AXI_TRY(axi::check_ptr("plan_tc_status", info, "info"));
   AXI_TRY(axi::check_ptr("plan_tc_status", plan_dev, "plan_dev"));
   *tc_error = 0;
-  if (!(info->flags & AXI_PLAN_TENSOR_CORES)) return AXI_OK;
   const PlanView v = plan_view(plan_dev, info);
   cudaStream_t s = axi::as_stream(stream);
-  if (cudaMemcpyAsync(tc_error, v.tc_err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+  if (cudaMemcpyAsync(tc_error, v.err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return axi::launch_status("plan_tc_status");
   return AXI_OK;

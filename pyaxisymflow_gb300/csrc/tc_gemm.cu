@@ -10,60 +10,13 @@
 namespace axi_tc {
 namespace {
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ uint64_t globaltimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait on an mbarrier phase. False on timeout (error recorded) or when
-// another thread of the grid has already failed.
-__device__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = globaltimer();
-  for (;;) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if (*reinterpret_cast<volatile int*>(err) != 0) return false;
-    if (globaltimer() - t0 > WAIT_NS) {
-      atomicCAS(err, 0, code);
-      return false;
-    }
-  }
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1,
-                                            uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
-      : "memory");
-}
+using axi_tma::globaltimer;
+using axi_tma::mbar_expect_tx;
+using axi_tma::mbar_init;
+using axi_tma::mbar_try_wait;
+using axi_tma::mbar_wait;
+using axi_tma::smem_u32;
+using axi_tma::tma_load_2d;
 
 __device__ __forceinline__ void tmem_alloc(uint32_t slot, uint32_t ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot),
@@ -310,7 +263,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (threadIdx.x == 0 && progress[1] < progress[0]) {
     // a failure left copies in flight: wait for them (bounded) before exiting
     for (int g = progress[1]; g < progress[0]; ++g)
-      mbar_wait(full0 + 8 * (g % NSTAGE), (g / NSTAGE) & 1, err, ERR_DRAIN);
+      if (!axi_tma::mbar_wait_drain(full0 + 8 * (g % NSTAGE), (g / NSTAGE) & 1))
+        atomicCAS(err, 0, ERR_DRAIN);
   }
   tc_fence_before();
   __syncthreads();
@@ -319,17 +273,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                         &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  });
-  return fn;
+  return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(axi_tma::encode_tiled_fn());
 }
 
 }  // namespace
@@ -377,6 +321,54 @@ int launch(const TcJob* jobs_dev, const int4* tiles_dev, int n_tiles, int* err_d
 }
 
 }  // namespace axi_tc
+
+namespace axi_tma {
+
+void* encode_tiled_fn() {
+  static void* fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = p;
+  });
+  return fn;
+}
+
+int encode_box(CUtensorMap* map, const void* base, int elem_bytes, int rows, int cols,
+               int box_rows, int box_cols) {
+  auto fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(encode_tiled_fn());
+  if (!fn) {
+    axi::set_error("tensor map: cuTensorMapEncodeTiled unavailable");
+    return AXI_ERR_CUDA;
+  }
+  if ((elem_bytes != 4 && elem_bytes != 8) || (reinterpret_cast<uintptr_t>(base) & 15) != 0 ||
+      ((int64_t)cols * elem_bytes) % 16 != 0 || (box_cols * elem_bytes) % 16 != 0 ||
+      box_rows < 1 || box_rows > 256 || box_cols < 1 || box_cols > 256) {
+    axi::set_error("tensor map: %d x %d array (box %d x %d) breaks the 16-byte rules", rows, cols,
+                   box_rows, box_cols);
+    return AXI_ERR_INVALID;
+  }
+  const cuuint64_t dims[2] = {static_cast<cuuint64_t>(cols), static_cast<cuuint64_t>(rows)};
+  const cuuint64_t strides[1] = {static_cast<cuuint64_t>(cols) * elem_bytes};
+  const cuuint32_t box[2] = {static_cast<cuuint32_t>(box_cols), static_cast<cuuint32_t>(box_rows)};
+  const cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                       : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                  2, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    axi::set_error("tensor map: cuTensorMapEncodeTiled failed (%d)", static_cast<int>(r));
+    return AXI_ERR_CUDA;
+  }
+  return AXI_OK;
+}
+
+}  // namespace axi_tma
 
 // ---------------------------------------------------------------------------
 // Standalone entry: C (M, N) = A (M, K) * B (N, K)^T in FP32 via 3xTF32.

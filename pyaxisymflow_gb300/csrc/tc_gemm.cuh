@@ -29,6 +29,7 @@
 #include <cstdint>
 
 #include "axi_common.cuh"
+#include "tma.cuh"
 
 
 namespace axi_tc {
@@ -42,7 +43,6 @@ constexpr int STAGE_BYTES = 4 * TILE_BYTES;     // A_hi, A_lo, B_hi, B_lo
 constexpr int EPI_WARPS = 4;
 constexpr int THREADS = 32 * (2 + EPI_WARPS);   // TMA warp, MMA warp, 4 epilogue warps
 constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 + 256 + EPI_WARPS * 32 * 33 * 4;
-constexpr unsigned long long WAIT_NS = 1000000000ull;
 
 enum { MODE_PLAIN = 0, MODE_SPLIT = 1, MODE_SCALE_SPLIT = 2 };
 enum { ERR_PRODUCER = 1, ERR_MMA = 2, ERR_EPILOGUE = 3, ERR_DRAIN = 4 };
