@@ -10,22 +10,23 @@
 //
 // Launches per step, each covering every case of the plan:
 //   kill_reset   one block per case: sine tapers, free stream of this step,
-//                counters cleared
+//                counters cleared, float copies of the step scalars
 //   transform    four grouped dense products (the spectral Poisson solve)
-//   vel_max      per tile: max(|u_z| + |u_r|); the last tile of a case turns
-//                it into dt and the dt-dependent constants of the step
+//   vel_max      persistent, per tile: max(|u_z| + |u_r|) into the case
+//   step_dt      one thread per case: dt and the dt-dependent constants
 //   penalise     per tile: velocity + Brinkman + curl(u_pen - u) into omega,
 //                drag partials; the last tile of a case finalises the drag
-//   advect_diffuse per tile: ENO3 advection (axis mirror by index reflection)
-//                and both RK2 stages in shared memory (halo 4); advances the
-//                time (sedimenting cases: mask rebuild, drag, body ODE)
+//   advect_diffuse per tile: ENO3 advection (axis mirror) and both RK2
+//                stages in shared memory (halo 4); advances the time
+//                (sedimenting cases: mask rebuild, drag, body ODE)
+// The stencil kernels receive their halo boxes by TMA.
 //
-// GB300 runs FP64 at 1/70 of its FP32 rate, so the FP32 engine keeps every
-// per-cell operation in FP32: per-row factors (1 / (2 dx r), 1 / r^2, r) are
-// precomputed vectors in the engine precision and the per-step scalars are
-// computed once per case. FP64 remains where the reference needs it: the
-// axis / outer-boundary one-sided rows of u_z (the r = 0 closure), the time
-// step, time and the drag sums across warps and tiles.
+// GB300 runs FP64 at a small fraction of its FP32 rate, so the FP32 engine
+// keeps every per-cell operation in FP32: per-row factors (1 / (2 dx r),
+// 1 / r^2, r) are precomputed vectors in the engine precision and the
+// per-step scalars are computed once per case. FP64 remains in the time
+// step, the simulated time, the drag sums across warps and tiles and the
+// body ODE.
 #include "axi_common.cuh"
 #include "tc_gemm.cuh"
 #include "tma.cuh"
@@ -289,8 +290,9 @@ __device__ __forceinline__ int ring_prologue(const Ring& ring, const CUtensorMap
 }
 
 // ---------------------------------------------------------------------------
-// vel_max: max over the case of |u_z| + |u_r| (flow_past_sphere.py:150-153);
-// the last tile of the case derives dt and the per-step constants.
+// vel_max: max over the case of |u_z| + |u_r| (flow_past_sphere.py:150-153),
+// one atomic maximum per tile. step_dt_kernel turns it into dt (one thread
+// per case), so no tile waits on a per-case counter.
 // ---------------------------------------------------------------------------
 template <typename T>
 __device__ __forceinline__ unsigned long long order_bits(T v) {
@@ -376,29 +378,8 @@ __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict_
     if (threadIdx.x == 0) {
       unsigned long long m = 0;
       for (int q = 0; q < NT / 32; ++q) m = wm[it & 1][q] > m ? wm[it & 1][q] : m;
+      // fire-and-forget: the maximum is read after this kernel has finished
       atomicMax(reinterpret_cast<unsigned long long*>(&k.state[AXI_ST_UMAX]), m);
-      __threadfence();
-      if (atomicAdd(counter(k, 0), 1u) == dev_tiles_of(k) - 1) {
-        __threadfence();
-        const unsigned long long mb =
-            atomicAdd(reinterpret_cast<unsigned long long*>(&k.state[AXI_ST_UMAX]), 0ull);
-        const double umax = sizeof(T) == 8 ? __longlong_as_double((long long)mb)
-                                           : (double)__uint_as_float((unsigned int)mb);
-        if (!(umax <= 1.7976931348623157e308))
-          atomicOr(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_STATUS]),
-                   1u << AXI_ERR_NONFINITE);
-        const double dt = fmin(k.dt_diff, (k.cfl * k.dx) / (umax + k.eps));
-        k.state[AXI_ST_DT] = dt;
-        k.state[AXI_ST_LAMDT] = k.lam * dt;
-        k.state[AXI_ST_ADV] = -dt / k.dx;
-        k.state[AXI_ST_C1] = 0.5 * k.nu * dt;
-        k.state[AXI_ST_C2] = k.nu * dt;
-        float* f = fslots(k);
-        f[SF_LAMDT] = (float)(k.lam * dt);
-        f[SF_ADV] = (float)(-dt / k.dx);
-        f[SF_C1] = (float)(0.5 * k.nu * dt);
-        f[SF_C2] = (float)(k.nu * dt);
-      }
     }
   }
   if (!ok && threadIdx.x == 0) ring.drain(it, issued, err);
@@ -412,6 +393,42 @@ __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict_
 // drag integrand); the curl of the difference then updates omega of the
 // owned cells.
 // ---------------------------------------------------------------------------
+// dt = min(diffusive limit, CFL / max(|u_z| + |u_r|)) (flow_past_sphere.py:150-155)
+// from the maximum that vel_max left in the state block. Every block that
+// needs dt evaluates it from the same bits, so all get the same value.
+template <typename T>
+__device__ __forceinline__ double step_dt(const axi_case& k, double* umax_out = nullptr) {
+  const unsigned long long mb =
+      *reinterpret_cast<const volatile unsigned long long*>(&k.state[AXI_ST_UMAX]);
+  const double umax = sizeof(T) == 8 ? __longlong_as_double((long long)mb)
+                                     : (double)__uint_as_float((unsigned int)mb);
+  if (umax_out) *umax_out = umax;
+  return fmin(k.dt_diff, (k.cfl * k.dx) / (umax + k.eps));
+}
+
+// One thread per case: dt and the dt-dependent constants of the step (double
+// state words and the float copies), between vel_max and penalise.
+template <typename T>
+__global__ void step_dt_kernel(const axi_case* __restrict__ cases, int n_cases) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cases) return;
+  const axi_case& k = cases[c];
+  double umax;
+  const double dt = step_dt<T>(k, &umax);
+  if (!(umax <= 1.7976931348623157e308))
+    atomicOr(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_STATUS]), 1u << AXI_ERR_NONFINITE);
+  k.state[AXI_ST_DT] = dt;
+  k.state[AXI_ST_LAMDT] = k.lam * dt;
+  k.state[AXI_ST_ADV] = -dt / k.dx;
+  k.state[AXI_ST_C1] = 0.5 * k.nu * dt;
+  k.state[AXI_ST_C2] = k.nu * dt;
+  float* f = fslots(k);
+  f[SF_LAMDT] = (float)(k.lam * dt);
+  f[SF_ADV] = (float)(-dt / k.dx);
+  f[SF_C1] = (float)(0.5 * k.nu * dt);
+  f[SF_C2] = (float)(k.nu * dt);
+}
+
 template <typename T>
 __device__ __forceinline__ void penalise_point(T uz, T ur, T lc, T ubody, T& pz, T& pr) {
   const T inv = T(1) / (T(1) + lc);
@@ -435,6 +452,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 2) penalise_kernel(co
   extern __shared__ unsigned char pn_raw[];
   __shared__ __align__(8) uint64_t bars[PN_NBUF];
   __shared__ double red[2][NT / 32];
+  __shared__ T rowf[2][PN_SH];
   PnRing<T> ring{reinterpret_cast<T*>(align_smem(pn_raw)), axi_tma::smem_u32(bars)};
   T* duz = ring.base + PnRing<T>::BYTES / sizeof(T);
   T* dur = duz + PN_SH * PN_SW;
@@ -463,10 +481,16 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 2) penalise_kernel(co
     const T* __restrict__ rinv2dx = CF<T>(k.rinv2dx);
     const T* __restrict__ rw = CF<T>(k.rw);
     const T ufree = scalar<T>(k, SF_UFREE);
-    const T lamdt = scalar<T>(k, SF_LAMDT);
     const T ubody = scalar<T>(k, SF_UBODY);
     const T inv2dx = scalar<T>(k, SF_INV2DX);
     T* w = F<T>(k.omega);
+    const T lamdt = scalar<T>(k, SF_LAMDT);
+    // per-row factors of the tile + halo 1 (rows i0 - 1 .. i0 + TY)
+    if (threadIdx.x < PN_SH) {
+      const int gi = min(max(i0 - 1 + (int)threadIdx.x, 0), nr - 1);
+      rowf[0][threadIdx.x] = rinv2dx[gi];
+      rowf[1][threadIdx.x] = rw[gi];
+    }
     if (!__syncthreads_and(ring.wait(it, err))) {
       ok = false;
       break;
@@ -485,7 +509,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 2) penalise_kernel(co
       if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
         const T ch = sc[(a + 1) * BOXW + (b + 3)];
         T uz, ur, pz, pr;
-        velocity_at<T>(k, sp, gi, gj, rinv2dx[gi], ufree, uz, ur);
+        velocity_at<T>(k, sp, gi, gj, rowf[0][a], ufree, uz, ur);
         penalise_point<T>(uz, ur, lamdt * ch, ubody, pz, pr);
         dz = pz - uz;
         dr = pr - ur;
@@ -495,7 +519,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 2) penalise_kernel(co
           urp[c] = pr;
           // drag / penalisation force integrand r chi (u_z - U_body)
           // (flow_past_sphere.py:173, compute_forces.py:14)
-          cd_part += rw[gi] * ch * (pz - ubody);
+          cd_part += rowf[1][a] * ch * (pz - ubody);
         }
       }
       duz[e] = dz;
@@ -612,6 +636,7 @@ __global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __re
   extern __shared__ unsigned char ad_raw[];
   __shared__ __align__(8) uint64_t bars[AD_NBUF];
   __shared__ double red[2][NT / 32];
+  __shared__ T rowf[3][AD_SH];  // 1 / (2 dx r), 1 / r^2, r of rows i0 - 1 .. i0 + TY
   AdRing<T> ring{reinterpret_cast<T*>(align_smem(ad_raw)), axi_tma::smem_u32(bars)};
   T* wa = ring.base + AdRing<T>::BYTES / sizeof(T);
   constexpr int which[3] = {MAP_W, MAP_UZ, MAP_UR};
@@ -641,6 +666,12 @@ __global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __re
     const T c1 = scalar<T>(k, SF_C1);
     const T c2 = scalar<T>(k, SF_C2);
     const T inv_dx2 = scalar<T>(k, SF_INVDX2);
+    if (threadIdx.x < AD_SH) {
+      const int gi = min(max(i0 - 1 + (int)threadIdx.x, 0), nr - 1);
+      rowf[0][threadIdx.x] = rinv2dx[gi];
+      rowf[1][threadIdx.x] = rinv2[gi];
+      rowf[2][threadIdx.x] = CF<T>(k.rw)[gi];
+    }
     if (!__syncthreads_and(ring.wait(it, err))) {
       ok = false;
       break;
@@ -707,8 +738,8 @@ __global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __re
         tmp = c0;
         if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
           const T n = wa[c + AD_AW], s = wa[c - AD_AW], ee = wa[c + 1], ww = wa[c - 1];
-          const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rinv2dx[gi] -
-                        c0 * rinv2[gi];
+          const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rowf[0][p] -
+                        c0 * rowf[1][p];
           tmp = c0 + c1 * lap;
         }
       }
@@ -722,6 +753,8 @@ __global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __re
       const T zc = scalar<T>(k, SF_ZCM);
       const T rbody = scalar<T>(k, SF_RBODY);
       const T blendw = scalar<T>(k, SF_BLENDW);
+      const int gjt = j0 + threadIdx.x % TX;
+      const T zcol = (sediment && gjt < nz) ? CF<T>(k.zw)[gjt] : T(0);
 #pragma unroll
       for (int qq = 0; qq < CPT; ++qq) {
         const int p = threadIdx.x / TX + RG * qq, q = threadIdx.x % TX;
@@ -733,17 +766,18 @@ __global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __re
             const int d = (p + 1) * AD_SW + (q + 1);
             const T c0 = tp[d], n = tp[d + AD_SW], s = tp[d - AD_SW], ee = tp[d + 1],
                     ww = tp[d - 1];
-            const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rinv2dx[gi] -
-                          c0 * rinv2[gi];
+            const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rowf[0][p + 1] -
+                          c0 * rowf[1][p + 1];
             v = v + c2 * lap;
           }
           store_omega<T>(k, c, v);
           if (sediment) {
             // mask at the body position of this step (falling_rigid_sphere.py:156-157),
             // then the drag integrand with the new mask (:164-173)
-            const T ch = sphere_mask<T>(CF<T>(k.zw)[gj], CF<T>(k.rw)[gi], zc, rbody, blendw);
+            const T rr = rowf[2][p + 1];
+            const T ch = sphere_mask<T>(zcol, rr, zc, rbody, blendw);
             F<T>(k.chi)[c] = ch;
-            cd_part += CF<T>(k.rw)[gi] * ch * sz[(p + AD_H) * AD_LW + (q + AD_H)];
+            cd_part += rr * ch * sz[(p + AD_H) * AD_LW + (q + AD_H)];
           }
         }
       }
@@ -1105,6 +1139,7 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
       AXI_TRY(stencil_attrs<T>());
       vel_max_kernel<T><<<StencilGrid<T>::get(PH_VEL_MAX, nt), NT, vel_max_smem<T>(), s>>>(
           v.cases, v.stencil, nt, v.maps, v.err);
+      step_dt_kernel<T><<<(info->n_cases + 127) / 128, 128, 0, s>>>(v.cases, info->n_cases);
       break;
     case PH_PENALISE:
       AXI_TRY(stencil_attrs<T>());
