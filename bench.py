@@ -46,6 +46,13 @@ PHASES = ("kill", "transform", "vel_max", "penalise", "advect_diffuse")
 PHASE_FIELDS = {"vel_max": 1, "penalise": 6, "advect_diffuse": 4}
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of a phase, from the
+# ncu captures summarised in profiles/ (transform: sum over its four products).
+NCU_TRAFFIC = {
+    ("ensemble64", "f32", "transform"): None,
+}
+
+
 def ensemble_cases(workload, seed=4):
     from pyaxisymflow_gb300.engine import RigidBodyCase
     if workload == "sphere512":
@@ -144,38 +151,53 @@ def max_over_ranks(world, x):
     return float(t.item())
 
 
-def cpu_oracle_rate(cases, steps):
-    """Oracle (numpy FP64) cell-updates/s on the host for `cases`, `steps` steps each."""
-    from oracle import kernels as K
-    from oracle import simulation as sim
-    runs = []
-    for c in cases:
-        if c.sediment:
-            oc = sim.SedimentingCase(nz=c.nz, nr=c.nr, dx=c.dx, z_cm=c.z_cm,
-                                     r_sphere=c.r_sphere, rho_f=c.rho_f, rho_s=c.rho_s,
-                                     nu=c.nu, lam=c.lam, cfl=c.cfl, kill_width=c.kill_width,
-                                     gravity=c.gravity)
-            w0 = c.noise * np.random.default_rng(c.seed).standard_normal((c.nr, c.nz))
-            st, coords = sim.sedimenting_init(oc, K, vorticity=w0)
-            step = sim.sedimenting_step
-        else:
-            oc = sim.RigidSphereCase(nz=c.nz, nr=c.nr, dx=c.dx, z_cm=c.z_cm,
-                                     r_sphere=c.r_sphere, U0=c.U0, Re=c.Re, lam=c.lam,
-                                     cfl=c.cfl, kill_width=c.kill_width, ramp=c.ramp,
-                                     noise=c.noise, seed=c.seed)
-            st, coords = sim.rigid_sphere_init(oc, K)
-            step = sim.rigid_sphere_step
-        solver = K.FastDiagonalisationStokesSolver(oc.nr, oc.nz, oc.dx)
-        adv = K.gen_advect_vorticity_via_eno3(oc.dx, oc.nr, oc.nz)
-        runs.append((oc, st, coords, solver, adv, step))
-    cells = 0
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        for oc, st, coords, solver, adv, step in runs:
-            step(oc, st, coords, solver, adv, K)
-            cells += oc.nr * oc.nz
-    dt = time.perf_counter() - t0
-    return cells / dt, dt, cells
+class OracleRuns:
+    """The oracle (numpy FP64, the reference's CPU algorithm) set up for
+    `cases`; one round advances every case one timestep on the host."""
+
+    def __init__(self, cases):
+        from oracle import kernels as K
+        from oracle import simulation as sim
+        self.K = K
+        self.runs = []
+        for c in cases:
+            if c.sediment:
+                oc = sim.SedimentingCase(nz=c.nz, nr=c.nr, dx=c.dx, z_cm=c.z_cm,
+                                         r_sphere=c.r_sphere, rho_f=c.rho_f, rho_s=c.rho_s,
+                                         nu=c.nu, lam=c.lam, cfl=c.cfl,
+                                         kill_width=c.kill_width, gravity=c.gravity)
+                w0 = c.noise * np.random.default_rng(c.seed).standard_normal((c.nr, c.nz))
+                st, coords = sim.sedimenting_init(oc, K, vorticity=w0)
+                step = sim.sedimenting_step
+            else:
+                oc = sim.RigidSphereCase(nz=c.nz, nr=c.nr, dx=c.dx, z_cm=c.z_cm,
+                                         r_sphere=c.r_sphere, U0=c.U0, Re=c.Re, lam=c.lam,
+                                         cfl=c.cfl, kill_width=c.kill_width, ramp=c.ramp,
+                                         noise=c.noise, seed=c.seed)
+                st, coords = sim.rigid_sphere_init(oc, K)
+                step = sim.rigid_sphere_step
+            solver = K.FastDiagonalisationStokesSolver(oc.nr, oc.nz, oc.dx)
+            adv = K.gen_advect_vorticity_via_eno3(oc.dx, oc.nr, oc.nz)
+            self.runs.append((oc, st, coords, solver, adv, step))
+        self.cells = sum(r[0].nr * r[0].nz for r in self.runs)
+
+    def round(self):
+        """One timestep of every case; returns the wall time in seconds."""
+        t0 = time.perf_counter()
+        for oc, st, coords, solver, adv, step in self.runs:
+            step(oc, st, coords, solver, adv, self.K)
+        return time.perf_counter() - t0
+
+
+def cpu_oracle_rate(cases, steps, min_seconds=0.0):
+    """Oracle cell-updates/s on the host for `cases`: `steps` rounds, continued
+    until at least `min_seconds` of stepping have passed."""
+    runs = OracleRuns(cases)
+    secs, rounds = 0.0, 0
+    while rounds < steps or secs < min_seconds:
+        secs += runs.round()
+        rounds += 1
+    return runs.cells * rounds / secs, secs, rounds
 
 
 def run_reference(args, world, rank):
@@ -183,22 +205,27 @@ def run_reference(args, world, rank):
         return
     cases = ensemble_cases(args.workload)
     sample = cases[:4] if len(cases) > 4 else cases
-    from oracle import kernels as K  # noqa: F401  (import cost outside timing)
-    rates = []
+    runs = OracleRuns(sample)
     for _ in range(args.warmup):
-        cpu_oracle_rate(sample, 1)
+        runs.round()
+    # each step: one timestep of every sampled case; at most ~2 minutes of
+    # stepping in total (the remaining steps are not run)
+    times = []
+    budget = 120.0
     for _ in range(args.steps):
-        r, _, _ = cpu_oracle_rate(sample, 1)
-        rates.append(r)
-    value = float(np.median(rates))
+        times.append(runs.round())
+        if sum(times) > budget:
+            break
+    value = runs.cells * len(times) / sum(times)
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     desc = (f"{len(sample)} of the {len(cases)} cases "
             f"({', '.join(f'{c.nz}x{c.nr}' for c in sample)}), 1 timestep each per step, "
-            "numpy FP64 oracle (BLAS threads = all cores, elementwise single-threaded)")
+            f"{len(times)} steps timed, numpy FP64 oracle (BLAS threads = all cores, "
+            "elementwise single-threaded)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": float(1000.0 * sum(c.nr * c.nz for c in sample) / value),
+        "steps": len(times), "warmup": args.warmup,
+        "ms_per_step": float(1000.0 * sum(times) / len(times)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": {"workload": args.workload, "sample": desc},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
@@ -345,7 +372,9 @@ def run_gb300(args, world, rank, local):
                 "peak_source": f"{src} hbm"}
     roof["kernel"] = dom
     roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["traffic"] = None
+    # DRAM bytes (read + write) of one launch of the dominant phase, from the
+    # ncu capture summarised in profiles/ (same workload and kernels)
+    roof["traffic"] = NCU_TRAFFIC.get((args.workload, args.precision, dom))
     stencil_bytes = sum(sum(PHASE_FIELDS.values()) * esize * c.nr * c.nz for c in cases)
     stencil_ms = sum(ph_ms[p] for p in PHASE_FIELDS)
     line = {
@@ -368,16 +397,17 @@ def run_gb300(args, world, rank, local):
         "clocks": clocks.summary(),
         "status_ok": bool(np.all(status == 0)),
     }
-    n_launch = 1 + 4 + 3
+    # kill_reset, 4 spectral products, vel_max, step_dt, penalise, advect_diffuse
+    n_launch = 1 + 4 + 4
     line["gpu_launches"] = n_launch * args.steps
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        sample = cases[:2]
-        rate, secs, _ = cpu_oracle_rate(sample, 2)
+        sample = cases[:4]
+        rate, secs, rounds = cpu_oracle_rate(sample, 2, min_seconds=10.0)
         cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else 1
         line["cpu_baseline"] = {
             "value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"cases {', '.join(f'{c.nz}x{c.nr}' for c in sample)}, 2 timesteps each, "
-                      f"numpy FP64 oracle, {secs:.1f} s"}
+            "sample": f"cases {', '.join(f'{c.nz}x{c.nr}' for c in sample)}, {rounds} timesteps "
+                      f"each, numpy FP64 oracle (BLAS on all cores), {secs:.1f} s"}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -551,7 +581,7 @@ def run_serve(args, world, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ensemble64",

@@ -272,7 +272,7 @@ int axi_tf32x3_gemm(float* C, const float* A, const float* B, int M, int N, int 
  * (kernels/FastDiagonalisationStokesSolver.py:130-156 and
  * FastDiagonalisationPotentialSolver.py:119-145 with real_dtype float32).
  * Operands are K-major row-major float; every basis matrix is given as a
- * TF32 hi part and an FP32 remainder (lo). nr and nz multiples of 4.
+ * TF32 hi part and its TF32-rounded remainder (lo). nr and nz multiples of 4.
  * ------------------------------------------------------------------ */
 typedef struct axi_tc_transform {
   int32_t nr, nz;
@@ -302,8 +302,9 @@ int axi_tc_transform_run(const axi_tc_plan_info* info, const void* plan_dev, voi
 /* Pipeline status of the plan's launches (0 = healthy); synchronises. */
 int axi_tc_transform_status(const axi_tc_plan_info* info, const void* plan_dev, int* tc_error,
                             void* stream);
-/* TF32 split of n values: hi = x with the low 13 mantissa bits cleared,
- * lo = x - hi (from float) or fl32(x - hi) (from double). */
+/* TF32 split of n values: hi = nearest TF32 value of fl32(x), lo = nearest
+ * TF32 value of the remainder x - hi (taken in float, or in double for the
+ * f64 form). */
 int axi_tc_split_f32(float* hi, float* lo, const float* x, int64_t n, void* stream);
 int axi_tc_split_f64(float* hi, float* lo, const double* x, int64_t n, void* stream);
 /* Residual of one refinement step, in FP64: res = rhs - (L psi) / w_i with
@@ -424,7 +425,7 @@ typedef struct axi_case {
   double* history;       /* optional: 2 doubles (dt, Cd) per step, or NULL */
   int64_t history_len;
   /* FP32 engine with the spectral products on the tensor cores (plan flag
-   * AXI_PLAN_TENSOR_CORES): TF32 hi parts and FP32 remainders (lo) of the
+   * AXI_PLAN_TENSOR_CORES): TF32 hi parts and TF32 remainders (lo) of the
    * operands, row-major float. */
   void* omega_hi;        /* (nr, nz), kept in step with omega */
   void* omega_lo;

@@ -2,10 +2,10 @@
 //
 //   C[M, N] = A[M, K] * B[N, K]^T        (both operands K-major, FP32 in HBM)
 //
-// Each operand is stored as a TF32 "hi" part (low 13 mantissa bits cleared)
-// and the exact FP32 remainder "lo"; the tensor core accumulates
-// hi*hi + hi*lo + lo*hi in FP32 in tensor memory, which restores FP32-level
-// accuracy (the dropped lo*lo term is below FP32 rounding).
+// Each operand is stored as a TF32 "hi" part (x rounded to TF32) and the
+// TF32-rounded remainder "lo"; the tensor core accumulates
+// hi*hi + hi*lo + lo*hi in FP32 in tensor memory, which restores close to
+// FP32 accuracy (the dropped lo*lo term is near FP32 rounding).
 //
 // Persistent CTAs (one per SM) walk a list of 128 x 128 output tiles:
 //   warp 0, one thread   TMA producer: cp.async.bulk.tensor tiles (128 rows x
@@ -58,10 +58,19 @@ struct TcJob {
   int mode;
 };
 
-// TF32 split: hi keeps the top 19 bits, lo is the exact remainder.
+// Nearest TF32 value of x (10 explicit mantissa bits, ties away from zero):
+// the tensor core ignores the low 13 bits of an operand, so operands are
+// rounded before they are stored.
+__device__ __forceinline__ float tf32_round(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
+// TF32 split: hi = nearest TF32 of x, lo = nearest TF32 of the exact
+// remainder x - hi. hi + lo carries about 23 significant bits (truncating
+// either part would lose two of them).
 __device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
-  hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
-  lo = x - hi;
+  hi = tf32_round(x);
+  lo = tf32_round(x - hi);
 }
 
 // Host: encode a 2-D K-major FP32 operand (rows x K, row stride ld floats)

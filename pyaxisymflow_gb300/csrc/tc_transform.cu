@@ -25,16 +25,16 @@ __global__ void split_f32_kernel(const float* __restrict__ x, float* __restrict_
   if (k < n) axi_tc::tf32_split(x[k], hi[k], lo[k]);
 }
 
-// hi = TF32(fl32(x)), lo = fl32(x - hi): the split of an FP64 value keeps
-// about 22 significant bits.
+// hi = nearest TF32 of fl32(x), lo = nearest TF32 of fl32(x - hi) (remainder
+// taken in double): the split of an FP64 value keeps about 23 significant bits.
 __global__ void split_f64_kernel(const double* __restrict__ x, float* __restrict__ hi,
                                  float* __restrict__ lo, long long n) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) {
     const double v = x[k];
-    const float h = __uint_as_float(__float_as_uint((float)v) & 0xFFFFE000u);
+    const float h = axi_tc::tf32_round((float)v);
     hi[k] = h;
-    lo[k] = (float)(v - (double)h);
+    lo[k] = axi_tc::tf32_round((float)(v - (double)h));
   }
 }
 

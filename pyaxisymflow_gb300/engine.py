@@ -18,6 +18,7 @@ import torch
 
 from . import _native as N
 from .kernels.FastDiagonalisationStokesSolver import FastDiagonalisationStokesSolver
+from .kernels._spectral import tf32_split
 from .kernels.smooth_Heaviside import smooth_Heaviside
 
 ST_T, ST_DT, ST_CD, ST_STEPS, ST_UMAX, ST_COUNT, ST_STATUS, ST_FORCE = range(8)
@@ -139,15 +140,6 @@ class AxiPlanInfo(ctypes.Structure):
 
 
 PLAN_TENSOR_CORES = 1
-
-
-def tf32_split(x):
-    """TF32 hi part (low 13 mantissa bits of the FP32 value cleared) and the
-    FP32 remainder, from a float64 array."""
-    x32 = np.asarray(x, dtype=np.float32)
-    hi = (x32.view(np.uint32) & np.uint32(0xFFFFE000)).view(np.float32)
-    lo = (np.asarray(x, dtype=np.float64) - hi.astype(np.float64)).astype(np.float32)
-    return hi, lo
 
 
 class _Bases:

@@ -54,12 +54,20 @@ def _row_stride(t, nr, nz, name):
     return t.stride(0)
 
 
+def tf32_round(x32):
+    """Nearest TF32 value (10 explicit mantissa bits, ties away from zero) of a
+    float32 array, as float32."""
+    b = np.ascontiguousarray(x32, dtype=np.float32).view(np.uint32)
+    return ((b + np.uint32(0x1000)) & np.uint32(0xFFFFE000)).view(np.float32)
+
+
 def tf32_split(x):
-    """TF32 hi part (low 13 mantissa bits of fl32(x) cleared) and the FP32
-    remainder fl32(x - hi), from a float64 array."""
-    x32 = np.asarray(x, dtype=np.float32)
-    hi = (x32.view(np.uint32) & np.uint32(0xFFFFE000)).view(np.float32)
-    lo = (np.asarray(x, dtype=np.float64) - hi.astype(np.float64)).astype(np.float32)
+    """Operand pair of the 3xTF32 products from a float64 array: hi = nearest
+    TF32 of fl32(x), lo = nearest TF32 of fl32(x - hi) (remainder in double);
+    hi + lo carries about 23 significant bits."""
+    x64 = np.asarray(x, dtype=np.float64)
+    hi = tf32_round(x64.astype(np.float32))
+    lo = tf32_round((x64 - hi.astype(np.float64)).astype(np.float32))
     return hi, lo
 
 
