@@ -1331,6 +1331,7 @@ extern "C" int axi_plan_upload(const axi_case* cases, const axi_plan_info* info,
         axi::set_error("plan_upload: cases changed since plan_init");
         return AXI_ERR_INVALID;
       }
+      axi_tc::order_tiles_by_k(tt, qq, jobs);
     }
   }
   cudaStream_t s = axi::as_stream(stream);

@@ -1,6 +1,7 @@
 // tcgen05 3xTF32 GEMM: kernel and host helpers (see tc_gemm.cuh).
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -95,7 +96,7 @@ __device__ __forceinline__ void store_value(const TcJob& job, int row, int col, 
 
 // Persistent, warp-specialised kernel (one CTA per SM, tiles strided over the
 // grid): warp 0 issues TMA, warp 1 issues MMAs into one of two TMEM
-// accumulators (2 x 128 columns), warps 2-5 drain the other accumulator, so
+// accumulators (2 x 128 columns), warps 2-9 drain the other accumulator, so
 // the epilogue of a tile overlaps the main loop of the next one.
 __global__ void __launch_bounds__(THREADS, 1)
     tf32x3_gemm_kernel(const TcJob* __restrict__ jobs, const int4* __restrict__ tiles,
@@ -206,8 +207,10 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     __syncwarp();
   } else {
-    // ---- epilogue warps 2..5: TMEM lane quarter = warp % 4 ----
+    // ---- epilogue warps 2..9: TMEM lane quarter = warp % 4, column half ----
     const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
+    constexpr int CHUNKS = BN / 32 / 2;  // 32-column chunks per warp
     float* stg = stage_out + (warp - 2) * 32 * 33;
     int it = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
@@ -220,7 +223,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int row0 = tr.y + 32 * q;
       const bool scaled = job.mode == MODE_SCALE_SPLIT;
 #pragma unroll 1
-      for (int cc = 0; cc < BN / 32; ++cc) {
+      for (int cc = half * CHUNKS; cc < (half + 1) * CHUNKS; ++cc) {
         const int col = tr.z + cc * 32 + lane;
         // the elementwise factors of this 32 x 32 block are fetched before the
         // accumulator is read, all 32 loads in flight at once (one load per
@@ -300,6 +303,11 @@ int encode_operand(CUtensorMap* map, const float* base, int rows, int K, int ld)
     return AXI_ERR_CUDA;
   }
   return AXI_OK;
+}
+
+void order_tiles_by_k(int4* tiles, int n, const TcJob* jobs) {
+  std::stable_sort(tiles, tiles + n,
+                   [jobs](const int4& a, const int4& b) { return jobs[a.x].K > jobs[b.x].K; });
 }
 
 int launch(const TcJob* jobs_dev, const int4* tiles_dev, int n_tiles, int* err_dev,

@@ -15,8 +15,9 @@
 //   warp 1, one thread   MMA issuer: 3 x 4 tcgen05.mma.kind::tf32 per stage into
 //                        one of two 128-lane x 128-column FP32 accumulators in
 //                        TMEM; tcgen05.commit releases stages and accumulators
-//   warps 2-5            epilogue: tcgen05.ld (warp w reads TMEM lanes
-//                        32 (w % 4) ..), a per-warp shared-memory transpose for
+//   warps 2-9            epilogue: tcgen05.ld (warp w reads TMEM lanes
+//                        32 (w % 4) .., warps 2-5 columns 0-63, warps 6-9
+//                        columns 64-127), a per-warp shared-memory transpose for
 //                        row-contiguous stores, and the stage-specific store
 //                        (plain, hi/lo split, or scaled then split); it drains
 //                        one accumulator while the MMAs fill the other
@@ -40,8 +41,8 @@ constexpr int BKF = 32;                         // K floats per stage (128-byte 
 constexpr int NSTAGE = 3;
 constexpr int TILE_BYTES = BM * BKF * 4;        // 16 KB per operand tile
 constexpr int STAGE_BYTES = 4 * TILE_BYTES;     // A_hi, A_lo, B_hi, B_lo
-constexpr int EPI_WARPS = 4;
-constexpr int THREADS = 32 * (2 + EPI_WARPS);   // TMA warp, MMA warp, 4 epilogue warps
+constexpr int EPI_WARPS = 8;                    // two per TMEM lane quarter
+constexpr int THREADS = 32 * (2 + EPI_WARPS);   // TMA warp, MMA warp, 8 epilogue warps
 constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 + 256 + EPI_WARPS * 32 * 33 * 4;
 
 enum { MODE_PLAIN = 0, MODE_SPLIT = 1, MODE_SCALE_SPLIT = 2 };
@@ -76,6 +77,11 @@ __device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
 // Host: encode a 2-D K-major FP32 operand (rows x K, row stride ld floats)
 // for 128-row x 32-float boxes with 128-byte swizzle. Returns AXI status.
 int encode_operand(CUtensorMap* map, const float* base, int rows, int K, int ld);
+
+// Host: order a tile table (job, m0, n0, -) longest main loop (largest K)
+// first, stable within equal K. The persistent CTAs take tiles with a fixed
+// stride, so the long tiles are spread over all SMs before the short ones.
+void order_tiles_by_k(int4* tiles, int n, const TcJob* jobs);
 
 // Host: launch the grouped kernel over `n_tiles` (job, m0, n0) tiles.
 int launch(const TcJob* jobs_dev, const int4* tiles_dev, int n_tiles, int* err_dev,

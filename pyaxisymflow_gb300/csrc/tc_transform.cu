@@ -175,6 +175,7 @@ extern "C" int axi_tc_transform_plan(const axi_tc_transform* t, int n, void* pla
       for (int m0 = 0; m0 < M; m0 += axi_tc::BM)
         for (int n0 = 0; n0 < N; n0 += axi_tc::BN) tt[qq++] = make_int4(4 * q + st, m0, n0, 0);
     }
+    axi_tc::order_tiles_by_k(tt, qq, jobs);
   }
   cudaStream_t s = axi::as_stream(stream);
   if (cudaMemcpyAsync(plan_dev, buf.data(), buf.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
