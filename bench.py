@@ -284,24 +284,22 @@ def run_gb300(args, world, rank, local):
         for k, p in enumerate(PHASES):
             ph_ms[p] += evs[s][k][0].elapsed_time(evs[s][k][1]) / nph
     # ---- end to end through the public API with host buffers ------------------
-    host_w = [torch.empty(c.nr * c.nz, dtype=ens.dtype, pin_memory=True) for c in cases]
-    for k in range(len(cases)):
-        host_w[k].copy_(ens.fields[k]["omega"].reshape(-1))
+    # every case's vorticity in one pinned host buffer laid out like the
+    # engine's device arena
+    host_w = torch.empty(ens.omega_arena.numel(), dtype=ens.dtype, pin_memory=True)
+    host_w.copy_(ens.omega_arena)
     host_state = torch.empty(ens.state.shape, dtype=torch.float64, pin_memory=True)
     torch.cuda.synchronize(dev)
-    field_bytes = sum(h.numel() * h.element_size() for h in host_w)
+    field_bytes = host_w.numel() * host_w.element_size()
     h2d = field_bytes
     d2h = field_bytes + host_state.numel() * 8
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         # host-resident vorticity in, one step, vorticity and (dt, Cd) back out
-        for k in range(len(cases)):
-            ens.fields[k]["omega"].view(-1).copy_(host_w[k], non_blocking=True)
-        ens.refresh_operands()
+        ens.load_vorticity(host_w)
         ens.step(1)
-        for k in range(len(cases)):
-            host_w[k].copy_(ens.fields[k]["omega"].view(-1), non_blocking=True)
+        ens.store_vorticity(host_w)
         host_state.copy_(ens.state, non_blocking=True)
         torch.cuda.synchronize(dev)
         _ = float(host_state[0, ST_CD]) + float(host_state[0, ST_DT])

@@ -306,9 +306,26 @@ class RigidEnsemble:
         self.members.append(m)
         return m
 
+    def _pack_vorticity(self):
+        """Place every member's omega in one contiguous device arena (members
+        in order, each (nr, nz) row-major), so host transfers of all cases'
+        vorticity are one copy each way (omega_arena)."""
+        n = sum(m.case.nr * m.case.nz for m in self.members)
+        arena = torch.empty(max(n, 1), dtype=self.dtype, device=self.device)
+        off = 0
+        for m in self.members:
+            c = m.case
+            view = arena[off:off + c.nr * c.nz].view(c.nr, c.nz)
+            view.copy_(m.fields["omega"])
+            m.fields["omega"] = view
+            m.struct.omega = view.data_ptr()
+            off += c.nr * c.nz
+        self.omega_arena = arena[:n]
+
     def _replan(self):
         self.graph = None
         n = len(self.members)
+        self._pack_vorticity()
         self.structs = (AxiCase * max(n, 1))()
         for k, m in enumerate(self.members):
             self.structs[k] = m.struct
@@ -401,11 +418,12 @@ class RigidEnsemble:
         self.graph.replay()
 
     def status(self):
-        """Sticky status bits per case (0 = healthy); a tensor-core pipeline
-        failure marks every case with bit 1 << AXI_ERR_CUDA."""
+        """Sticky status bits per case (0 = healthy); a failed asynchronous copy
+        (tensor-core products or stencil boxes) marks every case with bit
+        1 << AXI_ERR_CUDA."""
         st = self.state[:, ST_STATUS].cpu().numpy().view(np.uint64)
         out = (st & 0xFFFFFFFF).astype(np.int64)
-        if self.tensor_cores:
+        if self.plan is not None:
             err = ctypes.c_int(0)
             N.check(N.lib().axi_plan_tc_status(
                 ctypes.byref(self.info), ctypes.c_void_p(self.plan.data_ptr()),
@@ -423,6 +441,22 @@ class RigidEnsemble:
             N.check(N.lib().axi_rigid_refresh_operands(
                 ctypes.byref(self.info), ctypes.c_void_p(self.plan.data_ptr()),
                 ctypes.c_void_p(s.cuda_stream)), "rigid_refresh_operands")
+
+    def load_vorticity(self, src, stream=None):
+        """Replace the vorticity of every case from one flat buffer laid out like
+        omega_arena (e.g. pinned host memory): one copy, then the tensor-core
+        operand refresh. Asynchronous on the stream."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(s):
+            self.omega_arena.copy_(src.view(-1), non_blocking=True)
+        self.refresh_operands(stream=s)
+
+    def store_vorticity(self, dst, stream=None):
+        """Copy the vorticity of every case into one flat buffer laid out like
+        omega_arena (one copy; asynchronous on the stream)."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(s):
+            dst.view(-1).copy_(self.omega_arena, non_blocking=True)
 
     def set_vorticity(self, k, w):
         """Replace the vorticity of case k (keeps the tensor-core operand copy in step)."""

@@ -84,6 +84,50 @@ def test_engine_graph_replay_equals_eager():
     assert torch.equal(a.state, b.state)
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_vorticity_arena_host_round_trip(precision):
+    """All cases' vorticity moves in one copy each way (store_vorticity /
+    load_vorticity); loading is equivalent to replacing each case's omega."""
+    from pyaxisymflow_gb300.engine import RigidBodyCase, RigidEnsemble
+    cases = [RigidBodyCase(nz=64, nr=32, dx=2.0 / 64, r_sphere=0.125, seed=1),
+             RigidBodyCase(nz=128, nr=64, dx=2.0 / 128, r_sphere=0.1, seed=2),
+             RigidBodyCase(nz=96, nr=48, dx=2.0 / 96, r_sphere=0.1, seed=3)]
+    a = RigidEnsemble(cases, precision=precision)
+    b = RigidEnsemble(cases, precision=precision)
+    a.step(3)
+    b.step(3)
+    host = torch.empty(a.omega_arena.numel(), dtype=a.dtype, pin_memory=True)
+    a.store_vorticity(host)
+    torch.cuda.synchronize()
+    off = 0
+    for k, c in enumerate(cases):
+        n = c.nr * c.nz
+        assert torch.equal(host[off:off + n].view(c.nr, c.nz), a.fields[k]["omega"].cpu())
+        off += n
+    assert off == host.numel()
+    # perturb on the host, load into a; the same values per case into b
+    host.mul_(1.5)
+    a.load_vorticity(host)
+    off = 0
+    for k, c in enumerate(cases):
+        n = c.nr * c.nz
+        b.set_vorticity(k, host[off:off + n].view(c.nr, c.nz).cuda())
+        off += n
+    a.step(2)
+    b.step(2)
+    torch.cuda.synchronize()
+    for k in range(len(cases)):
+        assert torch.equal(a.fields[k]["omega"], b.fields[k]["omega"]), k
+    assert torch.equal(a.state, b.state)
+    # the arena survives a membership change: case 1 leaves, the others keep
+    # their vorticity
+    keep = [a.fields[0]["omega"].clone(), a.fields[2]["omega"].clone()]
+    a.remove_case(a.members[1])
+    assert a.omega_arena.numel() == sum(c.nr * c.nz for c in (cases[0], cases[2]))
+    assert torch.equal(a.fields[0]["omega"], keep[0])
+    assert torch.equal(a.fields[1]["omega"], keep[1])
+
+
 def test_engine_f32_error_vs_fp64_oracle():
     from pyaxisymflow_gb300.engine import RigidBodyCase, RigidEnsemble
     c = RigidBodyCase(nz=256, nr=128, dx=2.0 / 256, r_sphere=0.0625)
