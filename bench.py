@@ -49,7 +49,8 @@ PHASE_FIELDS = {"vel_max": 1, "penalise": 6, "advect_diffuse": 4}
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of a phase, from the
 # ncu captures summarised in profiles/ (transform: sum over its four products).
 NCU_TRAFFIC = {
-    ("ensemble64", "f32", "transform"): None,
+    # profiles/tf32x3_gemm_ensemble64.md: 265.6 + 251.4 + 264.8 + 194.5 MB
+    ("ensemble64", "f32", "transform"): 976.3e6,
 }
 
 
@@ -373,6 +374,7 @@ def run_gb300(args, world, rank, local):
     # DRAM bytes (read + write) of one launch of the dominant phase, from the
     # ncu capture summarised in profiles/ (same workload and kernels)
     roof["traffic"] = NCU_TRAFFIC.get((args.workload, args.precision, dom))
+    roof["traffic_unit"] = "bytes per launch of the phase"
     stencil_bytes = sum(sum(PHASE_FIELDS.values()) * esize * c.nr * c.nz for c in cases)
     stencil_ms = sum(ph_ms[p] for p in PHASE_FIELDS)
     line = {
