@@ -239,7 +239,7 @@ def run_reference(args, world, rank):
 def run_gb300(args, world, rank, local):
     import torch
     from pyaxisymflow_gb300 import _native
-    from pyaxisymflow_gb300.engine import ST_CD, ST_DT, RigidEnsemble
+    from pyaxisymflow_gb300.engine import ST_CD, ST_DT, ST_WORDS, HostPipeline, RigidEnsemble
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     _native.lib()
@@ -285,24 +285,23 @@ def run_gb300(args, world, rank, local):
         for k, p in enumerate(PHASES):
             ph_ms[p] += evs[s][k][0].elapsed_time(evs[s][k][1]) / nph
     # ---- end to end through the public API with host buffers ------------------
-    # every case's vorticity in one pinned host buffer laid out like the
-    # engine's device arena
-    host_w = torch.empty(ens.omega_arena.numel(), dtype=ens.dtype, pin_memory=True)
-    host_w.copy_(ens.omega_arena)
-    host_state = torch.empty(ens.state.shape, dtype=torch.float64, pin_memory=True)
-    torch.cuda.synchronize(dev)
+    # every case's vorticity in pinned host memory; each step copies it in,
+    # advances every case and copies it and the state blocks (dt, Cd) back,
+    # with the transfers of 4 case groups overlapped with their computation
+    pipe = HostPipeline(cases, groups=4, precision=args.precision, device=dev)
+    host_w = pipe.host_buffer()
+    host_state = torch.empty((len(cases), ST_WORDS), dtype=torch.float64, pin_memory=True)
+    for _ in range(2):
+        pipe.step(host_w, host_state)
+        pipe.synchronize()
     field_bytes = host_w.numel() * host_w.element_size()
     h2d = field_bytes
     d2h = field_bytes + host_state.numel() * 8
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        # host-resident vorticity in, one step, vorticity and (dt, Cd) back out
-        ens.load_vorticity(host_w)
-        ens.step(1)
-        ens.store_vorticity(host_w)
-        host_state.copy_(ens.state, non_blocking=True)
-        torch.cuda.synchronize(dev)
+        pipe.step(host_w, host_state)
+        pipe.synchronize()
         _ = float(host_state[0, ST_CD]) + float(host_state[0, ST_DT])
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_s = max_over_ranks(world, e2e_s)

@@ -202,7 +202,9 @@ class CaseState:
                                  * ((c.nz + TILE_NZ - 1) // TILE_NZ) + 8, **f64),
         )
         if ens.tensor_cores:
-            whi, wlo = tf32_split(w0)
+            # the operand pair describes the stored float32 field, exactly as
+            # the device refresh (axi_rigid_refresh_operands) computes it
+            whi, wlo = tf32_split(np.asarray(w0, dtype=np.float32))
             t["omega_hi"] = torch.tensor(whi, device=dev)
             t["omega_lo"] = torch.tensor(wlo, device=dev)
             t["tc_work"] = [torch.zeros(c.nr * c.nz, dtype=torch.float32, device=dev)
@@ -468,3 +470,72 @@ class RigidEnsemble:
 
     def time(self):
         return self.state[:, ST_T].cpu().numpy()
+
+
+class HostPipeline:
+    """Cases whose vorticity lives in host memory, advanced one step per call
+    with the host transfers overlapped with computation.
+
+    The cases are split into `groups` sub-ensembles of about equal size, each
+    with its own stream. One step() issues, per group: the H2D copy of the
+    group's vorticity (load_vorticity), one step, and the D2H copy back
+    (store_vorticity). Groups run concurrently, so while one group computes
+    the copy engines move the next group's input and the previous group's
+    output. Every case's result is the same as in a single RigidEnsemble.
+    """
+
+    def __init__(self, cases, groups=4, precision="f32", device="cuda", **kw):
+        cases = list(cases)
+        groups = max(1, min(groups, len(cases)))
+        # greedy balance by cells, keeping each group's cases in input order
+        order = sorted(range(len(cases)), key=lambda k: -cases[k].nr * cases[k].nz)
+        load = [0] * groups
+        parts = [[] for _ in range(groups)]
+        for k in order:
+            g = load.index(min(load))
+            parts[g].append(k)
+            load[g] += cases[k].nr * cases[k].nz
+        self.index = [sorted(p) for p in parts if p]
+        self.device = torch.device(device)
+        self.ensembles = [RigidEnsemble([cases[k] for k in idx], precision=precision,
+                                        device=self.device, **kw) for idx in self.index]
+        self.streams = [torch.cuda.Stream(self.device) for _ in self.ensembles]
+        self.dtype = self.ensembles[0].dtype
+        # one flat host buffer: the groups' arenas back to back
+        self.offsets = [0]
+        for e in self.ensembles:
+            self.offsets.append(self.offsets[-1] + e.omega_arena.numel())
+
+    def cells(self):
+        return sum(e.cells() for e in self.ensembles)
+
+    def host_buffer(self):
+        """A pinned host buffer holding every case's vorticity (group arenas
+        back to back), filled with the current device values."""
+        h = torch.empty(self.offsets[-1], dtype=self.dtype, pin_memory=True)
+        for e, a, b in zip(self.ensembles, self.offsets, self.offsets[1:]):
+            h[a:b].copy_(e.omega_arena)
+        return h
+
+    def step(self, host, state_out=None):
+        """One step of every case: host vorticity in, step, host vorticity out.
+        Asynchronous; call synchronize() before reading `host`. state_out
+        (pinned, one row of AXI_ST_WORDS per case, groups in order) receives
+        each case's state block."""
+        cur = torch.cuda.current_stream(self.device)
+        row = 0
+        for e, s, a, b in zip(self.ensembles, self.streams, self.offsets, self.offsets[1:]):
+            s.wait_stream(cur)
+            with torch.cuda.stream(s):
+                e.load_vorticity(host[a:b], stream=s)
+                e.step(1, stream=s)
+                e.store_vorticity(host[a:b], stream=s)
+                if state_out is not None:
+                    n = e.n_cases
+                    state_out[row:row + n].copy_(e.state, non_blocking=True)
+                    row += n
+
+    def synchronize(self):
+        for s in self.streams:
+            s.synchronize()
+

@@ -128,6 +128,35 @@ def test_vorticity_arena_host_round_trip(precision):
     assert torch.equal(a.fields[1]["omega"], keep[1])
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_host_pipeline_matches_single_ensemble(precision):
+    """Overlapped host transfers over case groups give every case the same
+    result as one ensemble round-tripping its vorticity through the host."""
+    from pyaxisymflow_gb300.engine import ST_WORDS, HostPipeline, RigidBodyCase, RigidEnsemble
+    cases = [RigidBodyCase(nz=64 * (1 + k % 3), nr=32 * (1 + k % 3), dx=2.0 / (64 * (1 + k % 3)),
+                           r_sphere=0.125, seed=10 + k) for k in range(7)]
+    pipe = HostPipeline(cases, groups=3, precision=precision)
+    assert sorted(k for idx in pipe.index for k in idx) == list(range(len(cases)))
+    ref = RigidEnsemble(cases, precision=precision)
+    host = pipe.host_buffer()
+    state = torch.empty((len(cases), ST_WORDS), dtype=torch.float64, pin_memory=True)
+    for _ in range(3):
+        pipe.step(host, state)
+        pipe.synchronize()
+    ref.step(3)
+    torch.cuda.synchronize()
+    row = 0
+    for g, idx in enumerate(pipe.index):
+        a = pipe.offsets[g]
+        for k in idx:
+            c = cases[k]
+            n = c.nr * c.nz
+            assert torch.equal(host[a:a + n].view(c.nr, c.nz), ref.fields[k]["omega"].cpu()), k
+            assert torch.equal(state[row], ref.state[k].cpu()), k
+            a += n
+            row += 1
+
+
 def test_engine_f32_error_vs_fp64_oracle():
     from pyaxisymflow_gb300.engine import RigidBodyCase, RigidEnsemble
     c = RigidBodyCase(nz=256, nr=128, dx=2.0 / 256, r_sphere=0.0625)
