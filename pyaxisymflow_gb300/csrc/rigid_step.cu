@@ -617,7 +617,6 @@ __device__ __forceinline__ T sphere_mask(T z, T r, T zc, T radius, T w) {
 // here and close the step (falling_rigid_sphere.py:156-181).
 // ---------------------------------------------------------------------------
 constexpr int AD_H = 4;
-constexpr int AD_LW = BOXW;                      // staged inputs: the TMA boxes
 constexpr int AD_AW = TX + 4, AD_AH = TY + 4;    // advected (halo 2)
 constexpr int AD_SW = TX + 2, AD_SH = TY + 2;    // stage 1 (halo 1)
 template <typename T>
@@ -627,8 +626,48 @@ constexpr int advect_diffuse_smem() {
   return AdRing<T>::BYTES + (int)sizeof(T) * AD_AH * AD_AW + 128;
 }
 
+// Tile-relative indices (row p, column q) into the shared arrays: the staged
+// boxes (rows -4..TY+3, columns -4..TX+3), the advected values wa (rows
+// -2..TY+1, columns -2..TX+1) and the stage-1 values tp (rows -1..TY,
+// columns -1..TX).
+__device__ __forceinline__ int ad_box(int p, int q) { return (p + AD_H) * BOXW + (q + AD_H); }
+__device__ __forceinline__ int ad_wa(int p, int q) { return (p + 2) * AD_AW + (q + 2); }
+__device__ __forceinline__ int ad_tp(int p, int q) { return (p + 1) * AD_SW + (q + 1); }
+// rows per thread of the column march: advection (TY + 4 rows), stage 1
+// (TY + 2 rows, one spare), stage 2 (TY rows), over RG row groups
+constexpr int AD_RA = (TY + 4) / RG, AD_RC = TY / RG;
+static_assert(AD_RA * RG == TY + 4 && AD_RA * RG >= TY + 2 && AD_RC * RG == TY, "row groups");
+static_assert(2 * 32 == TX && NT == 8 * 32, "two warps per row group");
+
+// Advected omega at one point with all four face fluxes evaluated here (the
+// halo columns of the tile).
 template <typename T>
-__global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __restrict__ cases,
+__device__ __forceinline__ T advect_point(const T* sw, const T* sz, const T* sr, int p, int q,
+                                          int gi, int gj, int nr, int nz, T a) {
+  if (!(gi >= 0 && gi < nr && gj >= 0 && gj < nz)) return T(0);
+  const int c = ad_box(p, q);
+  const T f0 = sw[c];
+  T flux = T(0);
+  if (gi < nr - 2 && gj >= 2 && gj < nz - 2) {
+    const int L = BOXW;
+    const T xf = face_flux(sw[c - 1], f0, sw[c + 1], sw[c + 2], sz[c - 1], sz[c], sz[c + 1],
+                           sz[c + 2]);
+    const T xb = face_flux(sw[c - 2], sw[c - 1], f0, sw[c + 1], sz[c - 2], sz[c - 1], sz[c],
+                           sz[c + 1]);
+    const T yf = face_flux(sw[c - L], f0, sw[c + L], sw[c + 2 * L], sr[c - L], sr[c], sr[c + L],
+                           sr[c + 2 * L]);
+    const T yb = face_flux(sw[c - 2 * L], sw[c - L], f0, sw[c + L], sr[c - 2 * L], sr[c - L],
+                           sr[c], sr[c + L]);
+    flux = a * xf;
+    flux = flux - a * xb;
+    flux = flux + a * yf;
+    flux = flux - a * yb;
+  }
+  return f0 + flux;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) advect_diffuse_kernel(const axi_case* __restrict__ cases,
                                                             const int4* __restrict__ tiles,
                                                             int n_tiles,
                                                             const CUtensorMap* __restrict__ maps,
@@ -696,90 +735,149 @@ __global__ void __launch_bounds__(NT) advect_diffuse_kernel(const axi_case* __re
       }
       __syncthreads();
     }
-    // advected omega on the tile + halo 2
-    for (int e = threadIdx.x; e < AD_AH * AD_AW; e += NT) {
-      const int p = e / AD_AW, q = e - p * AD_AW;
-      const int gi = i0 - 2 + p, gj = j0 - 2 + q;
-      T val = T(0);
-      if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
-        const int c = (p + 2) * AD_LW + (q + 2);  // position in the staged boxes
-        const T f0 = sw[c];
-        T flux = T(0);
-        // pystencils ghost layers: no flux in the last two rows and the first
-        // and last two columns
-        if (gi < nr - 2 && gj >= 2 && gj < nz - 2) {
-          const T xf = face_flux(sw[c - 1], f0, sw[c + 1], sw[c + 2], sz[c - 1], sz[c], sz[c + 1],
-                                 sz[c + 2]);
-          const T xb = face_flux(sw[c - 2], sw[c - 1], f0, sw[c + 1], sz[c - 2], sz[c - 1], sz[c],
-                                 sz[c + 1]);
-          const int L = AD_LW;
-          const T yf = face_flux(sw[c - L], f0, sw[c + L], sw[c + 2 * L], sr[c - L], sr[c],
-                                 sr[c + L], sr[c + 2 * L]);
-          const T yb = face_flux(sw[c - 2 * L], sw[c - L], f0, sw[c + L], sr[c - 2 * L],
-                                 sr[c - L], sr[c], sr[c + L]);
-          flux = a * xf;
-          flux = flux - a * xb;
-          flux = flux + a * yf;
-          flux = flux - a * yb;
+    // Work split of the three passes: warp w owns tile columns
+    // 32 (w % 2) .. 32 (w % 2) + 31 and a run of consecutive rows starting at
+    // (w / 2) x (rows per group), so each thread marches down one column and
+    // keeps the values of the rows above and below it in registers; the
+    // halo columns left and right of the tile are separate small loops.
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int qm = (warp & 1) * 32 + lane;  // tile column of the column march
+    const int grp = warp >> 1;              // row group 0..3
+    const int gjm = j0 + qm;
+    constexpr int L = BOXW;
+    // ---- advected omega on the tile + halo 2: rows -2..TY+1, columns -2..TX+1
+    {
+      const bool jin = gjm < nz, jflux = gjm >= 2 && gjm < nz - 2;
+      const int p0 = -2 + AD_RA * grp;
+      int c = ad_box(p0, qm);
+      // r-direction face fluxes: yb of row p is yf of row p - 1
+      T fm2 = sw[c - 2 * L], fm1 = sw[c - L], f0 = sw[c], f1 = sw[c + L];
+      T um2 = sr[c - 2 * L], um1 = sr[c - L], u0 = sr[c], u1 = sr[c + L];
+      T yb = face_flux(fm2, fm1, f0, f1, um2, um1, u0, u1);
+#pragma unroll 1
+      for (int m = 0; m < AD_RA; ++m, c += L) {
+        const int pr = p0 + m, gi = i0 + pr;
+        const T f2 = sw[c + 2 * L], u2 = sr[c + 2 * L];
+        const T yf = face_flux(fm1, f0, f1, f2, um1, u0, u1, u2);
+        T val = T(0);
+        if (jin && gi >= 0 && gi < nr) {
+          T flux = T(0);
+          // pystencils ghost layers: no flux in the last two rows and the
+          // first and last two columns
+          if (jflux && gi < nr - 2) {
+            const T xf = face_flux(sw[c - 1], f0, sw[c + 1], sw[c + 2], sz[c - 1], sz[c],
+                                   sz[c + 1], sz[c + 2]);
+            const T xb = face_flux(sw[c - 2], sw[c - 1], f0, sw[c + 1], sz[c - 2], sz[c - 1],
+                                   sz[c], sz[c + 1]);
+            flux = a * xf;
+            flux = flux - a * xb;
+            flux = flux + a * yf;
+            flux = flux - a * yb;
+          }
+          val = f0 + flux;
         }
-        val = f0 + flux;
+        wa[ad_wa(pr, qm)] = val;
+        yb = yf;
+        fm2 = fm1;
+        fm1 = f0;
+        f0 = f1;
+        f1 = f2;
+        um2 = um1;
+        um1 = u0;
+        u0 = u1;
+        u1 = u2;
       }
-      wa[e] = val;
+      // halo columns -2, -1, TX, TX + 1
+      if (threadIdx.x < 4 * AD_AH) {
+        const int pr = -2 + (int)threadIdx.x / 4, s4 = threadIdx.x % 4;
+        const int qe = s4 < 2 ? s4 - 2 : TX + s4 - 2;
+        wa[ad_wa(pr, qe)] = advect_point<T>(sw, sz, sr, pr, qe, i0 + pr, j0 + qe, nr, nz, a);
+      }
     }
     __syncthreads();
-    // RK2 stage 1 on the tile + halo 1
-    for (int e = threadIdx.x; e < AD_SH * AD_SW; e += NT) {
-      const int p = e / AD_SW, q = e - p * AD_SW;
-      const int gi = i0 - 1 + p, gj = j0 - 1 + q;
-      T tmp = T(0);
-      if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
-        const int c = (p + 1) * AD_AW + (q + 1);
-        const T c0 = wa[c];
-        tmp = c0;
-        if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
-          const T n = wa[c + AD_AW], s = wa[c - AD_AW], ee = wa[c + 1], ww = wa[c - 1];
-          const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rowf[0][p] -
-                        c0 * rowf[1][p];
-          tmp = c0 + c1 * lap;
+    // ---- RK2 stage 1 on the tile + halo 1: rows -1..TY, columns -1..TX
+    {
+      const bool jin = gjm < nz, jint = gjm >= 1 && gjm < nz - 1;
+      const int p0 = -1 + AD_RA * grp;
+      int d = ad_wa(p0, qm);
+      T s_ = wa[d - AD_AW], c_ = wa[d];
+#pragma unroll
+      for (int m = 0; m < AD_RA; ++m, d += AD_AW) {
+        const int pr = p0 + m;
+        if (pr > TY) break;
+        const T n_ = wa[d + AD_AW];
+        const int gi = i0 + pr;
+        T tmpv = T(0);
+        if (jin && gi >= 0 && gi < nr) {
+          tmpv = c_;
+          if (jint && gi >= 1 && gi < nr - 1) {
+            const T ee = wa[d + 1], ww = wa[d - 1];
+            const T lap = (n_ + s_ + ee + ww - T(4) * c_) * inv_dx2 +
+                          (n_ - s_) * rowf[0][pr + 1] - c_ * rowf[1][pr + 1];
+            tmpv = c_ + c1 * lap;
+          }
         }
+        tp[ad_tp(pr, qm)] = tmpv;
+        s_ = c_;
+        c_ = n_;
       }
-      tp[e] = tmp;
+      // halo columns -1 and TX
+      if (threadIdx.x < 2 * AD_SH) {
+        const int pr = -1 + (int)threadIdx.x / 2, qe = (threadIdx.x & 1) ? TX : -1;
+        const int gi = i0 + pr, gj = j0 + qe;
+        T tmpv = T(0);
+        if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
+          const int e = ad_wa(pr, qe);
+          const T c0 = wa[e];
+          tmpv = c0;
+          if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
+            const T n = wa[e + AD_AW], s = wa[e - AD_AW], ee = wa[e + 1], ww = wa[e - 1];
+            const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rowf[0][pr + 1] -
+                          c0 * rowf[1][pr + 1];
+            tmpv = c0 + c1 * lap;
+          }
+        }
+        tp[ad_tp(pr, qe)] = tmpv;
+      }
     }
     __syncthreads();
-    // RK2 stage 2 on the tile
+    // ---- RK2 stage 2 on the tile (rows 0..TY-1, columns 0..TX-1)
     const bool sediment = (k.flags & AXI_CASE_SEDIMENTING) != 0;
     T cd_part = T(0);
     {
       const T zc = scalar<T>(k, SF_ZCM);
       const T rbody = scalar<T>(k, SF_RBODY);
       const T blendw = scalar<T>(k, SF_BLENDW);
-      const int gjt = j0 + threadIdx.x % TX;
-      const T zcol = (sediment && gjt < nz) ? CF<T>(k.zw)[gjt] : T(0);
+      const T zcol = (sediment && gjm < nz) ? CF<T>(k.zw)[gjm] : T(0);
+      const bool jin = gjm < nz, jint = gjm >= 1 && gjm < nz - 1;
+      const int p0 = AD_RC * grp;
+      int d = ad_tp(p0, qm);
+      T s_ = tp[d - AD_SW], c_ = tp[d];
 #pragma unroll
-      for (int qq = 0; qq < CPT; ++qq) {
-        const int p = threadIdx.x / TX + RG * qq, q = threadIdx.x % TX;
-        const int gi = i0 + p, gj = j0 + q;
-        if (gi < nr && gj < nz) {
-          const int c = gi * nz + gj;
-          T v = wa[(p + 2) * AD_AW + (q + 2)];
-          if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
-            const int d = (p + 1) * AD_SW + (q + 1);
-            const T c0 = tp[d], n = tp[d + AD_SW], s = tp[d - AD_SW], ee = tp[d + 1],
-                    ww = tp[d - 1];
-            const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rowf[0][p + 1] -
-                          c0 * rowf[1][p + 1];
+      for (int m = 0; m < AD_RC; ++m, d += AD_SW) {
+        const int pr = p0 + m, gi = i0 + pr;
+        const T n_ = tp[d + AD_SW];
+        if (jin && gi < nr) {
+          const int c = gi * nz + gjm;
+          T v = wa[ad_wa(pr, qm)];
+          if (jint && gi >= 1 && gi < nr - 1) {
+            const T ee = tp[d + 1], ww = tp[d - 1];
+            const T lap = (n_ + s_ + ee + ww - T(4) * c_) * inv_dx2 +
+                          (n_ - s_) * rowf[0][pr + 1] - c_ * rowf[1][pr + 1];
             v = v + c2 * lap;
           }
           store_omega<T>(k, c, v);
           if (sediment) {
             // mask at the body position of this step (falling_rigid_sphere.py:156-157),
             // then the drag integrand with the new mask (:164-173)
-            const T rr = rowf[2][p + 1];
+            const T rr = rowf[2][pr + 1];
             const T ch = sphere_mask<T>(zcol, rr, zc, rbody, blendw);
             F<T>(k.chi)[c] = ch;
-            cd_part += rr * ch * sz[(p + AD_H) * AD_LW + (q + AD_H)];
+            cd_part += rr * ch * sz[ad_box(pr, qm)];
           }
         }
+        s_ = c_;
+        c_ = n_;
       }
     }
     if (sediment) {
