@@ -257,8 +257,15 @@ struct BoxRing {
       axi_tma::tma_load_2d(axi_tma::smem_u32(box(slot, q)), maps + MAP_COUNT * tr.x + which[q],
                            tr.z - 4, tr.y + row0, bar);
   }
-  __device__ bool wait(int it, int* err) const {
-    return axi_tma::mbar_wait(bar0 + 8 * (it % NBUF), (it / NBUF) & 1, err, ERR_STENCIL_WAIT);
+  // Block-wide: thread 0 waits (bounded) for the boxes of iteration `it`,
+  // the other threads wait at the barrier (no issue slots spent polling);
+  // false on failure, for every thread.
+  __device__ bool wait_all(int it, int* err) const {
+    int failed = 0;
+    if (threadIdx.x == 0)
+      failed = !axi_tma::mbar_wait(bar0 + 8 * (it % NBUF), (it / NBUF) & 1, err,
+                                   ERR_STENCIL_WAIT);
+    return !__syncthreads_or(failed);
   }
   // thread 0, after a failure: wait (bounded) for the copies still in flight
   __device__ void drain(int consumed, int issued, int* err) const {
@@ -341,7 +348,7 @@ __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict_
     const int nr = k.nr, nz = k.nz;
     const T* __restrict__ rinv2dx = CF<T>(k.rinv2dx);
     const T ufree = scalar<T>(k, SF_UFREE);
-    if (!__syncthreads_and(ring.wait(it, err))) {
+    if (!ring.wait_all(it, err)) {
       ok = false;
       break;
     }
@@ -491,7 +498,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 2) penalise_kernel(co
       rowf[0][threadIdx.x] = rinv2dx[gi];
       rowf[1][threadIdx.x] = rw[gi];
     }
-    if (!__syncthreads_and(ring.wait(it, err))) {
+    if (!ring.wait_all(it, err)) {
       ok = false;
       break;
     }
@@ -711,7 +718,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) advect_diffuse_ker
       rowf[1][threadIdx.x] = rinv2[gi];
       rowf[2][threadIdx.x] = CF<T>(k.rw)[gi];
     }
-    if (!__syncthreads_and(ring.wait(it, err))) {
+    if (!ring.wait_all(it, err)) {
       ok = false;
       break;
     }

@@ -55,15 +55,17 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
       : "memory");
 }
 
-// Shared-memory matrix descriptor of a K-major tile with 128-byte rows and the
-// 128-byte swizzle (8-row atoms of 1024 bytes, atoms 1024 bytes apart).
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+// Shared-memory matrix descriptor of a K-major tile with ROW_BYTES-wide rows
+// and the matching swizzle (8-row atoms of 8 x ROW_BYTES bytes, consecutive
+// atoms 8 x ROW_BYTES apart); layout codes 2 = 128-byte, 4 = 64-byte swizzle.
+static_assert(ROW_BYTES == 64 || ROW_BYTES == 128, "tile rows must be 64 or 128 bytes");
+__device__ __forceinline__ uint64_t sw_desc(uint32_t saddr) {
   uint64_t d = 0;
-  d |= static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);  // start address >> 4
-  d |= static_cast<uint64_t>(1) << 16;                   // leading byte offset (unused here)
-  d |= static_cast<uint64_t>(1024 >> 4) << 32;           // stride byte offset: 8 rows x 128 B
-  d |= static_cast<uint64_t>(1) << 46;                   // descriptor version
-  d |= static_cast<uint64_t>(2) << 61;                   // swizzle: 128 B
+  d |= static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);        // start address >> 4
+  d |= static_cast<uint64_t>(1) << 16;                         // leading byte offset (unused)
+  d |= static_cast<uint64_t>((8 * ROW_BYTES) >> 4) << 32;      // stride byte offset: 8 rows
+  d |= static_cast<uint64_t>(1) << 46;                         // descriptor version
+  d |= static_cast<uint64_t>(ROW_BYTES == 128 ? 2 : 4) << 61;  // swizzle mode
   return d;
 }
 
@@ -186,9 +188,8 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
           tc_fence_after();
           const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
-          const uint64_t ah = sw128_desc(st), al = sw128_desc(st + TILE_BYTES);
-          const uint64_t bh = sw128_desc(st + 2 * TILE_BYTES),
-                         bl = sw128_desc(st + 3 * TILE_BYTES);
+          const uint64_t ah = sw_desc(st), al = sw_desc(st + TILE_BYTES);
+          const uint64_t bh = sw_desc(st + 2 * TILE_BYTES), bl = sw_desc(st + 3 * TILE_BYTES);
 #pragma unroll
           for (int kk = 0; kk < BKF / 8; ++kk) {
             const uint64_t o = static_cast<uint64_t>(kk * 32) >> 4;  // 8 TF32 = 32 bytes
@@ -296,7 +297,8 @@ int encode_operand(CUtensorMap* map, const float* base, int rows, int K, int ld)
   const cuuint32_t box[2] = {BKF, BM};
   const cuuint32_t estr[2] = {1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides,
-                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  ROW_BYTES == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     axi::set_error("tensor core GEMM: cuTensorMapEncodeTiled failed (%d)", static_cast<int>(r));

@@ -37,7 +37,12 @@ namespace axi_tc {
 
 constexpr int BM = 128;
 constexpr int BN = 128;
-constexpr int BKF = 32;                         // K floats per stage (128-byte rows)
+// 32 K floats (128-byte rows, 128-byte swizzle) per stage and 3 stages:
+// measured faster than 16-float stages with a 6-deep ring (64-byte swizzle),
+// whose doubled barrier and copy count per FLOP cost more than the deeper
+// ring saved.
+constexpr int BKF = 32;                         // K floats per stage
+constexpr int ROW_BYTES = BKF * 4;              // swizzle span of a tile row
 constexpr int NSTAGE = 3;
 constexpr int TILE_BYTES = BM * BKF * 4;        // 16 KB per operand tile
 constexpr int STAGE_BYTES = 4 * TILE_BYTES;     // A_hi, A_lo, B_hi, B_lo
@@ -75,7 +80,7 @@ __device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
 }
 
 // Host: encode a 2-D K-major FP32 operand (rows x K, row stride ld floats)
-// for 128-row x 32-float boxes with 128-byte swizzle. Returns AXI status.
+// for 128-row x BKF-float boxes with the ROW_BYTES swizzle. Returns AXI status.
 int encode_operand(CUtensorMap* map, const float* base, int rows, int K, int ld);
 
 // Host: order a tile table (job, m0, n0, -) longest main loop (largest K)
