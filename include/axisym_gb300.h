@@ -227,6 +227,37 @@ int axi_extrapolate_lsq_first_order_f64(int16_t* current_flag, const int16_t* ta
                                         double* eta_x, double* eta_y, const double* grid_x,
                                         const double* grid_y, int n0, int n1, int max_sweeps,
                                         void* work, int* sweeps_out, void* stream);
+/* ------------------------------------------------------------------
+ * Particle remeshing (kernels/advect_particle.py:5-68)
+ *
+ * axi_particles_to_mesh_2d_mp4_f64 replaces the compiled
+ * pyaxisymflow.core.particles_to_mesh functions particles_to_mesh_2D_mp4
+ * (periodic = 1, core/src/particles_to_mesh.hpp:69-91) and
+ * particles_to_mesh_2D_unbounded_mp4 (periodic = 0, :163-184): the MP4
+ * interpolation of particle values (n0, n1) onto the cell-centred (n0, n1)
+ * mesh of spacing dx, dy, bit-identical to the reference's sequential sum.
+ * Particle (j, i) must lie less than one cell from mesh point (j, i) along
+ * each axis (the reference's remeshing resets particles to the mesh each
+ * step); otherwise the output is invalid and axi_p2m_status reports it.
+ * `work` is device scratch of axi_p2m_mp4_work_bytes(n0, n1) bytes; both
+ * sides 5 .. 65535.
+ * ------------------------------------------------------------------ */
+int64_t axi_p2m_mp4_work_bytes(int n0, int n1);
+int axi_particles_to_mesh_2d_mp4_f64(const double* particle_positions_x,
+                                     const double* particle_positions_y,
+                                     const double* input_field_at_particle_positions,
+                                     double* output_field_at_mesh, int n0, int n1, double dx,
+                                     double dy, int periodic, void* work, void* stream);
+/* *displaced (host) = 1 when the last interpolation using `work` met a
+ * particle a cell or more from its mesh point (result invalid). Synchronises. */
+int axi_p2m_status(const void* work, int n0, int n1, int* displaced, void* stream);
+/* kernels/advect_particle.py:20-28: particles on the mirrored (2 nr, nz)
+ * domain move by u dt (rows below the axis: u_z even, u_r odd) and take the
+ * vorticity (rows below the axis odd). u_z, u_r, vorticity are (nr, nz). */
+int axi_advect_particles_prepare_f64(double* z_particles, double* r_particles,
+                                     double* vort_particles, const double* vorticity,
+                                     const double* u_z, const double* u_r, int nr, int nz,
+                                     double dt, void* stream);
 /* elasto_kernels/extrapolate_eta_using_least_squares_unb.py:7-30 with
  * elasto_kernels/extrapolate_using_least_squares.py:33-38 folded in: builds the
  * axis-mirrored (2*nr, nz) level set, masked eta and flags (phi < 0, phi <

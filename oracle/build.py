@@ -2,7 +2,10 @@
 
 * oracle/_ref/libref_lsq.so: the reference's own least-squares core compiled
   from its sources in place (core/src/extrapolate_using_least_squares.hpp)
-  through oracle/ref_shim.cpp. Built only where the reference sources exist.
+  through oracle/ref_shim.cpp.
+* oracle/_ref/libref_p2m.so: the reference's particle-to-mesh interpolation
+  (core/src/particles_to_mesh.hpp) through oracle/ref_p2m_shim.cpp.
+Built only where the reference sources exist; never shipped.
 """
 import os
 import subprocess
@@ -16,23 +19,35 @@ def ref_lsq_path():
     return os.path.join(REF_DIR, "libref_lsq.so")
 
 
-def build_ref():
+def ref_p2m_path():
+    return os.path.join(REF_DIR, "libref_p2m.so")
+
+
+def _build_shim(shim_name, out):
     src_dir = os.path.join(REF_ROOT, "pyaxisymflow", "core", "src")
     if not os.path.isdir(src_dir):
         return None
     os.makedirs(REF_DIR, exist_ok=True)
-    out = ref_lsq_path()
-    shim = os.path.join(HERE, "ref_shim.cpp")
+    shim = os.path.join(HERE, shim_name)
     if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(shim):
         return out
+    # no FMA contraction: the reference's expressions evaluated as written
     cmd = ["g++", "-O2", "-std=c++14", "-fPIC", "-shared", "-ffp-contract=off", "-I", src_dir,
            "-o", out, shim]
     subprocess.run(cmd, check=True)
     return out
 
 
+def build_ref():
+    return _build_shim("ref_shim.cpp", ref_lsq_path())
+
+
+def build_ref_p2m():
+    return _build_shim("ref_p2m_shim.cpp", ref_p2m_path())
+
+
 def build_all():
-    return {"ref_lsq": build_ref()}
+    return {"ref_lsq": build_ref(), "ref_p2m": build_ref_p2m()}
 
 
 if __name__ == "__main__":

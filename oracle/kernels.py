@@ -684,3 +684,117 @@ def extrapolate_eta_with_least_squares(inside_solid, ball_phi, eta1, eta2,
     )
     eta1[...] = eta1_double[grid_size_r:, :]
     eta2[...] = eta2_double[grid_size_r:, :]
+
+
+# --------------------------------------------------------------------------
+# Particle remeshing (remeshed vortex method): P2M with the MP4 kernel
+# --------------------------------------------------------------------------
+
+def _mp4_inner(t):
+    """MP4 for |x| <= 1 (core/src/particle_kernels/MP4.hpp, _f<0>)."""
+    return 1.0 + t * t * (-2.5 + 1.5 * t)
+
+
+def _mp4_outer(t):
+    """MP4 for 1 < |x| <= 2 (core/src/particle_kernels/MP4.hpp, _f<1>)."""
+    return 2.0 + t * (-4.0 + t * (2.5 - 0.5 * t))
+
+
+def _mp4_stencil(pos):
+    """Stencil anchor and the four weights per particle along one axis
+    (core/src/interpolation/particles_to_mesh_2D.hpp:60-118): the anchor is
+    the mesh index nearest above the particle on the cell-centred mesh; slot
+    k (offset k - 2) has scaled distance |pos - ((h + 0.5) + (k - 2))| and
+    weight _f<1> for the outer slots 0 and 3, _f<0> for the inner slots 1 and
+    2 (core/src/particle_kernels/KernelWrapper.hpp:31-47)."""
+    fl = np.floor(pos)
+    h = (pos >= fl + 0.5).astype(np.int64) + fl.astype(np.int64)
+    hd = h.astype(np.float64)
+    w = np.empty(pos.shape + (4,))
+    for k in range(4):
+        d = np.fabs(pos - ((hd + 0.5) + float(k - 2)))
+        w[..., k] = _mp4_outer(d) if k in (0, 3) else _mp4_inner(d)
+    return h, w
+
+
+def _particles_to_mesh_mp4(px, py, vin, out, dx, dy, periodic):
+    n0, n1 = out.shape
+    pos_x = np.asarray(px, dtype=np.float64) / dx
+    pos_y = np.asarray(py, dtype=np.float64) / dy
+    hx, wx = _mp4_stencil(pos_x.reshape(-1))
+    hy, wy = _mp4_stencil(pos_y.reshape(-1))
+    inp = np.asarray(vin, dtype=np.float64).reshape(-1)
+    s = np.arange(-2, 2)
+    # (particle, sy, sx) in the reference's loop order
+    my = hy[:, None, None] + s[None, :, None]
+    mx = hx[:, None, None] + s[None, None, :]
+    weight = wy[:, :, None] * wx[:, None, :]
+    val = weight * inp[:, None, None]
+    if periodic:
+        # (h + s + n) % n (particles_to_mesh_2D.hpp:122-137); C's % truncates
+        ry, rx = my + n0, mx + n1
+        if ry.min() < 0 or rx.min() < 0:
+            raise ValueError("particle too far outside the periodic domain")
+        idx = (rx % n1) + n1 * (ry % n0)
+        valid = np.ones(idx.shape, dtype=bool)
+    else:
+        # one-sided near the edges: mesh points outside the grid are skipped
+        # (particles_to_mesh_2D.hpp:266-318)
+        valid = (my >= 0) & (my < n0) & (mx >= 0) & (mx < n1)
+        idx = np.where(valid, mx + n1 * my, 0)
+    flat = np.zeros(n0 * n1)
+    np.add.at(flat, idx[valid], val[valid])
+    out[...] = flat.reshape(n0, n1)
+
+
+def particles_to_mesh_2D_mp4(particle_positions_x, particle_positions_y,
+                             input_field_at_particle_positions, output_field_at_mesh,
+                             delta_x, delta_y):
+    """core/src/particles_to_mesh.hpp:69-91 (periodic in both directions,
+    core/src/interpolation/particles_to_mesh_2D.hpp:14-143)."""
+    _particles_to_mesh_mp4(particle_positions_x, particle_positions_y,
+                           input_field_at_particle_positions, output_field_at_mesh,
+                           delta_x, delta_y, periodic=True)
+
+
+def particles_to_mesh_2D_unbounded_mp4(particle_positions_x, particle_positions_y,
+                                       input_field_at_particle_positions,
+                                       output_field_at_mesh, delta_x, delta_y):
+    """core/src/particles_to_mesh.hpp:163-184 (unbounded,
+    core/src/interpolation/particles_to_mesh_2D.hpp:152-324)."""
+    _particles_to_mesh_mp4(particle_positions_x, particle_positions_y,
+                           input_field_at_particle_positions, output_field_at_mesh,
+                           delta_x, delta_y, periodic=False)
+
+
+def _advect_vorticity_via_particles(z_particles, r_particles, vort_particles, vorticity,
+                                    Z_double, R_double, grid_size_r, u_z, u_r, dx, dt,
+                                    p2m):
+    z_particles[grid_size_r:, :] += u_z * dt
+    z_particles[:grid_size_r, :] += np.flip(u_z, axis=0) * dt
+    r_particles[grid_size_r:, :] += u_r * dt
+    r_particles[:grid_size_r, :] += -np.flip(u_r, axis=0) * dt
+    vort_particles[grid_size_r:, :] = vorticity
+    vort_particles[:grid_size_r, :] = -np.flip(vorticity, axis=0)
+    vort_double = 0 * Z_double
+    p2m(z_particles, r_particles, vort_particles, vort_double, dx, dx)
+    z_particles[...] = Z_double
+    r_particles[...] = R_double
+    vorticity[...] = vort_double[grid_size_r:, :]
+
+
+def advect_vorticity_via_particles(z_particles, r_particles, vort_particles, vorticity,
+                                   Z_double, R_double, grid_size_r, u_z, u_r, dx, dt):
+    """kernels/advect_particle.py:5-35."""
+    _advect_vorticity_via_particles(z_particles, r_particles, vort_particles, vorticity,
+                                    Z_double, R_double, grid_size_r, u_z, u_r, dx, dt,
+                                    particles_to_mesh_2D_unbounded_mp4)
+
+
+def advect_vorticity_via_particles_periodic(z_particles, r_particles, vort_particles,
+                                            vorticity, Z_double, R_double, grid_size_r, u_z,
+                                            u_r, dx, dt):
+    """kernels/advect_particle.py:38-68."""
+    _advect_vorticity_via_particles(z_particles, r_particles, vort_particles, vorticity,
+                                    Z_double, R_double, grid_size_r, u_z, u_r, dx, dt,
+                                    particles_to_mesh_2D_mp4)

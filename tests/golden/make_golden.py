@@ -14,8 +14,10 @@ What runs unmodified from the reference:
     what the numpy the reference pins (^1.20) did; with numpy >= 2 the
     implicit diffusion stepper cannot write its complex result into a float
     field otherwise;
-  * the C++ least-squares extrapolator, compiled from the reference header by
-    ``oracle/build.py`` (``oracle/_ref/libref_lsq.so``).
+  * the C++ least-squares extrapolator and particle-to-mesh interpolation,
+    compiled from the reference headers by ``oracle/build.py``
+    (``oracle/_ref/libref_lsq.so``, ``oracle/_ref/libref_p2m.so``), and
+    ``kernels/advect_particle.py`` over the latter.
 
 What cannot run: the pystencils ENO3 kernels (pystencils is not installed).
 Full-step vectors therefore use the oracle's ENO3 restatement for the
@@ -381,6 +383,80 @@ def soft_vectors(ref):
     return out
 
 
+def _ref_p2m_module():
+    """A stand-in for the compiled module pyaxisymflow.core.particles_to_mesh
+    whose 2-D MP4 functions call the reference's own C++
+    (oracle/_ref/libref_p2m.so, built from core/src/particles_to_mesh.hpp)."""
+    lib = ctypes.CDLL(os.path.join(REPO, "oracle", "_ref", "libref_p2m.so"))
+    P = ctypes.c_void_p
+    for f in (lib.ref_p2m_2d_mp4, lib.ref_p2m_2d_unbounded_mp4):
+        f.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+
+    def wrap(fn):
+        def call(x, y, vin, out, dx, dy):
+            arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, vin)]
+            assert out.flags.c_contiguous and out.dtype == np.float64
+            fn(arrs[0].ctypes.data, arrs[1].ctypes.data, arrs[2].ctypes.data, out.ctypes.data,
+               out.shape[0], out.shape[1], dx, dy)
+        return call
+
+    mod = types.ModuleType("pyaxisymflow.core.particles_to_mesh")
+    mod.particles_to_mesh_2D_mp4 = wrap(lib.ref_p2m_2d_mp4)
+    mod.particles_to_mesh_2D_unbounded_mp4 = wrap(lib.ref_p2m_2d_unbounded_mp4)
+    return mod
+
+
+def p2m_vectors():
+    """Particle-to-mesh (MP4) and vorticity advection by remeshed particles,
+    computed by the reference: the C++ interpolation compiled from its header
+    and kernels/advect_particle.py run unmodified over it."""
+    mod = _ref_p2m_module()
+    sys.modules["pyaxisymflow.core.particles_to_mesh"] = mod
+    import pyaxisymflow.core
+    pyaxisymflow.core.particles_to_mesh = mod
+    from pyaxisymflow.kernels import advect_particle as ap
+    rng = np.random.default_rng(11)
+    out = {}
+    # (tag, n0, n1, dx, displacement in cells; None = anywhere in the domain)
+    for tag, n0, n1, dx, disp in (("a", 16, 24, 0.1, 0.95), ("b", 64, 48, 1.0 / 64, 0.3),
+                                  ("c", 40, 40, 0.05, None)):
+        Z, R = np.meshgrid((np.arange(n1) + 0.5) * dx, (np.arange(n0) + 0.5) * dx)
+        if disp is None:
+            px = rng.uniform(0.0, n1 * dx, Z.shape)
+            py = rng.uniform(0.0, n0 * dx, Z.shape)
+        else:
+            px = Z + disp * dx * rng.uniform(-1.0, 1.0, Z.shape)
+            py = R + disp * dx * rng.uniform(-1.0, 1.0, Z.shape)
+        v = rng.standard_normal(Z.shape)
+        out[f"{tag}/px"], out[f"{tag}/py"], out[f"{tag}/v"] = px, py, v
+        out[f"{tag}/dx"] = np.array(dx)
+        for name, fn in (("periodic", mod.particles_to_mesh_2D_mp4),
+                         ("unbounded", mod.particles_to_mesh_2D_unbounded_mp4)):
+            o = np.zeros((n0, n1))
+            fn(px, py, v, o, dx, dx)
+            out[f"{tag}/{name}"] = o
+    # two steps of each advection function on a (2 nr, nz) mirrored domain
+    nr, nz = 24, 32
+    dx = 1.0 / nz
+    z = (np.arange(nz) + 0.5) * dx
+    r2 = (np.arange(2 * nr) + 0.5) * dx
+    Zd, Rd = np.meshgrid(z, r2)
+    w0 = rng.standard_normal((nr, nz))
+    uz = rng.uniform(-1.0, 1.0, (nr, nz))
+    ur = rng.uniform(-1.0, 1.0, (nr, nz))
+    dt = 0.5 * dx
+    out["adv/w0"], out["adv/u_z"], out["adv/u_r"] = w0, uz, ur
+    out["adv/dx"], out["adv/dt"], out["adv/nr"] = np.array(dx), np.array(dt), np.array(nr)
+    for name, fn in (("unbounded", ap.advect_vorticity_via_particles),
+                     ("periodic", ap.advect_vorticity_via_particles_periodic)):
+        w = w0.copy()
+        zp, rp, vp = Zd.copy(), Rd.copy(), np.zeros_like(Zd)
+        for _ in range(2):
+            fn(zp, rp, vp, w, Zd, Rd, nr, uz, ur, dx, dt)
+        out[f"adv/{name}"] = w
+    return out
+
+
 def main(ref_root):
     _install_reference(ref_root)
     ref = _ref_kernels()
@@ -388,10 +464,18 @@ def main(ref_root):
     np.savez_compressed(os.path.join(HERE, "kernels.npz"), **kernel_vectors(ref))
     np.savez_compressed(os.path.join(HERE, "solvers.npz"), **solver_vectors(ref))
     np.savez_compressed(os.path.join(HERE, "lsq.npz"), **lsq_vectors(extrap_first_order))
+    np.savez_compressed(os.path.join(HERE, "p2m.npz"), **p2m_vectors())
     np.savez_compressed(os.path.join(HERE, "steps.npz"), **step_vectors(ref))
     np.savez_compressed(os.path.join(HERE, "soft.npz"), **soft_vectors(ref))
     print("golden vectors written to", HERE)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) > 2 and sys.argv[2] == "p2m":
+        # only the particle remeshing vectors
+        _install_reference(root)
+        np.savez_compressed(os.path.join(HERE, "p2m.npz"), **p2m_vectors())
+        print("p2m vectors written to", HERE)
+    else:
+        main(root)

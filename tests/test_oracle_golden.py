@@ -196,3 +196,62 @@ def test_soft_sphere_loop(golden):
     for f, mine in (("omega", st.vorticity), ("eta1", st.eta1), ("eta2", st.eta2),
                     ("phi", st.ball_phi), ("chi", st.ball_char_func)):
         assert rel_l2(mine, g[f"soft/{f}_12"]) < 1e-12, f
+
+
+@pytest.mark.parametrize("tag", ["a", "b", "c"])
+def test_particles_to_mesh_mp4_bit_exact(golden, tag):
+    """The oracle's MP4 particle-to-mesh against the reference's C++
+    (core/src/interpolation/particles_to_mesh_2D.hpp), periodic and unbounded,
+    particles near their mesh points (a, b) and anywhere in the domain (c)."""
+    g = golden("p2m")
+    px, py, v, dx = g[f"{tag}/px"], g[f"{tag}/py"], g[f"{tag}/v"], float(g[f"{tag}/dx"])
+    for name, fn in (("periodic", K.particles_to_mesh_2D_mp4),
+                     ("unbounded", K.particles_to_mesh_2D_unbounded_mp4)):
+        out = np.zeros_like(v)
+        fn(px, py, v, out, dx, dx)
+        np.testing.assert_array_equal(out, g[f"{tag}/{name}"])
+
+
+def test_advect_vorticity_via_particles_bit_exact(golden):
+    """kernels/advect_particle.py (both variants), two steps, against the
+    reference run over its compiled interpolation."""
+    g = golden("p2m")
+    nr, dx, dt = int(g["adv/nr"]), float(g["adv/dx"]), float(g["adv/dt"])
+    nz = g["adv/w0"].shape[1]
+    z = (np.arange(nz) + 0.5) * dx
+    Zd, Rd = np.meshgrid(z, (np.arange(2 * nr) + 0.5) * dx)
+    for name, fn in (("unbounded", K.advect_vorticity_via_particles),
+                     ("periodic", K.advect_vorticity_via_particles_periodic)):
+        w = g["adv/w0"].copy()
+        zp, rp, vp = Zd.copy(), Rd.copy(), np.zeros_like(Zd)
+        for _ in range(2):
+            fn(zp, rp, vp, w, Zd, Rd, nr, g["adv/u_z"], g["adv/u_r"], dx, dt)
+        np.testing.assert_array_equal(w, g[f"adv/{name}"])
+
+
+def test_oracle_particles_to_mesh_matches_compiled_reference():
+    """Random cases against the reference's C++ itself, where it was built
+    (oracle/_ref, only in a container holding the reference sources)."""
+    import ctypes
+    import os
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle",
+                        "_ref", "libref_p2m.so")
+    if not os.path.exists(path):
+        pytest.skip("reference particle-to-mesh not built here")
+    lib = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    for f in (lib.ref_p2m_2d_mp4, lib.ref_p2m_2d_unbounded_mp4):
+        f.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+    rng = np.random.default_rng(3)
+    for n0, n1 in ((8, 8), (33, 17), (20, 64)):
+        dx = 0.03
+        Z, R = np.meshgrid((np.arange(n1) + 0.5) * dx, (np.arange(n0) + 0.5) * dx)
+        px = Z + 0.99 * dx * rng.uniform(-1, 1, Z.shape)
+        py = R + 0.99 * dx * rng.uniform(-1, 1, Z.shape)
+        v = rng.standard_normal(Z.shape)
+        for ref, ora in ((lib.ref_p2m_2d_mp4, K.particles_to_mesh_2D_mp4),
+                         (lib.ref_p2m_2d_unbounded_mp4, K.particles_to_mesh_2D_unbounded_mp4)):
+            a, b = np.zeros((n0, n1)), np.zeros((n0, n1))
+            ref(px.ctypes.data, py.ctypes.data, v.ctypes.data, a.ctypes.data, n0, n1, dx, dx)
+            ora(px, py, v, b, dx, dx)
+            np.testing.assert_array_equal(a, b)
