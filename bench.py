@@ -17,6 +17,7 @@ Workloads (synthetic, seeded; there is no dataset):
               of 32 Gaussian vortex rings (seed 3); FP32 tensor-core solve +
               one FP64 refinement step vs plain FP64
   serve       continuous-batching server on a Poisson request stream
+  remesh      vorticity advection by remeshed particles (MP4), 2048 x 1024
 
 --impl reference times the reference's CPU path restated by the oracle
 (numpy FP64, all host cores for BLAS) on a bounded sample of the same
@@ -577,6 +578,95 @@ def run_serve(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_remesh(args, world, rank, local):
+    """Vorticity advection by remeshed particles (kernels/advect_particle.py),
+    2048 x 1024 (nz x nr) cells, particles on the (2048, 2048) mirrored domain:
+    one step = particle update + MP4 particle-to-mesh + reset, FP64, through
+    the drop-in advect_vorticity_via_particles. Synthetic seeded vorticity and
+    velocity with |u| dt <= 0.5 dx."""
+    import torch
+    from pyaxisymflow_gb300 import _native as N
+    from pyaxisymflow_gb300.kernels.advect_particle import advect_vorticity_via_particles
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nz, nr = 2048, 1024
+    dx = 1.0 / nz
+    rng = np.random.default_rng(7)
+    f64 = dict(dtype=torch.float64, device=dev)
+    Zd, Rd = np.meshgrid((np.arange(nz) + 0.5) * dx, (np.arange(2 * nr) + 0.5) * dx)
+    Zt, Rt = torch.tensor(Zd, **f64), torch.tensor(Rd, **f64)
+    zp, rp, vp = Zt.clone(), Rt.clone(), torch.zeros_like(Zt)
+    w0 = rng.standard_normal((nr, nz))
+    w = torch.tensor(w0, **f64)
+    uz = torch.tensor(rng.uniform(-1, 1, (nr, nz)), **f64)
+    ur = torch.tensor(rng.uniform(-1, 1, (nr, nz)), **f64)
+    dt = 0.5 * dx
+    stream = torch.cuda.current_stream(dev)
+    step = lambda: advect_vorticity_via_particles(zp, rp, vp, w, Zt, Rt, nr, uz, ur, dx, dt)  # noqa
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        torch.cuda.synchronize(dev)
+        wall = (time.perf_counter() - t0) / args.steps
+    # device time of the particle-to-mesh kernels alone (CUDA events)
+    work = torch.empty(int(N.lib().axi_p2m_mp4_work_bytes(2 * nr, nz)), dtype=torch.uint8,
+                       device=dev)
+    out = torch.empty_like(Zt)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    k = max(10, args.steps // 4)
+    ev[0].record(stream)
+    for _ in range(k):
+        N.call("axi_particles_to_mesh_2d_mp4_f64", N.ptr(Zt), N.ptr(Rt), N.ptr(vp), N.ptr(out),
+               2 * nr, nz, dx, dx, 0, N.ptr(work), N.stream_of(out))
+    ev[1].record(stream)
+    torch.cuda.synchronize(dev)
+    p2m_ms = ev[0].elapsed_time(ev[1]) / k
+    hbm, _, src = peaks()
+    n_part = 2 * nr * nz
+    alg = 32.0 * n_part  # positions x, y, values in; mesh values out (FP64)
+    line = {
+        "metric": "cell-updates/s, vorticity advection by remeshed particles (FP64)",
+        "value": nr * nz / wall, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": wall * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "remesh", "grid": f"nz {nz} x nr {nr}",
+                   "particles": n_part, "kernel": "MP4, unbounded",
+                   "timing": "wall clock per call of the drop-in (it synchronises to check "
+                             "particle displacement)"},
+        "roofline": {"bound": "hbm", "kernel": "particles_to_mesh (stencil + gather)",
+                     "achieved": alg / (p2m_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": alg / (p2m_ms / 1e3) / 1e9 / hbm, "traffic": None,
+                     "peak_source": f"{src} hbm", "p2m_ms": p2m_ms,
+                     "algorithmic_bytes": "32 B per particle"},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        # the oracle (numpy, the reference's algorithm) on a 256 x 128 sample
+        snr, snz = 128, 256
+        sdx = 1.0 / snz
+        sZ, sR = np.meshgrid((np.arange(snz) + 0.5) * sdx, (np.arange(2 * snr) + 0.5) * sdx)
+        from oracle import kernels as K
+        sw = rng.standard_normal((snr, snz))
+        suz, sur = rng.uniform(-1, 1, (snr, snz)), rng.uniform(-1, 1, (snr, snz))
+        szp, srp, svp = sZ.copy(), sR.copy(), np.zeros_like(sZ)
+        n, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < 10.0:
+            K.advect_vorticity_via_particles(szp, srp, svp, sw, sZ, sR, snr, suz, sur, sdx,
+                                             0.5 * sdx)
+            n += 1
+        secs = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": snr * snz * n / secs, "unit": UNIT, "cores": 1,
+                                "kind": "port",
+                                "sample": f"{snz} x {snr} cells, {n} steps, numpy oracle, "
+                                          f"{secs:.1f} s"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -584,7 +674,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ensemble64",
-                    choices=["ensemble64", "sphere512", "poisson2048", "serve"])
+                    choices=["ensemble64", "sphere512", "poisson2048", "serve", "remesh"])
     ap.add_argument("--requests", type=int, default=40)
     ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -599,6 +689,8 @@ def main():
         run_poisson(args, world, rank, local)
     elif args.workload == "serve":
         run_serve(args, world, rank, local)
+    elif args.workload == "remesh":
+        run_remesh(args, world, rank, local)
     else:
         run_gb300(args, world, rank, local)
 
