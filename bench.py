@@ -49,10 +49,7 @@ PHASE_FIELDS = {"vel_max": 1, "penalise": 6, "advect_diffuse": 4}
 
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of a phase, from the
 # ncu captures summarised in profiles/ (transform: sum over its four products).
-NCU_TRAFFIC = {
-    # profiles/tf32x3_gemm_ensemble64.md: 265.6 + 251.4 + 264.8 + 194.5 MB
-    ("ensemble64", "f32", "transform"): 976.3e6,
-}
+NCU_TRAFFIC = {}
 
 
 def ensemble_cases(workload, seed=4):
@@ -285,6 +282,20 @@ def run_gb300(args, world, rank, local):
     for s in range(nph):
         for k, p in enumerate(PHASES):
             ph_ms[p] += evs[s][k][0].elapsed_time(evs[s][k][1]) / nph
+    # the four launches of the transform one at a time (phase ids 5..8)
+    part_ms = [0.0] * 4
+    pev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            for _ in range(4)] for _ in range(nph)]
+    for s in range(nph):
+        for q in range(4):
+            pev[s][q][0].record(stream)
+            ens.phase(5 + q)
+            pev[s][q][1].record(stream)
+    torch.cuda.synchronize(dev)
+    for s in range(nph):
+        for q in range(4):
+            part_ms[q] += pev[s][q][0].elapsed_time(pev[s][q][1]) / nph
+    uses_dct = ens.dct
     # ---- end to end through the public API with host buffers ------------------
     # every case's vorticity in pinned host memory; each step copies it in,
     # advances every case and copies it and the state blocks (dt, Cd) back,
@@ -346,35 +357,51 @@ def run_gb300(args, world, rank, local):
                 "rel_l2_fp32_vs_fp64_max_over_sizes": errs, "accuracy_steps": nsteps}
     # ---- roofline of the dominant kernel ---------------------------------------
     hbm, bf16, src = peaks()
-    dom = max(ph_ms, key=ph_ms.get)
     esize = 8 if args.precision == "f64" else 4
-    if uses_tc:
-        PHASE_FIELDS["advect_diffuse"] += 2
+    if uses_tc and not uses_dct:
+        PHASE_FIELDS["advect_diffuse"] += 2   # omega's TF32 operand pair
     if any(c.sediment for c in cases):
-        PHASE_FIELDS["advect_diffuse"] += 1
-    if dom == "transform":
-        flops = sum(4.0 * c.nr * c.nz * (c.nr + c.nz) for c in cases)
-        achieved = flops / (ph_ms[dom] / 1000.0) / 1e12
-        if args.precision == "f64":
-            roof = {"bound": "fp64", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
-                    "peak_source": "nominal GB300 FP64 (DFMA probe on this pool: 1.0)"}
+        PHASE_FIELDS["advect_diffuse"] += 1   # the rebuilt mask
+    zname = "z_transforms" if uses_dct else "z_products"
+    kern_ms = {"kill": ph_ms["kill"], zname: part_ms[0] + part_ms[2],
+               "r_products": part_ms[1] + part_ms[3], "vel_max": ph_ms["vel_max"],
+               "penalise": ph_ms["penalise"], "advect_diffuse": ph_ms["advect_diffuse"]}
+    dom = max(kern_ms, key=kern_ms.get)
+    if dom in ("r_products", "z_products"):
+        # useful FLOPs: two products of 2 n^2 m each per case
+        flops = sum(4.0 * (c.nr * c.nr * c.nz if dom == "r_products" else c.nz * c.nz * c.nr)
+                    for c in cases)
+        achieved = flops / (kern_ms[dom] / 1000.0) / 1e12
+        if args.precision == "f64" or not uses_tc:
+            roof = {"bound": "fp64" if args.precision == "f64" else "fp32",
+                    "achieved": achieved, "peak": 1.25 if args.precision == "f64" else 73.0,
+                    "unit": "TFLOP/s",
+                    "peak_source": "nominal GB300 FP64 (DFMA probe on this pool: 1.0)"
+                    if args.precision == "f64" else "nominal GB300 FP32"}
         else:
             # 3xTF32: three tensor products per useful product; the TF32 dense
             # rate is half the BF16 rate
             roof = {"bound": "tensor", "achieved": 3 * achieved, "peak": bf16 / 2,
                     "unit": "TFLOP/s", "useful_tflops": achieved,
                     "peak_source": f"{src} bf16 / 2 (TF32 dense rate)"}
+    elif dom == "z_transforms":
+        # per transform: read the rows (4 B), write the TF32 pair (8 B)
+        nbytes = sum(2 * 12.0 * c.nr * c.nz for c in cases)
+        achieved = nbytes / (kern_ms[dom] / 1000.0) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "peak_source": f"{src} hbm"}
     else:
-        nbytes = sum(PHASE_FIELDS[dom] * esize * c.nr * c.nz for c in cases)
-        achieved = nbytes / (ph_ms[dom] / 1000.0) / 1e9
+        nbytes = sum(PHASE_FIELDS.get(dom, 0) * esize * c.nr * c.nz for c in cases)
+        achieved = nbytes / (kern_ms[dom] / 1000.0) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "peak_source": f"{src} hbm"}
     roof["kernel"] = dom
     roof["frac"] = roof["achieved"] / roof["peak"]
-    # DRAM bytes (read + write) of one launch of the dominant phase, from the
-    # ncu capture summarised in profiles/ (same workload and kernels)
+    roof["kernel_ms"] = kern_ms[dom]
+    # DRAM bytes (read + write) of the dominant kernel's launches in one step,
+    # from the ncu capture summarised in profiles/ (same workload and kernels)
     roof["traffic"] = NCU_TRAFFIC.get((args.workload, args.precision, dom))
-    roof["traffic_unit"] = "bytes per launch of the phase"
+    roof["traffic_unit"] = "bytes per step"
     stencil_bytes = sum(sum(PHASE_FIELDS.values()) * esize * c.nr * c.nz for c in cases)
     stencil_ms = sum(ph_ms[p] for p in PHASE_FIELDS)
     line = {
@@ -387,6 +414,9 @@ def run_gb300(args, world, rank, local):
                    "parallelism": f"case-parallel replicas x{world}"},
         "roofline": roof,
         "phase_ms": ph_ms,
+        "kernel_ms": kern_ms,
+        "transform": "z DCT + radial tensor-core products" if uses_dct
+                     else ("tensor-core products" if uses_tc else "SIMT products"),
         "step_latency_ms": {"p50": float(np.percentile(step_ms, 50)),
                             "p99": float(np.percentile(step_ms, 99))},
         "plain_fp64": fp64,

@@ -463,21 +463,32 @@ typedef struct axi_case {
   const void* tc_basis[8]; /* E_z^-1 hi, lo (nz, nz); E_r^-1 diag(r) hi, lo (nr, nr);
                               E_z hi, lo (nz, nz); E_r hi, lo (nr, nr) */
   void* tc_work[4];        /* X hi, lo (nz, nr); Y hi, lo (nr, nz) */
+  /* AXI_PLAN_DCT_Z: float tables of the z transform for this nz (shared by
+   * cases of equal nz): exp(-2 pi i m / nz) as (cos, sin) pairs, m < nz;
+   * (cos, sin)(pi k / 2 nz), k < nz; c_k; 1 / c_k (c_0 = sqrt(1 / nz),
+   * c_k = sqrt(2 / nz)); inv_eig then holds 1 / (lambda_r_i + lambda_z_k) in
+   * DCT order, lambda_z_k = (2 - 2 cos(pi k / nz)) / dx^2. */
+  const void* dct_table;
 } axi_case;
 
 /* Launch plan of a set of cases: tile tables in device memory. */
 typedef struct axi_plan_info {
   int32_t n_cases;
-  int32_t n_stencil_tiles; /* 64 x 16 cell tiles over all cases */
+  int32_t n_stencil_tiles; /* AXI_TILE_NR x AXI_TILE_NZ cell tiles over all cases */
   int32_t n_gemm_tiles;    /* output tiles of the grouped spectral products */
   int32_t elem_bytes;      /* 8: float64 fields, 4: float32 fields */
   int64_t bytes;           /* device bytes the plan needs */
   int32_t flags;           /* AXI_PLAN_* */
   int32_t n_tc_tiles[4];   /* tensor-core tiles per spectral stage */
-  int32_t reserved;
+  int32_t n_dct_items;     /* row groups of the z transforms (AXI_PLAN_DCT_Z) */
 } axi_plan_info;
 
-enum { AXI_PLAN_TENSOR_CORES = 1 };
+/* AXI_PLAN_DCT_Z (with AXI_PLAN_TENSOR_CORES): the z-direction products run
+ * as orthonormal DCT-II / DCT-III transforms (the eigenbasis of the Neumann
+ * z operator), the radial ones on the tensor cores; every nz even with no
+ * prime factor other than 2 and 3; omega_hi / omega_lo and the z entries of
+ * tc_basis are then unused (may be NULL). */
+enum { AXI_PLAN_TENSOR_CORES = 1, AXI_PLAN_DCT_Z = 2 };
 
 /* Host only: validates the cases, assigns each its first tile
  * (cases[k].stencil_tile0) and fills `info` (sizes of the plan). flags:
@@ -504,7 +515,9 @@ int axi_rigid_step_f32(const axi_plan_info* info, const void* plan_dev, int n_st
                        void* stream);
 /* One phase of a step (0 kill, 1 spectral transform, 2 velocity max and dt,
  * 3 penalisation and drag, 4 advection and both diffusion stages); running
- * phases 0..4 in order equals one step. Lets a caller time each kernel. */
+ * phases 0..4 in order equals one step. Phases 5..8 are the four launches of
+ * phase 1 one at a time (z product or DCT, radial product, z product or
+ * inverse DCT, radial product). Lets a caller time each kernel. */
 int axi_rigid_phase_f64(const axi_plan_info* info, const void* plan_dev, int phase,
                         void* stream);
 int axi_rigid_phase_f32(const axi_plan_info* info, const void* plan_dev, int phase,

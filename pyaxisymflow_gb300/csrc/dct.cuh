@@ -1,0 +1,60 @@
+// Orthonormal DCT-II / DCT-III along the rows of (rows, N) float arrays, the
+// z-direction products of the spectral Poisson solve when the z operator is
+// the uniform Neumann Laplacian (FD matrix of
+// kernels/FastDiagonalisationStokesSolver.py:41-97 with bc_type
+// homogenous_neumann_along_z_and_r): its eigenvectors are the DCT-II basis
+// vectors c_k cos(pi k (j + 1/2) / N) (c_0 = sqrt(1/N), c_k = sqrt(2/N)), so
+// E_z^-1 x (= E_z^T x) is the orthonormal DCT-II of x and E_z y its inverse.
+// psi does not depend on which eigenbasis diagonalises the operator, so the
+// O(N^2) dense products become O(N log N) transforms.
+//
+// Each transform reorders the row (Makhoul: even samples forward, odd
+// samples backward), runs a complex mixed-radix (4, 2, 3) Stockham FFT in
+// shared memory and rotates by exp(-+ i pi k / 2N). Output is written
+// transposed, (N, rows), as the TF32 operand pair of the radial tensor-core
+// product that follows.
+#pragma once
+
+#include <cstdint>
+
+#include "axi_common.cuh"
+
+namespace axi_dct {
+
+constexpr int MAX_STAGES = 16;
+constexpr int ELEMS = 4096;                      // complex values per shared buffer
+constexpr int THREADS = 512;
+// two ping-pong buffers of float2 and the twiddle table (N <= ELEMS)
+constexpr int SMEM_BYTES = 3 * ELEMS * 8;
+
+// One row-transform problem (one case).
+struct DctJob {
+  int N;                       // row length (nz), even, 2^a 3^b, <= ELEMS
+  int rows;                    // rows of the input (nr)
+  int nstages;
+  int radix[MAX_STAGES];       // Stockham radices, first to last
+  const float* in;             // (rows, N) row-major
+  float* out_hi;               // (N, rows) row-major: TF32 hi part
+  float* out_lo;               // (N, rows): TF32 remainder
+  const float2* twiddle;       // exp(-2 pi i m / N), m < N
+  const float2* rot;           // (cos, sin)(pi k / 2N), k < N
+  const float* scale;          // c_k (forward) or 1 / c_k (inverse), k < N
+};
+
+// Rows one work item of the generic path transforms for a row length N.
+__host__ __device__ inline int rows_per_item(int N) { return ELEMS / N > 0 ? ELEMS / N : 1; }
+
+// Host: rows per work item for row length N (lengths with a specialised
+// kernel pack two real rows per complex transform).
+int rows_for(int N);
+
+// Host: Stockham radices of N (4s, then a 2, then 3s); false if N has
+// another factor or needs more than MAX_STAGES stages.
+bool plan_radices(int N, int* radix, int* nstages);
+
+// Host: launch over `n_items` work items (job, row0, -, -); forward = DCT-II
+// (E_z^T x), else DCT-III (E_z y).
+int launch(const DctJob* jobs_dev, const int4* items_dev, int n_items, bool forward,
+           cudaStream_t s);
+
+}  // namespace axi_dct

@@ -28,6 +28,7 @@
 // step, the simulated time, the drag sums across warps and tiles and the
 // body ODE.
 #include "axi_common.cuh"
+#include "dct.cuh"
 #include "tc_gemm.cuh"
 #include "tma.cuh"
 
@@ -1064,6 +1065,8 @@ struct PlanView {
   const CUtensorMap* maps;
   const axi_tc::TcJob* jobs;
   const int4* tc_tiles[4];
+  const axi_dct::DctJob* dct_jobs;  // forward jobs, then inverse jobs (n_cases each)
+  const int4* dct_items;
   int* err;
 };
 
@@ -1071,7 +1074,7 @@ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 inline size_t align128(size_t x) { return (x + 127) & ~size_t(127); }
 
 struct PlanOffsets {
-  size_t stencil, gemm, maps, jobs, tc_tiles[4], err, total;
+  size_t stencil, gemm, maps, jobs, tc_tiles[4], dct_jobs, dct_items, err, total;
 };
 
 // Plan buffer: cases | stencil tiles | SIMT GEMM tiles | stencil tensor maps
@@ -1094,6 +1097,14 @@ inline PlanOffsets plan_offsets(const axi_plan_info* info) {
     o.jobs = 0;
     for (int st = 0; st < 4; ++st) o.tc_tiles[st] = 0;
   }
+  if (info->flags & AXI_PLAN_DCT_Z) {
+    o.dct_jobs = align128(end);
+    end = o.dct_jobs + (size_t)2 * info->n_cases * sizeof(axi_dct::DctJob);
+    o.dct_items = align16(end);
+    end = o.dct_items + (size_t)info->n_dct_items * sizeof(int4);
+  } else {
+    o.dct_jobs = o.dct_items = 0;
+  }
   o.err = align16(end);
   end = o.err + 16;
   o.total = align16(end);
@@ -1112,6 +1123,9 @@ inline PlanView plan_view(const void* plan_dev, const axi_plan_info* info) {
   v.jobs = tc ? reinterpret_cast<const axi_tc::TcJob*>(base + o.jobs) : nullptr;
   for (int st = 0; st < 4; ++st)
     v.tc_tiles[st] = tc ? reinterpret_cast<const int4*>(base + o.tc_tiles[st]) : nullptr;
+  const bool dct = (info->flags & AXI_PLAN_DCT_Z) != 0;
+  v.dct_jobs = dct ? reinterpret_cast<const axi_dct::DctJob*>(base + o.dct_jobs) : nullptr;
+  v.dct_items = dct ? reinterpret_cast<const int4*>(base + o.dct_items) : nullptr;
   v.err = reinterpret_cast<int*>(const_cast<char*>(base) + o.err);
   return v;
 }
@@ -1124,11 +1138,30 @@ inline PlanView plan_view(const void* plan_dev, const axi_plan_info* info) {
 //   stage 3  psi (nr, nz) = Er (nr, nr) * [X]^T                     -> plain
 // i.e. psi = E_r ((E_r^-1 diag(r) omega E_z^-T) .* inv_eig) E_z^T as in
 // kernels/FastDiagonalisationStokesSolver.py:137-156.
-int build_tc_jobs(const axi_case& k, axi_tc::TcJob job[4]) {
+// With `dct`, stages 0 and 2 run as z transforms (build_dct_jobs) and stage 1
+// writes its scaled result plain for the inverse transform.
+int build_tc_jobs(const axi_case& k, axi_tc::TcJob job[4], bool dct) {
   const int nr = k.nr, nz = k.nz;
   const float* const* b = reinterpret_cast<const float* const*>(k.tc_basis);
   float* const* w = reinterpret_cast<float* const*>(k.tc_work);
   memset(job, 0, 4 * sizeof(axi_tc::TcJob));
+  if (dct) {
+    AXI_TRY(axi_tc::encode_operand(&job[1].a_hi, b[2], nr, nr, nr));
+    AXI_TRY(axi_tc::encode_operand(&job[1].a_lo, b[3], nr, nr, nr));
+    AXI_TRY(axi_tc::encode_operand(&job[1].b_hi, w[0], nz, nr, nr));
+    AXI_TRY(axi_tc::encode_operand(&job[1].b_lo, w[1], nz, nr, nr));
+    job[1].c = w[2];
+    job[1].scale = static_cast<const float*>(k.inv_eig);
+    job[1].M = nr; job[1].N = nz; job[1].K = nr; job[1].ldc = nz;
+    job[1].mode = axi_tc::MODE_SCALE;
+    AXI_TRY(axi_tc::encode_operand(&job[3].a_hi, b[6], nr, nr, nr));
+    AXI_TRY(axi_tc::encode_operand(&job[3].a_lo, b[7], nr, nr, nr));
+    AXI_TRY(axi_tc::encode_operand(&job[3].b_hi, w[0], nz, nr, nr));
+    AXI_TRY(axi_tc::encode_operand(&job[3].b_lo, w[1], nz, nr, nr));
+    job[3].c = static_cast<float*>(k.psi); job[3].M = nr; job[3].N = nz;
+    job[3].K = nr; job[3].ldc = nz; job[3].mode = axi_tc::MODE_PLAIN;
+    return AXI_OK;
+  }
   // stage 0
   AXI_TRY(axi_tc::encode_operand(&job[0].a_hi, b[0], nz, nz, nz));
   AXI_TRY(axi_tc::encode_operand(&job[0].a_lo, b[1], nz, nz, nz));
@@ -1161,6 +1194,39 @@ int build_tc_jobs(const axi_case& k, axi_tc::TcJob job[4]) {
   return AXI_OK;
 }
 
+// z transforms of one case: forward (DCT-II of the rows of omega into the
+// X operand pair) and inverse (DCT-III of the rows of the plain stage-1
+// result Y into the X operand pair of stage 3).
+int build_dct_jobs(const axi_case& k, axi_dct::DctJob* fwd, axi_dct::DctJob* inv) {
+  axi_dct::DctJob j;
+  memset(&j, 0, sizeof(j));
+  j.N = k.nz;
+  j.rows = k.nr;
+  if (!axi_dct::plan_radices(k.nz, j.radix, &j.nstages)) {
+    axi::set_error("plan: nz %d has no DCT plan (even, factors 2 and 3 only, <= %d)", k.nz,
+                   axi_dct::ELEMS);
+    return AXI_ERR_INVALID;
+  }
+  const char* t = static_cast<const char*>(k.dct_table);
+  j.twiddle = reinterpret_cast<const float2*>(t);
+  j.rot = reinterpret_cast<const float2*>(t + (size_t)8 * k.nz);
+  float* const* w = reinterpret_cast<float* const*>(k.tc_work);
+  j.out_hi = w[0];
+  j.out_lo = w[1];
+  *fwd = j;
+  fwd->in = static_cast<const float*>(k.omega);
+  fwd->scale = reinterpret_cast<const float*>(t + (size_t)16 * k.nz);
+  *inv = j;
+  inv->in = w[2];
+  inv->scale = reinterpret_cast<const float*>(t + (size_t)20 * k.nz);
+  return AXI_OK;
+}
+
+inline int dct_items_of(const axi_case& k) {
+  const int r = axi_dct::rows_for(k.nz);
+  return (k.nr + r - 1) / r;
+}
+
 inline int tc_tiles_of(const axi_case& k, int stage) {
   const int M = (stage % 2 == 0) ? k.nz : k.nr;
   const int N = (stage % 2 == 0) ? k.nr : k.nz;
@@ -1168,7 +1234,10 @@ inline int tc_tiles_of(const axi_case& k, int stage) {
 }
 
 enum { PH_KILL = 0, PH_TRANSFORM = 1, PH_VEL_MAX = 2, PH_PENALISE = 3, PH_ADVECT_DIFFUSE = 4,
-       PH_COUNT = 5 };
+       PH_COUNT = 5,
+       // the four launches of PH_TRANSFORM one at a time (timing): z product
+       // or transform, radial product, z product or inverse transform, radial
+       PH_TRANSFORM_PART0 = 5, PH_PARTS_END = 9 };
 
 // The persistent stencil kernels reserve their dynamic shared memory once per
 // process and run as many blocks as fit on every SM (at most one block per
@@ -1230,6 +1299,15 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
       kill_reset_kernel<T><<<info->n_cases, 256, 0, s>>>(v.cases);
       break;
     case PH_TRANSFORM:
+      if (v.dct_jobs) {
+        // z transform, radial product, inverse z transform, radial product
+        AXI_TRY(axi_dct::launch(v.dct_jobs, v.dct_items, info->n_dct_items, true, s));
+        AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[1], info->n_tc_tiles[1], v.err, s));
+        AXI_TRY(axi_dct::launch(v.dct_jobs + info->n_cases, v.dct_items, info->n_dct_items,
+                                false, s));
+        AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[3], info->n_tc_tiles[3], v.err, s));
+        break;
+      }
       if (v.jobs) {
         for (int st = 0; st < 4; ++st)
           AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[st], info->n_tc_tiles[st], v.err, s));
@@ -1257,6 +1335,27 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
           <<<StencilGrid<T>::get(PH_ADVECT_DIFFUSE, nt), NT, advect_diffuse_smem<T>(), s>>>(
               v.cases, v.stencil, nt, v.maps, v.err);
       break;
+    case PH_TRANSFORM_PART0:
+    case PH_TRANSFORM_PART0 + 1:
+    case PH_TRANSFORM_PART0 + 2:
+    case PH_TRANSFORM_PART0 + 3: {
+      const int st = phase - PH_TRANSFORM_PART0;
+      if (v.dct_jobs && (st == 0 || st == 2)) {
+        AXI_TRY(axi_dct::launch(st == 0 ? v.dct_jobs : v.dct_jobs + info->n_cases, v.dct_items,
+                                info->n_dct_items, st == 0, s));
+      } else if (v.jobs) {
+        AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[st], info->n_tc_tiles[st], v.err, s));
+      } else if (st == 0) {
+        grouped_gemm_kernel<T, 0><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
+      } else if (st == 1) {
+        grouped_gemm_kernel<T, 1><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
+      } else if (st == 2) {
+        grouped_gemm_kernel<T, 2><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
+      } else {
+        grouped_gemm_kernel<T, 3><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
+      }
+      break;
+    }
     default:
       axi::set_error("rigid_phase: unknown phase %d", phase);
       return AXI_ERR_INVALID;
@@ -1339,36 +1438,52 @@ extern "C" int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, int f
   int bm, bn;
   AXI_TRY(gemm_tile_dims(elem_bytes, &bm, &bn));
   const bool tc = (flags & AXI_PLAN_TENSOR_CORES) != 0;
+  const bool dct = (flags & AXI_PLAN_DCT_Z) != 0;
   if (tc && elem_bytes != 4) {
     axi::set_error("plan_init: tensor-core products need float32 fields");
     return AXI_ERR_INVALID;
   }
+  if (dct && !tc) {
+    axi::set_error("plan_init: the DCT z transform goes with the tensor-core products");
+    return AXI_ERR_INVALID;
+  }
   memset(info, 0, sizeof(*info));
-  int nt = 0, ng = 0;
+  int nt = 0, ng = 0, nd = 0;
   for (int c = 0; c < n_cases; ++c) {
     const axi_case& k = cases[c];
     cases[c].stencil_tile0 = nt;
     nt += tiles_of(k);
     ng += ((k.nr + bm - 1) / bm) * ((k.nz + bn - 1) / bn);
     if (tc) {
-      if (!k.omega_hi || !k.omega_lo || (k.nr % 4) || (k.nz % 4)) {
+      if ((!dct && (!k.omega_hi || !k.omega_lo)) || (k.nr % 4) || (k.nz % 4)) {
         axi::set_error("plan_init: case %d lacks tensor-core operands or nr, nz not multiples of 4",
                        c);
         return AXI_ERR_INVALID;
       }
-      for (int q = 0; q < 8; ++q)
-        if (!k.tc_basis[q] || (q < 4 && !k.tc_work[q])) {
+      for (int q = 0; q < 8; ++q) {
+        const bool z_basis = q == 0 || q == 1 || q == 4 || q == 5;
+        if ((!k.tc_basis[q] && !(dct && z_basis)) || (q < 4 && !k.tc_work[q])) {
           axi::set_error("plan_init: case %d lacks tensor-core operand %d", c, q);
           return AXI_ERR_INVALID;
         }
-      for (int st = 0; st < 4; ++st) info->n_tc_tiles[st] += tc_tiles_of(k, st);
+      }
+      int radix[axi_dct::MAX_STAGES], ns;
+      if (dct && (!k.dct_table || !axi_dct::plan_radices(k.nz, radix, &ns))) {
+        axi::set_error("plan_init: case %d: no DCT table or nz %d not even with factors 2, 3",
+                       c, k.nz);
+        return AXI_ERR_INVALID;
+      }
+      for (int st = 0; st < 4; ++st)
+        if (!(dct && (st == 0 || st == 2))) info->n_tc_tiles[st] += tc_tiles_of(k, st);
+      if (dct) nd += dct_items_of(k);
     }
   }
   info->n_cases = n_cases;
   info->n_stencil_tiles = nt;
   info->n_gemm_tiles = ng;
   info->elem_bytes = elem_bytes;
-  info->flags = tc ? AXI_PLAN_TENSOR_CORES : 0;
+  info->flags = (tc ? AXI_PLAN_TENSOR_CORES : 0) | (dct ? AXI_PLAN_DCT_Z : 0);
+  info->n_dct_items = nd;
   info->bytes = (int64_t)plan_offsets(info).total;
   return AXI_OK;
 }
@@ -1421,10 +1536,26 @@ extern "C" int axi_plan_upload(const axi_case* cases, const axi_plan_info* info,
   if (info->flags & AXI_PLAN_TENSOR_CORES) {
     const PlanOffsets& o = po;
     axi_tc::TcJob* jobs = reinterpret_cast<axi_tc::TcJob*>(&buf[o.jobs]);
-    for (int c = 0; c < n; ++c) AXI_TRY(build_tc_jobs(cases[c], jobs + 4 * c));
+    const bool dct = (info->flags & AXI_PLAN_DCT_Z) != 0;
+    for (int c = 0; c < n; ++c) AXI_TRY(build_tc_jobs(cases[c], jobs + 4 * c, dct));
+    if (dct) {
+      axi_dct::DctJob* dj = reinterpret_cast<axi_dct::DctJob*>(&buf[o.dct_jobs]);
+      int4* di = reinterpret_cast<int4*>(&buf[o.dct_items]);
+      int q = 0;
+      for (int c = 0; c < n; ++c) {
+        AXI_TRY(build_dct_jobs(cases[c], dj + c, dj + n + c));
+        const int rows = axi_dct::rows_for(cases[c].nz);
+        for (int r0 = 0; r0 < cases[c].nr; r0 += rows) di[q++] = make_int4(c, r0, 0, 0);
+      }
+      if (q != info->n_dct_items) {
+        axi::set_error("plan_upload: cases changed since plan_init");
+        return AXI_ERR_INVALID;
+      }
+    }
     for (int st = 0; st < 4; ++st) {
       int4* tt = reinterpret_cast<int4*>(&buf[o.tc_tiles[st]]);
       int qq = 0;
+      if (dct && (st == 0 || st == 2)) continue;
       for (int c = 0; c < n; ++c) {
         const axi_case& k = cases[c];
         const int M = (st % 2 == 0) ? k.nz : k.nr;
@@ -1451,7 +1582,7 @@ extern "C" int axi_rigid_refresh_operands(const axi_plan_info* info, const void*
   axi::clear_error();
   AXI_TRY(axi::check_ptr("rigid_refresh_operands", info, "info"));
   AXI_TRY(axi::check_ptr("rigid_refresh_operands", plan_dev, "plan_dev"));
-  if (!(info->flags & AXI_PLAN_TENSOR_CORES)) return AXI_OK;
+  if (!(info->flags & AXI_PLAN_TENSOR_CORES) || (info->flags & AXI_PLAN_DCT_Z)) return AXI_OK;
   const PlanView v = plan_view(plan_dev, info);
   refresh_split_kernel<<<info->n_stencil_tiles, NT, 0, axi::as_stream(stream)>>>(v.cases,
                                                                                   v.stencil);

@@ -83,10 +83,10 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// v already carries the elementwise factor of MODE_SCALE_SPLIT.
+// v already carries the elementwise factor of MODE_SCALE_SPLIT / MODE_SCALE.
 __device__ __forceinline__ void store_value(const TcJob& job, int row, int col, float v) {
   const long long idx = (long long)row * job.ldc + col;
-  if (job.mode == MODE_PLAIN) {
+  if (job.mode == MODE_PLAIN || job.mode == MODE_SCALE) {
     job.c[idx] = v;
     return;
   }
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (!__all_sync(0xffffffffu, ok && *reinterpret_cast<volatile int*>(err) == 0)) break;
       tc_fence_after();
       const int row0 = tr.y + 32 * q;
-      const bool scaled = job.mode == MODE_SCALE_SPLIT;
+      const bool scaled = job.mode == MODE_SCALE_SPLIT || job.mode == MODE_SCALE;
 #pragma unroll 1
       for (int cc = half * CHUNKS; cc < (half + 1) * CHUNKS; ++cc) {
         const int col = tr.z + cc * 32 + lane;

@@ -50,7 +50,7 @@ constexpr int EPI_WARPS = 8;                    // two per TMEM lane quarter
 constexpr int THREADS = 32 * (2 + EPI_WARPS);   // TMA warp, MMA warp, 8 epilogue warps
 constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 + 256 + EPI_WARPS * 32 * 33 * 4;
 
-enum { MODE_PLAIN = 0, MODE_SPLIT = 1, MODE_SCALE_SPLIT = 2 };
+enum { MODE_PLAIN = 0, MODE_SPLIT = 1, MODE_SCALE_SPLIT = 2, MODE_SCALE = 3 };
 enum { ERR_PRODUCER = 1, ERR_MMA = 2, ERR_EPILOGUE = 3, ERR_DRAIN = 4 };
 
 // One GEMM problem. Tensor maps are encoded on the host (cuTensorMapEncodeTiled)
@@ -59,7 +59,7 @@ struct TcJob {
   CUtensorMap a_hi, a_lo, b_hi, b_lo;
   float* c;            // output (MODE_PLAIN) or its hi part
   float* c_lo;         // lo part (split modes)
-  const float* scale;  // elementwise factor, row-major (M, N) (MODE_SCALE_SPLIT)
+  const float* scale;  // elementwise factor, row-major (M, N) (MODE_SCALE*)
   int M, N, K, ldc;
   int mode;
 };

@@ -53,6 +53,7 @@ class AxiCase(ctypes.Structure):
         ("history_len", ctypes.c_int64),
         ("omega_hi", ctypes.c_void_p), ("omega_lo", ctypes.c_void_p),
         ("tc_basis", ctypes.c_void_p * 8), ("tc_work", ctypes.c_void_p * 4),
+        ("dct_table", ctypes.c_void_p),
     ]
 
 
@@ -136,26 +137,63 @@ class AxiPlanInfo(ctypes.Structure):
     _fields_ = [("n_cases", ctypes.c_int32), ("n_stencil_tiles", ctypes.c_int32),
                 ("n_gemm_tiles", ctypes.c_int32), ("elem_bytes", ctypes.c_int32),
                 ("bytes", ctypes.c_int64), ("flags", ctypes.c_int32),
-                ("n_tc_tiles", ctypes.c_int32 * 4), ("reserved", ctypes.c_int32)]
+                ("n_tc_tiles", ctypes.c_int32 * 4), ("n_dct_items", ctypes.c_int32)]
 
 
 PLAN_TENSOR_CORES = 1
+PLAN_DCT_Z = 2
+
+
+def dct_ok(nz):
+    """nz the z transform handles as a DCT: even, factors 2 and 3 only, <= 4096."""
+    n = int(nz)
+    if n < 2 or n % 2 or n > 4096:
+        return False
+    for f in (2, 3):
+        while n % f == 0:
+            n //= f
+    return n == 1
+
+
+def dct_table(nz):
+    """Float tables of the z transform (layout of axi_case.dct_table):
+    exp(-2 pi i m / nz) as (cos, sin), (cos, sin)(pi k / 2 nz), c_k, 1 / c_k."""
+    m = np.arange(nz, dtype=np.float64)
+    tw = np.stack([np.cos(2 * np.pi * m / nz), -np.sin(2 * np.pi * m / nz)], axis=1)
+    rot = np.stack([np.cos(np.pi * m / (2 * nz)), np.sin(np.pi * m / (2 * nz))], axis=1)
+    c = np.full(nz, np.sqrt(2.0 / nz))
+    c[0] = np.sqrt(1.0 / nz)
+    return np.concatenate([tw.ravel(), rot.ravel(), c, 1.0 / c]).astype(np.float32)
 
 
 class _Bases:
-    """Spectral bases shared by all cases with the same (nr, nz, dx)."""
+    """Spectral bases shared by all cases with the same (nr, nz, dx).
 
-    def __init__(self, nr, nz, dx, dtype, device, tensor_cores=False):
+    With `dct`, the z eigenbasis is the orthonormal DCT-II basis (the Neumann
+    z operator of the solver is diagonal in it): the z products become
+    transforms, inv_eig is 1 / (lambda_r_i + lambda_z_k) in DCT order and only
+    the radial operands are kept for the tensor cores."""
+
+    def __init__(self, nr, nz, dx, dtype, device, tensor_cores=False, dct=False):
         solver = FastDiagonalisationStokesSolver(nr, nz, dx, device=device)
         d = solver.engine.dev
         self.t = {k: d[k].to(dtype).contiguous() for k in
                   ("Er", "Er_inv_w", "EzinvT", "EzT", "inv_eig")}
         self.tc = []
+        self.dct_table = None
+        if dct:
+            lam_z = (2.0 - 2.0 * np.cos(np.pi * np.arange(nz) / nz)) / (dx * dx)
+            inv = 1.0 / (solver.engine.eig_vals_r.reshape(nr, 1) + lam_z.reshape(1, nz))
+            self.t["inv_eig"] = torch.tensor(inv, dtype=dtype, device=device)
+            self.dct_table = torch.tensor(dct_table(nz), device=device)
         if tensor_cores:
             h = solver.engine.host
             # operands of the K-major tensor-core form (C = A B^T per stage):
-            # E_z^-1, E_r^-1 diag(r), E_z, E_r
-            for m in (h["EzinvT"].T, h["Er_inv_w"], h["EzT"].T, h["Er"]):
+            # E_z^-1, E_r^-1 diag(r), E_z, E_r (the z ones unused with dct)
+            for k, m in enumerate((h["EzinvT"].T, h["Er_inv_w"], h["EzT"].T, h["Er"])):
+                if dct and k in (0, 2):
+                    self.tc += [None, None]
+                    continue
                 hi, lo = tf32_split(np.ascontiguousarray(m))
                 self.tc.append(torch.tensor(hi, device=device))
                 self.tc.append(torch.tensor(lo, device=device))
@@ -201,12 +239,13 @@ class CaseState:
             partials=torch.zeros(2 * ((c.nr + TILE_NR - 1) // TILE_NR)
                                  * ((c.nz + TILE_NZ - 1) // TILE_NZ) + 8, **f64),
         )
-        if ens.tensor_cores:
+        if ens.tensor_cores and not ens.dct:
             # the operand pair describes the stored float32 field, exactly as
             # the device refresh (axi_rigid_refresh_operands) computes it
             whi, wlo = tf32_split(np.asarray(w0, dtype=np.float32))
             t["omega_hi"] = torch.tensor(whi, device=dev)
             t["omega_lo"] = torch.tensor(wlo, device=dev)
+        if ens.tensor_cores:
             t["tc_work"] = [torch.zeros(c.nr * c.nz, dtype=torch.float32, device=dev)
                             for _ in range(4)]
         self.fields = t
@@ -242,12 +281,15 @@ class CaseState:
         for name, v in b.t.items():
             setattr(s, name, v.data_ptr())
         if ens.tensor_cores:
-            s.omega_hi = t["omega_hi"].data_ptr()
-            s.omega_lo = t["omega_lo"].data_ptr()
+            if not ens.dct:
+                s.omega_hi = t["omega_hi"].data_ptr()
+                s.omega_lo = t["omega_lo"].data_ptr()
             for q in range(8):
-                s.tc_basis[q] = b.tc[q].data_ptr()
+                s.tc_basis[q] = b.tc[q].data_ptr() if b.tc[q] is not None else None
             for q in range(4):
                 s.tc_work[q] = t["tc_work"][q].data_ptr()
+        if ens.dct:
+            s.dct_table = b.dct_table.data_ptr()
         s.state = st.data_ptr()
         if self.history is not None:
             s.history = self.history.data_ptr()
@@ -267,18 +309,26 @@ class RigidEnsemble:
     step. Cases may join (add_case) and leave (remove_case) between steps."""
 
     def __init__(self, cases, precision="f64", device="cuda", history_steps=0,
-                 initial_vorticity=None, tensor_cores=None, capacity=None):
+                 initial_vorticity=None, tensor_cores=None, capacity=None, dct=None):
         if precision not in ("f64", "f32"):
             raise ValueError("precision must be 'f64' or 'f32'")
         if tensor_cores is None:
             tensor_cores = precision == "f32"
         if tensor_cores and precision != "f32":
             raise ValueError("tensor-core products are for the f32 engine")
+        cases = list(cases)
+        if dct is None:
+            # opt-in: the shared-memory DCT kernels are correct but, as
+            # measured on the 64-case ensemble, slower than the dense
+            # tensor-core z products
+            dct = False
+        if dct and not tensor_cores:
+            raise ValueError("the DCT z transform goes with the tensor-core products")
         self.tensor_cores = tensor_cores
+        self.dct = dct
         self.precision = precision
         self.dtype = torch.float64 if precision == "f64" else torch.float32
         self.device = torch.device(device)
-        cases = list(cases)
         capacity = max(capacity or 0, len(cases), 1)
         self.state_arena = torch.zeros((capacity, ST_WORDS), dtype=torch.float64,
                                        device=self.device)
@@ -298,12 +348,15 @@ class RigidEnsemble:
         key = (c.nr, c.nz, c.dx)
         if key not in self._bases:
             self._bases[key] = _Bases(c.nr, c.nz, c.dx, self.dtype, self.device,
-                                      tensor_cores=self.tensor_cores)
+                                      tensor_cores=self.tensor_cores, dct=self.dct)
         return self._bases[key]
 
     def _admit(self, case, history_steps=0, initial_vorticity=None):
         if not self._free:
             raise RuntimeError("ensemble is at capacity")
+        if self.dct and not dct_ok(case.nz):
+            raise ValueError(f"nz = {case.nz} has no DCT plan (even, factors 2 and 3 only); "
+                             "build the ensemble with dct=False for such grids")
         m = CaseState(self, case, self._free.pop(), history_steps, initial_vorticity)
         self.members.append(m)
         return m
@@ -338,8 +391,8 @@ class RigidEnsemble:
             return
         lib = N.lib()
         esize = 8 if self.precision == "f64" else 4
-        N.check(lib.axi_plan_init(ctypes.addressof(self.structs), n, esize,
-                                  PLAN_TENSOR_CORES if self.tensor_cores else 0,
+        flags = (PLAN_TENSOR_CORES if self.tensor_cores else 0) | (PLAN_DCT_Z if self.dct else 0)
+        N.check(lib.axi_plan_init(ctypes.addressof(self.structs), n, esize, flags,
                                   ctypes.byref(self.info)), "plan_init")
         self.n_tiles = self.info.n_stencil_tiles
         self.plan = torch.empty(int(self.info.bytes), dtype=torch.uint8, device=self.device)
@@ -396,6 +449,8 @@ class RigidEnsemble:
                               int(n), ctypes.c_void_p(s.cuda_stream)), "rigid_step")
 
     PHASES = ("kill", "transform", "vel_max", "penalise", "advect_diffuse")
+    # the four launches of "transform" (phase ids 5..8), for timing
+    TRANSFORM_PARTS = ("z_forward", "r_product", "z_inverse", "r_product_2")
 
     def phase(self, ph, stream=None):
         """Run one phase of a step (see PHASES); all six in order = one step."""

@@ -157,6 +157,33 @@ def test_host_pipeline_matches_single_ensemble(precision):
             row += 1
 
 
+def test_engine_dct_z_transform_tracks_fp64():
+    """The FP32 engine with the z products as DCTs (dct=True) against the
+    FP64 engine, and no worse than the dense tensor-core form."""
+    from pyaxisymflow_gb300.engine import RigidBodyCase, RigidEnsemble
+    cases = [RigidBodyCase(nz=256, nr=128, dx=2.0 / 256, r_sphere=0.0625, seed=3),
+             RigidBodyCase(nz=192, nr=96, dx=2.0 / 192, r_sphere=0.08, seed=4)]
+    ref = RigidEnsemble(cases, precision="f64")
+    dct = RigidEnsemble(cases, precision="f32", dct=True)
+    dense = RigidEnsemble(cases, precision="f32", dct=False)
+    assert dct.dct and not dense.dct
+    for e in (ref, dct, dense):
+        e.step(30)
+    torch.cuda.synchronize()
+    assert not dct.status().any()
+    for k in range(len(cases)):
+        for f in ("omega", "psi", "u_z", "u_r"):
+            y = ref.fields[k][f].double().cpu().numpy()
+            e_dct = rel_l2(dct.fields[k][f].double().cpu().numpy(), y)
+            e_dense = rel_l2(dense.fields[k][f].double().cpu().numpy(), y)
+            assert e_dct < 1e-5, (k, f, e_dct, e_dense)
+            assert e_dct < 2 * e_dense + 1e-6, (k, f, e_dct, e_dense)
+    # a grid the transform cannot take is refused
+    with pytest.raises(ValueError, match="no DCT plan"):
+        RigidEnsemble([RigidBodyCase(nz=100, nr=48, dx=2.0 / 100, r_sphere=0.1)],
+                      precision="f32", dct=True)
+
+
 def test_engine_f32_error_vs_fp64_oracle():
     from pyaxisymflow_gb300.engine import RigidBodyCase, RigidEnsemble
     c = RigidBodyCase(nz=256, nr=128, dx=2.0 / 256, r_sphere=0.0625)
