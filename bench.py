@@ -242,7 +242,8 @@ def run_gb300(args, world, rank, local):
     dev = torch.device("cuda", local)
     _native.lib()
     cases = ensemble_cases(args.workload)
-    ens = RigidEnsemble(cases, precision=args.precision, device=dev)
+    zopt = {} if args.z_transform == "default" else {"dct": args.z_transform == "dct"}
+    ens = RigidEnsemble(cases, precision=args.precision, device=dev, **zopt)
     cells = ens.cells()
     stream = torch.cuda.current_stream(dev)
     ens.capture(1)
@@ -300,7 +301,7 @@ def run_gb300(args, world, rank, local):
     # every case's vorticity in pinned host memory; each step copies it in,
     # advances every case and copies it and the state blocks (dt, Cd) back,
     # with the transfers of 4 case groups overlapped with their computation
-    pipe = HostPipeline(cases, groups=4, precision=args.precision, device=dev)
+    pipe = HostPipeline(cases, groups=4, precision=args.precision, device=dev, **zopt)
     host_w = pipe.host_buffer()
     host_state = torch.empty((len(cases), ST_WORDS), dtype=torch.float64, pin_memory=True)
     for _ in range(2):
@@ -709,6 +710,8 @@ def main():
     ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--z-transform", default="default", choices=["default", "dense", "dct"],
+                    help="FP32 engine: z products as dense tensor-core GEMMs or as DCTs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

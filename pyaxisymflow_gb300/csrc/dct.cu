@@ -94,6 +94,9 @@ __device__ __forceinline__ void store_split(const DctJob& job, int k, int i, flo
 
 template <int N>
 __device__ void dct_item_fixed(const DctJob& job, int row0, bool forward, float2* a, float2* b);
+template <int N>
+__device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* dsm,
+                             const float2* tw);
 
 __global__ void __launch_bounds__(THREADS) dct_rows_kernel(const DctJob* __restrict__ jobs,
                                                            const int4* __restrict__ items,
@@ -101,15 +104,16 @@ __global__ void __launch_bounds__(THREADS) dct_rows_kernel(const DctJob* __restr
   extern __shared__ __align__(16) float2 dsm[];
   float2* a = dsm;
   float2* b = dsm + ELEMS;
-  float2* tws = dsm + 2 * ELEMS;
   __shared__ DctJob sjob;
   const int4 it = items[blockIdx.x];
   if (threadIdx.x == 0) sjob = jobs[it.x];
   __syncthreads();
-  // the twiddle table of this row length, staged once per block (every
-  // thread takes the global pointer before thread 0 repoints the copy)
+  // the twiddle table of this row length, staged once per block at the end
+  // of shared memory (every thread takes the global pointer before thread 0
+  // repoints the copy)
   const float2* gtw = sjob.twiddle;
   const int n_tw = sjob.N;
+  float2* tws = dsm + 3 * ELEMS - n_tw;
   __syncthreads();
   if (threadIdx.x == 0) sjob.twiddle = tws;
   for (int m = threadIdx.x; m < n_tw; m += blockDim.x) tws[m] = __ldg(gtw + m);
@@ -118,10 +122,10 @@ __global__ void __launch_bounds__(THREADS) dct_rows_kernel(const DctJob* __restr
   const int N = job.N, half = N / 2;
   const int row0 = it.y;
   switch (N) {
-    case 256: dct_item_fixed<256>(job, row0, forward != 0, a, b); return;
-    case 512: dct_item_fixed<512>(job, row0, forward != 0, a, b); return;
-    case 768: dct_item_fixed<768>(job, row0, forward != 0, a, b); return;
-    case 1024: dct_item_fixed<1024>(job, row0, forward != 0, a, b); return;
+    case 256: dct_item_reg<256>(job, row0, forward != 0, dsm, tws); return;
+    case 512: dct_item_reg<512>(job, row0, forward != 0, dsm, tws); return;
+    case 768: dct_item_reg<768>(job, row0, forward != 0, dsm, tws); return;
+    case 1024: dct_item_reg<1024>(job, row0, forward != 0, dsm, tws); return;
     case 1536: dct_item_fixed<1536>(job, row0, forward != 0, a, b); return;
     case 2048: dct_item_fixed<2048>(job, row0, forward != 0, a, b); return;
     default: break;
@@ -305,12 +309,227 @@ __device__ void dct_item_fixed(const DctJob& job, int row0, bool forward, float2
   }
 }
 
+// ---------------------------------------------------------------------------
+// Register-resident FFT: decimation in frequency over a register array with
+// compile-time indices (radix 3 first, then 2). Output position p holds
+// X[dif_index(L, p)].
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int dif_radix(int L) { return (L % 3 == 0) ? 3 : 2; }
+__host__ __device__ constexpr int dif_index(int L, int p) {
+  return L == 1 ? 0
+                : (p / (L / dif_radix(L))) +
+                      dif_radix(L) * dif_index(L / dif_radix(L), p % (L / dif_radix(L)));
+}
+
+// dif_index(L, p) for all p, evaluated at compile time.
+template <int L>
+struct DifPerm {
+  int v[L];
+  __host__ __device__ constexpr DifPerm() : v() {
+    for (int p = 0; p < L; ++p) v[p] = dif_index(L, p);
+  }
+};
+
+// Sub-transform of length L at offset OFF of the register array v (size TOT);
+// tw: exp(-2 pi i m / NT), m < NT, in shared memory.
+template <int TOT, int L, int OFF, int NT, bool FWD>
+__device__ __forceinline__ void dif_rec(float2 (&v)[TOT], const float2* tw) {
+  if constexpr (L > 1) {
+    constexpr int R = dif_radix(L);
+    constexpr int L1 = L / R;
+#pragma unroll
+    for (int j = 0; j < L1; ++j) {
+      float2 o[R];
+      if constexpr (R == 2) {
+        const float2 a0 = v[OFF + j], a1 = v[OFF + j + L1];
+        o[0] = cadd(a0, a1);
+        o[1] = csub(a0, a1);
+      } else {
+        const float h = 0.86602540378443864676f;
+        const float2 a0 = v[OFF + j], a1 = v[OFF + j + L1], a2 = v[OFF + j + 2 * L1];
+        const float2 t1 = cadd(a1, a2), t2 = csub(a1, a2);
+        const float2 m = make_float2(a0.x - 0.5f * t1.x, a0.y - 0.5f * t1.y);
+        const float2 r = FWD ? make_float2(h * t2.y, -h * t2.x) : make_float2(-h * t2.y, h * t2.x);
+        o[0] = cadd(a0, t1);
+        o[1] = cadd(m, r);
+        o[2] = csub(m, r);
+      }
+      v[OFF + j] = o[0];
+#pragma unroll
+      for (int q = 1; q < R; ++q) {
+        if (j == 0) {
+          v[OFF + j + q * L1] = o[q];
+        } else {
+          float2 w = tw[j * q * (NT / L)];
+          if (!FWD) w = conj2(w);
+          v[OFF + j + q * L1] = cmul(o[q], w);
+        }
+      }
+    }
+    dif_rec<TOT, L1, OFF, NT, FWD>(v, tw);
+    dif_rec<TOT, L1, OFF + L1, NT, FWD>(v, tw);
+    if constexpr (R == 3) dif_rec<TOT, L1, OFF + 2 * L1, NT, FWD>(v, tw);
+  }
+}
+
+// Four-step FFT of one complex row of length N = N1 x N2 held by one warp in
+// `buf` (N + N1 complex values): input in natural order, output in natural
+// order (in buf[0, N)). x[N2 n1 + n2] -> X[k1 + N1 k2]. With N1, N2 <= 32
+// every lane has at most one transform per pass; all lanes reach every
+// __syncwarp.
+template <int N, int N1, bool FWD>
+__device__ __forceinline__ void warp_fft(float2* buf, const float2* tw, int lane) {
+  constexpr int N2 = N / N1;
+  constexpr int P = N2 + 1;  // padded row stride between the passes
+  static_assert(N1 <= 32 && N2 <= 32 && N1 * N2 == N, "four-step split");
+  constexpr DifPerm<N1> perm1{};
+  constexpr DifPerm<N2> perm2{};
+  // pass 1: the length-N1 transform over n1 for n2 = lane
+  const int n2 = lane;
+  float2 v[N1];
+  if (n2 < N2) {
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) v[n1] = buf[N2 * n1 + n2];
+    dif_rec<N1, N1, 0, N, FWD>(v, tw);
+  }
+  __syncwarp();
+  if (n2 < N2) {
+    // twiddle exp(-+2 pi i n2 k1 / N), stored as [k1][n2]
+#pragma unroll
+    for (int p = 0; p < N1; ++p) {
+      const int k1 = perm1.v[p];
+      float2 w = tw[n2 * k1];
+      if (!FWD) w = conj2(w);
+      buf[k1 * P + n2] = n2 == 0 ? v[p] : cmul(v[p], w);
+    }
+  }
+  __syncwarp();
+  // pass 2: the length-N2 transform over n2 for k1 = lane
+  const int k1 = lane;
+  float2 o[N2];
+  if (k1 < N1) {
+#pragma unroll
+    for (int m = 0; m < N2; ++m) o[m] = buf[k1 * P + m];
+    dif_rec<N2, N2, 0, N, FWD>(o, tw);
+  }
+  __syncwarp();
+  if (k1 < N1) {
+#pragma unroll
+    for (int p = 0; p < N2; ++p) buf[k1 + N1 * perm2.v[p]] = o[p];
+  }
+  __syncwarp();
+}
+
+// Z = V_a + i V_b for two real rows packed as (a, b): V[k] = exp(i pi k / 2N)
+// (X[k] - i X[N-k]) per row, x = X[k], y = X[N-k].
+__device__ __forceinline__ float2 inverse_pre(float2 cs, float2 x, float2 y) {
+  const float2 va = make_float2(cs.x * x.x + cs.y * y.x, cs.y * x.x - cs.x * y.x);
+  const float2 vb = make_float2(cs.x * x.y + cs.y * y.y, cs.y * x.y - cs.x * y.y);
+  return make_float2(va.x - vb.y, va.y + vb.x);
+}
+
+// Work item of the register path: warp w transforms real rows 2w, 2w + 1 of
+// the item as one complex row in its own buffer; the block then stores the
+// results transposed (rows fastest).
+template <int N>
+__device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* dsm,
+                             const float2* tw) {
+  constexpr int N1 = reg_n1(N);
+  constexpr int W = reg_warps(N);
+  constexpr int BUF = N + N1 + 1;
+  constexpr int RR = 2 * W;  // real rows of a full item
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nrows = min(2 * W, job.rows - row0);  // real rows of this item
+  const int ra = 2 * warp, rb = ra + 1;
+  if (warp < W) {
+    float2* buf = dsm + warp * BUF;
+    const bool has_a = ra < nrows, has_b = rb < nrows;
+    const float* ia = job.in + (long long)(row0 + ra) * N;
+    const float* ib = job.in + (long long)(row0 + rb) * N;
+    // rows are read as float4 (N a multiple of 4, rows 16-byte aligned), all
+    // loads of a lane issued before their first use
+    constexpr int NV = N / 128;  // float4 per lane per row
+    const float4* va4 = reinterpret_cast<const float4*>(ia);
+    const float4* vb4 = reinterpret_cast<const float4*>(ib);
+    float4 xa[NV], xb[NV];
+#pragma unroll
+    for (int m = 0; m < NV; ++m) {
+      xa[m] = has_a ? va4[lane + 32 * m] : make_float4(0.f, 0.f, 0.f, 0.f);
+      xb[m] = has_b ? vb4[lane + 32 * m] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if (forward) {
+      // z[n] = v_a[n] + i v_b[n], v[n] = x[2n], v[N-1-n] = x[2n+1]
+#pragma unroll
+      for (int m = 0; m < NV; ++m) {
+        const int p = 4 * (lane + 32 * m);  // even
+        const int h = p >> 1;
+        buf[h] = make_float2(xa[m].x, xb[m].x);
+        buf[N - 1 - h] = make_float2(xa[m].y, xb[m].y);
+        buf[h + 1] = make_float2(xa[m].z, xb[m].z);
+        buf[N - 2 - h] = make_float2(xa[m].w, xb[m].w);
+      }
+      __syncwarp();
+      warp_fft<N, N1, true>(buf, tw, lane);
+    } else {
+      // X = Y / c_k; Z[k] = V_a[k] + i V_b[k], V[k] = exp(i pi k / 2N) (X[k] - i X[N-k])
+      const float4* sc4 = reinterpret_cast<const float4*>(job.scale);
+#pragma unroll
+      for (int m = 0; m < NV; ++m) {
+        const float4 sc = __ldg(sc4 + lane + 32 * m);
+        const int k = 4 * (lane + 32 * m);
+        buf[k] = make_float2(xa[m].x * sc.x, xb[m].x * sc.x);
+        buf[k + 1] = make_float2(xa[m].y * sc.y, xb[m].y * sc.y);
+        buf[k + 2] = make_float2(xa[m].z * sc.z, xb[m].z * sc.z);
+        buf[k + 3] = make_float2(xa[m].w * sc.w, xb[m].w * sc.w);
+      }
+      __syncwarp();
+      // Z[k] and Z[N-k] both depend on X[k] and X[N-k] only: each lane
+      // rewrites its own pairs in place
+      for (int k = lane; k <= N / 2; k += 32) {
+        const float2 xk = buf[k];
+        const float2 xn = k == 0 ? make_float2(0.0f, 0.0f) : buf[N - k];
+        const float2 zk = inverse_pre(job.rot[k], xk, xn);
+        if (k != 0 && k != N / 2) buf[N - k] = inverse_pre(job.rot[N - k], xn, xk);
+        buf[k] = zk;
+      }
+      __syncwarp();
+      warp_fft<N, N1, false>(buf, tw, lane);
+    }
+  }
+  __syncthreads();
+  if (forward) {
+    for (int t = threadIdx.x; t < RR * N; t += blockDim.x) {
+      const int k = t / RR, r = t - k * RR;
+      if (r >= nrows) continue;
+      const float2* z = dsm + (r >> 1) * BUF;
+      const float2 zk = z[k], zn = z[k == 0 ? 0 : N - k];
+      float2 V;
+      if (r & 1)
+        V = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
+      else
+        V = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+      const float2 cs = job.rot[k];
+      store_split(job, k, row0 + r, job.scale[k] * (V.x * cs.x + V.y * cs.y));
+    }
+  } else {
+    const float inv_n = 1.0f / (float)N;
+    for (int t = threadIdx.x; t < RR * N; t += blockDim.x) {
+      const int j = t / RR, r = t - j * RR;
+      if (r >= nrows) continue;
+      const int src = (j & 1) ? N - 1 - (j >> 1) : (j >> 1);
+      const float2 zv = dsm[(r >> 1) * BUF + src];
+      store_split(job, j, row0 + r, ((r & 1) ? zv.y : zv.x) * inv_n);
+    }
+  }
+}
+
 }  // namespace
 
 // Rows per work item: specialised lengths pack two real rows per complex row.
 int rows_for(int N) {
+  if (reg_n1(N)) return 2 * reg_warps(N);
   switch (N) {
-    case 256: case 512: case 768: case 1024: case 1536: case 2048:
+    case 1536: case 2048:
       return 2 * (ELEMS / N);
     default:
       return rows_per_item(N);

@@ -23,7 +23,7 @@ namespace axi_dct {
 
 constexpr int MAX_STAGES = 16;
 constexpr int ELEMS = 4096;                      // complex values per shared buffer
-constexpr int THREADS = 512;
+constexpr int THREADS = 256;
 // two ping-pong buffers of float2 and the twiddle table (N <= ELEMS)
 constexpr int SMEM_BYTES = 3 * ELEMS * 8;
 
@@ -43,6 +43,22 @@ struct DctJob {
 
 // Rows one work item of the generic path transforms for a row length N.
 __host__ __device__ inline int rows_per_item(int N) { return ELEMS / N > 0 ? ELEMS / N : 1; }
+
+// Register-resident four-step FFT lengths N = N1 x N2 (one warp per pair
+// of real rows): N1 of the first pass, 0 when N has no such path.
+__host__ __device__ constexpr int reg_n1(int N) {
+  return N == 256 ? 16 : N == 512 ? 16 : N == 768 ? 24 : N == 1024 ? 32 : 0;
+}
+// Warps (pairs of real rows) per work item of the register path: each warp
+// holds N + N1 + 1 complex values (odd stride: the buffers of different
+// warps start in different banks) in shared memory next to the N-entry
+// twiddle table, within 3 x ELEMS complex values.
+__host__ __device__ constexpr int reg_warps(int N) {
+  return reg_n1(N) == 0 ? 0
+                        : ((3 * ELEMS - N) / (N + reg_n1(N) + 1) < THREADS / 32
+                               ? (3 * ELEMS - N) / (N + reg_n1(N) + 1)
+                               : THREADS / 32);
+}
 
 // Host: rows per work item for row length N (lengths with a specialised
 // kernel pack two real rows per complex transform).

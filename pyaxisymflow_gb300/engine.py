@@ -318,10 +318,9 @@ class RigidEnsemble:
             raise ValueError("tensor-core products are for the f32 engine")
         cases = list(cases)
         if dct is None:
-            # opt-in: the shared-memory DCT kernels are correct but, as
-            # measured on the 64-case ensemble, slower than the dense
-            # tensor-core z products
-            dct = False
+            # z products as DCTs when every case's nz allows it (faster than
+            # the dense tensor-core z products on the 64-case ensemble)
+            dct = tensor_cores and all(dct_ok(c.nz) for c in cases)
         if dct and not tensor_cores:
             raise ValueError("the DCT z transform goes with the tensor-core products")
         self.tensor_cores = tensor_cores

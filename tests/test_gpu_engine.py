@@ -178,10 +178,11 @@ def test_engine_dct_z_transform_tracks_fp64():
             e_dense = rel_l2(dense.fields[k][f].double().cpu().numpy(), y)
             assert e_dct < 1e-5, (k, f, e_dct, e_dense)
             assert e_dct < 2 * e_dense + 1e-6, (k, f, e_dct, e_dense)
-    # a grid the transform cannot take is refused
+    # a grid the transform cannot take is refused, and by default falls back
+    odd = RigidBodyCase(nz=100, nr=48, dx=2.0 / 100, r_sphere=0.1)
     with pytest.raises(ValueError, match="no DCT plan"):
-        RigidEnsemble([RigidBodyCase(nz=100, nr=48, dx=2.0 / 100, r_sphere=0.1)],
-                      precision="f32", dct=True)
+        RigidEnsemble([odd], precision="f32", dct=True)
+    assert not RigidEnsemble([odd], precision="f32").dct
 
 
 def test_engine_f32_error_vs_fp64_oracle():
