@@ -153,7 +153,10 @@ __global__ void __launch_bounds__(THREADS) dct_rows_kernel(const DctJob* __restr
     float* xs = reinterpret_cast<float*>(b);
     for (int t = threadIdx.x; t < nrows * N; t += blockDim.x) {
       const int r = t / N, k = t - r * N;
-      xs[r * N + k] = job.in[(long long)(row0 + r) * N + k] * job.scale[k];
+      const long long g = (long long)(row0 + r) * N + k;
+      float y = job.in[g];
+      if (job.row_scale) y = y * job.row_scale[g];
+      xs[r * N + k] = y * job.scale[k];
     }
     __syncthreads();
     for (int t = threadIdx.x; t < nrows * N; t += blockDim.x) {
@@ -282,7 +285,10 @@ __device__ void dct_item_fixed(const DctJob& job, int row0, bool forward, float2
     float* xs = reinterpret_cast<float*>(b);
     for (int t = threadIdx.x; t < ncrows * 2 * N; t += blockDim.x) {
       const int r = t / N, k = t - r * N;
-      xs[r * N + k] = r < nrows ? job.in[(long long)(row0 + r) * N + k] * job.scale[k] : 0.0f;
+      const long long g = (long long)(row0 + r) * N + k;
+      float y = r < nrows ? job.in[g] : 0.0f;
+      if (job.row_scale && r < nrows) y = y * job.row_scale[g];
+      xs[r * N + k] = y * job.scale[k];
     }
     __syncthreads();
     for (int t = threadIdx.x; t < ncrows * N; t += blockDim.x) {
@@ -473,6 +479,18 @@ __device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* 
     } else {
       // X = Y / c_k; Z[k] = V_a[k] + i V_b[k], V[k] = exp(i pi k / 2N) (X[k] - i X[N-k])
       const float4* sc4 = reinterpret_cast<const float4*>(job.scale);
+      if (job.row_scale) {
+        // Y = G .* inv_eig, elementwise, before 1 / c_k
+        const float4* ra4 = reinterpret_cast<const float4*>(job.row_scale + (long long)(row0 + ra) * N);
+        const float4* rb4 = reinterpret_cast<const float4*>(job.row_scale + (long long)(row0 + rb) * N);
+#pragma unroll
+        for (int m = 0; m < NV; ++m) {
+          const float4 sa = has_a ? __ldg(ra4 + lane + 32 * m) : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float4 sb = has_b ? __ldg(rb4 + lane + 32 * m) : make_float4(0.f, 0.f, 0.f, 0.f);
+          xa[m] = make_float4(xa[m].x * sa.x, xa[m].y * sa.y, xa[m].z * sa.z, xa[m].w * sa.w);
+          xb[m] = make_float4(xb[m].x * sb.x, xb[m].y * sb.y, xb[m].z * sb.z, xb[m].w * sb.w);
+        }
+      }
 #pragma unroll
       for (int m = 0; m < NV; ++m) {
         const float4 sc = __ldg(sc4 + lane + 32 * m);

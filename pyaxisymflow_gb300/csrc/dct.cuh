@@ -39,6 +39,9 @@ struct DctJob {
   const float2* twiddle;       // exp(-2 pi i m / N), m < N
   const float2* rot;           // (cos, sin)(pi k / 2N), k < N
   const float* scale;          // c_k (forward) or 1 / c_k (inverse), k < N
+  const float* row_scale;      // inverse: (rows, N) elementwise factor applied to
+                               // the input before 1 / c_k (the spectral
+                               // inverse), or nullptr
 };
 
 // Rows one work item of the generic path transforms for a row length N.

@@ -1150,10 +1150,11 @@ int build_tc_jobs(const axi_case& k, axi_tc::TcJob job[4], bool dct) {
     AXI_TRY(axi_tc::encode_operand(&job[1].a_lo, b[3], nr, nr, nr));
     AXI_TRY(axi_tc::encode_operand(&job[1].b_hi, w[0], nz, nr, nr));
     AXI_TRY(axi_tc::encode_operand(&job[1].b_lo, w[1], nz, nr, nr));
+    // the inverse spectrum is applied by the inverse transform as it reads
+    // the rows (the same float product), keeping this epilogue a plain store
     job[1].c = w[2];
-    job[1].scale = static_cast<const float*>(k.inv_eig);
     job[1].M = nr; job[1].N = nz; job[1].K = nr; job[1].ldc = nz;
-    job[1].mode = axi_tc::MODE_SCALE;
+    job[1].mode = axi_tc::MODE_PLAIN;
     AXI_TRY(axi_tc::encode_operand(&job[3].a_hi, b[6], nr, nr, nr));
     AXI_TRY(axi_tc::encode_operand(&job[3].a_lo, b[7], nr, nr, nr));
     AXI_TRY(axi_tc::encode_operand(&job[3].b_hi, w[0], nz, nr, nr));
@@ -1219,6 +1220,7 @@ int build_dct_jobs(const axi_case& k, axi_dct::DctJob* fwd, axi_dct::DctJob* inv
   *inv = j;
   inv->in = w[2];
   inv->scale = reinterpret_cast<const float*>(t + (size_t)20 * k.nz);
+  inv->row_scale = static_cast<const float*>(k.inv_eig);
   return AXI_OK;
 }
 
