@@ -98,6 +98,17 @@ template <int N>
 __device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* dsm,
                              const float2* tw);
 
+// Four consecutive outputs of row k (columns i .. i + 3, i a multiple of 4)
+// as the TF32 pair, one float4 store each.
+__device__ __forceinline__ void store_split4(const DctJob& job, int k, int i, const float (&x)[4]) {
+  float hi[4], lo[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) axi_tc::tf32_split(x[q], hi[q], lo[q]);
+  const long long o = (long long)k * job.rows + i;
+  *reinterpret_cast<float4*>(job.out_hi + o) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+  *reinterpret_cast<float4*>(job.out_lo + o) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+}
+
 __global__ void __launch_bounds__(THREADS) dct_rows_kernel(const DctJob* __restrict__ jobs,
                                                            const int4* __restrict__ items,
                                                            int forward) {
@@ -444,6 +455,7 @@ __device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* 
   constexpr int W = reg_warps(N);
   constexpr int BUF = N + N1 + 1;
   constexpr int RR = 2 * W;  // real rows of a full item
+  static_assert(RR % 4 == 0, "float4 output groups");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nrows = min(2 * W, job.rows - row0);  // real rows of this item
   const int ra = 2 * warp, rb = ra + 1;
@@ -515,28 +527,40 @@ __device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* 
     }
   }
   __syncthreads();
+  // transposed stores, four consecutive rows per thread as float4 (rows is a
+  // multiple of 4 and items start at multiples of RR, so both the row count
+  // of an item and the output offsets are multiples of 4)
+  constexpr int G = RR / 4;
   if (forward) {
-    for (int t = threadIdx.x; t < RR * N; t += blockDim.x) {
-      const int k = t / RR, r = t - k * RR;
-      if (r >= nrows) continue;
-      const float2* z = dsm + (r >> 1) * BUF;
-      const float2 zk = z[k], zn = z[k == 0 ? 0 : N - k];
-      float2 V;
-      if (r & 1)
-        V = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
-      else
-        V = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+    for (int t = threadIdx.x; t < G * N; t += blockDim.x) {
+      const int k = t / G, g = t - k * G;
+      const int r0 = 4 * g;
+      if (r0 >= nrows) continue;
       const float2 cs = job.rot[k];
-      store_split(job, k, row0 + r, job.scale[k] * (V.x * cs.x + V.y * cs.y));
+      const float sk = job.scale[k];
+      float x[4];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float2* z = dsm + (2 * g + h) * BUF;
+        const float2 zk = z[k], zn = z[k == 0 ? 0 : N - k];
+        // V_a = (Z[k] + conj Z[N-k]) / 2, V_b = (Z[k] - conj Z[N-k]) / 2i
+        const float2 va = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+        const float2 vb = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
+        x[2 * h] = sk * (va.x * cs.x + va.y * cs.y);
+        x[2 * h + 1] = sk * (vb.x * cs.x + vb.y * cs.y);
+      }
+      store_split4(job, k, row0 + r0, x);
     }
   } else {
     const float inv_n = 1.0f / (float)N;
-    for (int t = threadIdx.x; t < RR * N; t += blockDim.x) {
-      const int j = t / RR, r = t - j * RR;
-      if (r >= nrows) continue;
+    for (int t = threadIdx.x; t < G * N; t += blockDim.x) {
+      const int j = t / G, g = t - j * G;
+      const int r0 = 4 * g;
+      if (r0 >= nrows) continue;
       const int src = (j & 1) ? N - 1 - (j >> 1) : (j >> 1);
-      const float2 zv = dsm[(r >> 1) * BUF + src];
-      store_split(job, j, row0 + r, ((r & 1) ? zv.y : zv.x) * inv_n);
+      const float2 z0 = dsm[(2 * g) * BUF + src], z1 = dsm[(2 * g + 1) * BUF + src];
+      float x[4] = {z0.x * inv_n, z0.y * inv_n, z1.x * inv_n, z1.y * inv_n};
+      store_split4(job, j, row0 + r0, x);
     }
   }
 }
