@@ -185,6 +185,25 @@ def test_engine_dct_z_transform_tracks_fp64():
     assert not RigidEnsemble([odd], precision="f32").dct
 
 
+@pytest.mark.parametrize("nz", [96, 1536, 2048])
+def test_engine_dct_paths_agree_with_dense_products(nz):
+    """The DCT's other kernel paths (generic length 96, shared-memory Stockham
+    for 1536 and 2048) against the dense tensor-core z products."""
+    from pyaxisymflow_gb300.engine import RigidBodyCase, RigidEnsemble
+    c = RigidBodyCase(nz=nz, nr=nz // 2, dx=2.0 / nz, r_sphere=max(0.0625, 8 * 2.0 / nz),
+                      seed=nz)
+    a = RigidEnsemble([c], precision="f32", dct=True)
+    b = RigidEnsemble([c], precision="f32", dct=False)
+    a.step(5)
+    b.step(5)
+    torch.cuda.synchronize()
+    assert not a.status().any()
+    for f in ("psi", "u_z", "u_r", "omega"):
+        x = a.fields[0][f].double().cpu().numpy()
+        y = b.fields[0][f].double().cpu().numpy()
+        assert rel_l2(x, y) < 2e-5, (nz, f, rel_l2(x, y))
+
+
 def test_engine_f32_error_vs_fp64_oracle():
     from pyaxisymflow_gb300.engine import RigidBodyCase, RigidEnsemble
     c = RigidBodyCase(nz=256, nr=128, dx=2.0 / 256, r_sphere=0.0625)
