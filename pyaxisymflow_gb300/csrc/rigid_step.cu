@@ -445,6 +445,7 @@ __device__ __forceinline__ void penalise_point(T uz, T ur, T lc, T ubody, T& pz,
 }
 
 constexpr int PN_SW = TX + 2, PN_SH = TY + 2;  // u_pen - u, halo 1
+constexpr int PN_RB = (TY + 2 + RG - 1) / RG;  // rows per group of the halo-1 march
 template <typename T>
 using PnRing = BoxRing<T, PN_NBUF, 2, PSI_ROWS>;
 template <typename T>
@@ -471,7 +472,6 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 2) penalise_kernel(co
     issued = ring_prologue<PnRing<T>, PN_NBUF, 2>(ring, maps, tiles, n_tiles, which, -2);
   }
   __syncthreads();
-  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
   int it = 0;
   bool ok = true;
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
@@ -510,46 +510,99 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 2) penalise_kernel(co
     T* uzp = F<T>(k.u_z);
     T* urp = F<T>(k.u_r);
     T cd_part = T(0);
-    for (int e = threadIdx.x; e < PN_SH * PN_SW; e += NT) {
-      const int a = e / PN_SW, b = e - a * PN_SW;
-      const int gi = i0 - 1 + a, gj = j0 - 1 + b;
-      T dz = T(0), dr = T(0);
-      if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
-        const T ch = sc[(a + 1) * BOXW + (b + 3)];
-        T uz, ur, pz, pr;
-        velocity_at<T>(k, sp, gi, gj, rowf[0][a], ufree, uz, ur);
-        penalise_point<T>(uz, ur, lamdt * ch, ubody, pz, pr);
-        dz = pz - uz;
-        dr = pr - ur;
-        if (a >= 1 && a <= TY && b >= 1 && b <= TX) {
-          const int c = gi * nz + gj;
-          uzp[c] = pz;
-          urp[c] = pr;
-          // drag / penalisation force integrand r chi (u_z - U_body)
-          // (flow_past_sphere.py:173, compute_forces.py:14)
-          cd_part += rowf[1][a] * ch * (pz - ubody);
+    // Column march (as in advect_diffuse): warp w owns tile columns
+    // 32 (w % 2) .. + 31 and a run of consecutive rows from (w / 2) x rows
+    // per group; psi of the rows above and below stays in registers. The
+    // psi and chi boxes share one layout: point (p, q) of the tile is
+    // element (p + 2) * BOXW + q + 4 of both.
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int qm = (warp & 1) * 32 + lane, grp = warp >> 1;
+    const int gjm = j0 + qm;
+    // u_pen - u at one point of the tile + halo 1 (p in [-1, TY], q in [-1, TX])
+    auto point = [&](int p, int q, T uz, T ur, T ch, int gi, int gj) {
+      T pz, pr;
+      penalise_point<T>(uz, ur, lamdt * ch, ubody, pz, pr);
+      const int d = (p + 1) * PN_SW + (q + 1);
+      duz[d] = pz - uz;
+      dur[d] = pr - ur;
+      if (p >= 0 && p < TY && q >= 0 && q < TX) {
+        const int c = gi * nz + gj;
+        uzp[c] = pz;
+        urp[c] = pr;
+        // drag / penalisation force integrand r chi (u_z - U_body)
+        // (flow_past_sphere.py:173, compute_forces.py:14)
+        cd_part += rowf[1][p + 1] * ch * (pz - ubody);
+      }
+    };
+    {
+      const bool jin = gjm < nz, jint = gjm >= 1 && gjm < nz - 1;
+      const int p0 = -1 + PN_RB * grp;
+      int cb = (p0 + 2) * BOXW + (qm + 4);
+      T pm = ps[cb - BOXW], pc = ps[cb];
+#pragma unroll
+      for (int m = 0; m < PN_RB; ++m, cb += BOXW) {
+        const int pr_ = p0 + m;
+        if (pr_ > TY) break;
+        const T pn = ps[cb + BOXW];
+        const int gi = i0 + pr_;
+        if (jin && gi >= 0 && gi < nr) {
+          const T rv = rowf[0][pr_ + 1];
+          T uz, ur;
+          if (gi == 0 || gi == nr - 1 || !jint) {
+            velocity_at<T>(k, sp, gi, gjm, rv, ufree, uz, ur);
+          } else {
+            uz = (pn - pm) * rv + ufree;
+            ur = -(ps[cb + 1] - ps[cb - 1]) * rv;
+          }
+          point(pr_, qm, uz, ur, sc[cb], gi, gjm);
+        } else {
+          const int d = (pr_ + 1) * PN_SW + (qm + 1);
+          duz[d] = T(0);
+          dur[d] = T(0);
+        }
+        pm = pc;
+        pc = pn;
+      }
+      // halo columns -1 and TX
+      if (threadIdx.x < 2 * PN_SH) {
+        const int pe = -1 + (int)threadIdx.x / 2, qe = (threadIdx.x & 1) ? TX : -1;
+        const int gi = i0 + pe, gj = j0 + qe;
+        if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
+          T uz, ur;
+          velocity_at<T>(k, sp, gi, gj, rowf[0][pe + 1], ufree, uz, ur);
+          point(pe, qe, uz, ur, sc[(pe + 2) * BOXW + (qe + 4)], gi, gj);
+        } else {
+          const int d = (pe + 1) * PN_SW + (qe + 1);
+          duz[d] = T(0);
+          dur[d] = T(0);
         }
       }
-      duz[e] = dz;
-      dur[e] = dr;
     }
-    // omega of the owned cells: all loads issued before the first use
-    T wown[CPT];
+    // omega of the owned cells (column march, rows 8 grp .. 8 grp + 7):
+    // all loads issued before the first use
+    constexpr int RC = TY / RG;
+    const int p0c = RC * grp;
+    T wown[RC];
 #pragma unroll
-    for (int q = 0; q < CPT; ++q) {
-      const int gi = i0 + ty + RG * q, gj = j0 + tx;
-      wown[q] = (gi < nr && gj < nz) ? w[gi * nz + gj] : T(0);
+    for (int m = 0; m < RC; ++m) {
+      const int gi = i0 + p0c + m;
+      wown[m] = (gi < nr && gjm < nz) ? w[gi * nz + gjm] : T(0);
     }
     __syncthreads();
+    {
+      const bool jint = gjm >= 1 && gjm < nz - 1;
+      int d = (p0c + 1) * PN_SW + (qm + 1);
+      T zs = duz[d - PN_SW], zc = duz[d];
 #pragma unroll
-    for (int q = 0; q < CPT; ++q) {
-      const int a = ty + RG * q, b = tx;
-      const int gi = i0 + a, gj = j0 + b;
-      if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
-        const int d = (a + 1) * PN_SW + (b + 1);
-        const T pw =
-            (dur[d + 1] - dur[d - 1]) * inv2dx - (duz[d + PN_SW] - duz[d - PN_SW]) * inv2dx;
-        w[gi * nz + gj] = wown[q] + pw;
+      for (int m = 0; m < RC; ++m, d += PN_SW) {
+        const T zn = duz[d + PN_SW];
+        const int gi = i0 + p0c + m;
+        if (jint && gi >= 1 && gi < nr - 1) {
+          const T pw = (dur[d + 1] - dur[d - 1]) * inv2dx - (zn - zs) * inv2dx;
+          w[gi * nz + gjm] = wown[m] + pw;
+        }
+        zs = zc;
+        zc = zn;
       }
     }
     // drag: thread and warp sums in T, then warps and tiles in double, fixed order
