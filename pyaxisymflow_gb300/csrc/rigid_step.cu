@@ -126,10 +126,22 @@ __device__ __forceinline__ unsigned int dev_tiles_of(const axi_case& k) {
 // ---------------------------------------------------------------------------
 // kill_reset: kernels/kill_boundary_vorticity_sine.py:4-27 (literal 1 - Z,
 // 1 - R), the ramped free stream (flow_past_sphere.py:118-121), counters.
+//
+// The z-edge taper of every row, then the outer-r taper of rows nr - w ..
+// nr - 1 from row nr - w (itself z-tapered first), then row 0 set to zero,
+// computed as one map of the incoming omega. Each output depends only on
+// incoming values that its own thread reads before writing, except the two
+// z-taper sources of row nr - w (columns w - 1 and nz - w), which all 2w
+// edge columns of the outer rows read and two of them overwrite: those edge
+// columns are threads of block 0 that read before a barrier and write after
+// it. Work units of a case: the 2w edge columns, the nz - 2w inner columns
+// (outer rows and row 0), rows 1 .. nr - w - 1 (their two z strips).
 // ---------------------------------------------------------------------------
+constexpr int KILL_BLOCKS = 4;  // blocks per case (grid x)
+
 template <typename T>
-__global__ void kill_reset_kernel(const axi_case* __restrict__ cases) {
-  const axi_case& k = cases[blockIdx.x];
+__global__ void __launch_bounds__(256) kill_reset_kernel(const axi_case* __restrict__ cases) {
+  const axi_case& k = cases[blockIdx.y];
   T* w = F<T>(k.omega);
   const int nr = k.nr, nz = k.nz, wd = k.kill_width;
   // taper factors sin(pi (Z - dx/2) / 2 / (w - 1) / dx) etc., evaluated once on
@@ -137,7 +149,7 @@ __global__ void kill_reset_kernel(const axi_case* __restrict__ cases) {
   const double* cz0 = k.kill_coef;
   const double* cz1 = k.kill_coef + wd;
   const double* cr = k.kill_coef + 2 * wd;
-  if (threadIdx.x == 0) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
     *reinterpret_cast<unsigned long long*>(&k.state[AXI_ST_UMAX]) = 0ull;
     counter(k, 0)[0] = 0u;
     counter(k, 1)[0] = 0u;
@@ -155,19 +167,35 @@ __global__ void kill_reset_kernel(const axi_case* __restrict__ cases) {
     f[SF_RBODY] = (float)k.r_body;
     f[SF_BLENDW] = (float)k.blend_w;
   }
-  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-    const int row = i * nz;
-    const double left = (double)w[row + wd - 1];
-    const double right = (double)w[row + nz - wd];
-    for (int q = 0; q < wd; ++q) store_omega<T>(k, row + q, (T)(cz0[q] * left));
-    for (int q = 0; q < wd; ++q) store_omega<T>(k, row + nz - wd + q, (T)(cz1[q] * right));
-  }
+  const int band = (nr - wd) * nz;  // first outer row
+  // edge columns 0 .. w - 1 and nz - w .. nz - 1 of the outer rows (block 0):
+  // the z-tapered value of row nr - w, rounded to T as the reference stores it
+  const int t = threadIdx.x;
+  const bool edge = blockIdx.x == 0 && t < 2 * wd;
+  const int je = t < wd ? t : nz - 2 * wd + t;
+  double esrc = 0.0;
+  if (edge)
+    esrc = t < wd ? (double)(T)(cz0[t] * (double)w[band + wd - 1])
+                  : (double)(T)(cz1[t - wd] * (double)w[band + nz - wd]);
   __syncthreads();
-  for (int j = threadIdx.x; j < nz; j += blockDim.x) {
-    const double src = (double)w[(nr - wd) * nz + j];
-    for (int q = 0; q < wd; ++q)
-      store_omega<T>(k, (nr - wd + q) * nz + j, (T)(cr[q] * src));
-    store_omega<T>(k, j, T(0));
+  if (edge) {
+    for (int q = 0; q < wd; ++q) store_omega<T>(k, band + q * nz + je, (T)(cr[q] * esrc));
+    store_omega<T>(k, je, T(0));
+  }
+  const int n_units = nz + (nr - wd - 1 > 0 ? nr - wd - 1 : 0);
+  for (int u = 2 * wd + blockIdx.x * blockDim.x + t; u < n_units; u += gridDim.x * blockDim.x) {
+    if (u < nz) {
+      const int j = u - wd;  // inner column w .. nz - w - 1
+      const double src = (double)w[band + j];
+      for (int q = 0; q < wd; ++q) store_omega<T>(k, band + q * nz + j, (T)(cr[q] * src));
+      store_omega<T>(k, j, T(0));
+    } else {
+      const int row = (1 + u - nz) * nz;  // rows 1 .. nr - w - 1
+      const double left = (double)w[row + wd - 1];
+      const double right = (double)w[row + nz - wd];
+      for (int q = 0; q < wd; ++q) store_omega<T>(k, row + q, (T)(cz0[q] * left));
+      for (int q = 0; q < wd; ++q) store_omega<T>(k, row + nz - wd + q, (T)(cz1[q] * right));
+    }
   }
 }
 
@@ -1351,7 +1379,7 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
   const int nt = info->n_stencil_tiles, ng = info->n_gemm_tiles;
   switch (phase) {
     case PH_KILL:
-      kill_reset_kernel<T><<<info->n_cases, 256, 0, s>>>(v.cases);
+      kill_reset_kernel<T><<<dim3(KILL_BLOCKS, info->n_cases), 256, 0, s>>>(v.cases);
       break;
     case PH_TRANSFORM:
       if (v.dct_jobs) {

@@ -554,6 +554,7 @@ class HostPipeline:
         self.ensembles = [RigidEnsemble([cases[k] for k in idx], precision=precision,
                                         device=self.device, **kw) for idx in self.index]
         self.streams = [torch.cuda.Stream(self.device) for _ in self.ensembles]
+        self.graph = None
         self.dtype = self.ensembles[0].dtype
         # one flat host buffer: the groups' arenas back to back
         self.offsets = [0]
@@ -588,8 +589,31 @@ class HostPipeline:
                     n = e.n_cases
                     state_out[row:row + n].copy_(e.state, non_blocking=True)
                     row += n
+        for s in self.streams:
+            cur.wait_stream(s)
+
+    def capture(self, host, state_out=None):
+        """Record step(host, state_out) as one CUDA graph; replay() then issues
+        every group's copies and launches at once (about 0.1 ms of host work
+        per group saved each step). The graph holds the buffers' addresses:
+        host and state_out must stay alive and in place while it is used."""
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.step(host, state_out)
+        torch.cuda.synchronize(self.device)
+        self.graph = g
+        self._graph_buffers = (host, state_out)
+        return g
+
+    def replay(self):
+        """One captured step (asynchronous on the current stream)."""
+        self.graph.replay()
 
     def synchronize(self):
         for s in self.streams:
             s.synchronize()
+        torch.cuda.current_stream(self.device).synchronize()
 

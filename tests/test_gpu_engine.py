@@ -140,9 +140,13 @@ def test_host_pipeline_matches_single_ensemble(precision):
     ref = RigidEnsemble(cases, precision=precision)
     host = pipe.host_buffer()
     state = torch.empty((len(cases), ST_WORDS), dtype=torch.float64, pin_memory=True)
-    for _ in range(3):
+    # two direct steps, then one captured step (capture records without running)
+    for _ in range(2):
         pipe.step(host, state)
         pipe.synchronize()
+    pipe.capture(host, state)
+    pipe.replay()
+    pipe.synchronize()
     ref.step(3)
     torch.cuda.synchronize()
     row = 0
