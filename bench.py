@@ -391,8 +391,9 @@ def run_gb300(args, world, rank, local):
                     "unit": "TFLOP/s", "useful_tflops": achieved,
                     "peak_source": f"{src} bf16 / 2 (TF32 dense rate)"}
     elif dom == "z_transforms":
-        # per transform: read the rows (4 B), write the TF32 pair (8 B)
-        nbytes = sum(2 * 12.0 * c.nr * c.nz for c in cases)
+        # forward: read the rows (4 B), write the TF32 pair (8 B); inverse: read
+        # the rows and the spectral factor (4 + 4 B), write the pair (8 B)
+        nbytes = sum(28.0 * c.nr * c.nz for c in cases)
         achieved = nbytes / (kern_ms[dom] / 1000.0) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "peak_source": f"{src} hbm"}

@@ -124,10 +124,13 @@ __global__ void __launch_bounds__(THREADS) dct_rows_kernel(const DctJob* __restr
   // repoints the copy)
   const float2* gtw = sjob.twiddle;
   const int n_tw = sjob.N;
-  float2* tws = dsm + 3 * ELEMS - n_tw;
+  // the register path reads the table padded (reg_tw_index)
+  const bool padded = reg_n1(n_tw) != 0;
+  float2* tws = dsm + 3 * ELEMS - (padded ? reg_tw_size(n_tw) : n_tw);
   __syncthreads();
   if (threadIdx.x == 0) sjob.twiddle = tws;
-  for (int m = threadIdx.x; m < n_tw; m += blockDim.x) tws[m] = __ldg(gtw + m);
+  for (int m = threadIdx.x; m < n_tw; m += blockDim.x)
+    tws[padded ? reg_tw_index(m) : m] = __ldg(gtw + m);
   __syncthreads();
   const DctJob& job = sjob;
   const int N = job.N, half = N / 2;
@@ -348,7 +351,7 @@ struct DifPerm {
 };
 
 // Sub-transform of length L at offset OFF of the register array v (size TOT);
-// tw: exp(-2 pi i m / NT), m < NT, in shared memory.
+// tw: exp(-2 pi i m / NT), m < NT, in shared memory at reg_tw_index(m).
 template <int TOT, int L, int OFF, int NT, bool FWD>
 __device__ __forceinline__ void dif_rec(float2 (&v)[TOT], const float2* tw) {
   if constexpr (L > 1) {
@@ -377,7 +380,7 @@ __device__ __forceinline__ void dif_rec(float2 (&v)[TOT], const float2* tw) {
         if (j == 0) {
           v[OFF + j + q * L1] = o[q];
         } else {
-          float2 w = tw[j * q * (NT / L)];
+          float2 w = tw[reg_tw_index(j * q * (NT / L))];
           if (!FWD) w = conj2(w);
           v[OFF + j + q * L1] = cmul(o[q], w);
         }
@@ -415,7 +418,7 @@ __device__ __forceinline__ void warp_fft(float2* buf, const float2* tw, int lane
 #pragma unroll
     for (int p = 0; p < N1; ++p) {
       const int k1 = perm1.v[p];
-      float2 w = tw[n2 * k1];
+      float2 w = tw[reg_tw_index(n2 * k1)];
       if (!FWD) w = conj2(w);
       buf[k1 * P + n2] = n2 == 0 ? v[p] : cmul(v[p], w);
     }
@@ -453,7 +456,8 @@ __device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* 
                              const float2* tw) {
   constexpr int N1 = reg_n1(N);
   constexpr int W = reg_warps(N);
-  constexpr int BUF = N + N1 + 1;
+  constexpr int BUF = reg_buf(N);
+  static_assert(BUF >= N + N1 - 1 && BUF % 16 == 2, "warp buffer stride");
   constexpr int RR = 2 * W;  // real rows of a full item
   static_assert(RR % 4 == 0, "float4 output groups");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -477,14 +481,15 @@ __device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* 
     }
     if (forward) {
       // z[n] = v_a[n] + i v_b[n], v[n] = x[2n], v[N-1-n] = x[2n+1]
+      // (h, h + 1) and (N - 2 - h, N - 1 - h) are 16-byte aligned pairs (h
+      // even, buffers 16-byte aligned): one float4 store each
 #pragma unroll
       for (int m = 0; m < NV; ++m) {
         const int p = 4 * (lane + 32 * m);  // even
         const int h = p >> 1;
-        buf[h] = make_float2(xa[m].x, xb[m].x);
-        buf[N - 1 - h] = make_float2(xa[m].y, xb[m].y);
-        buf[h + 1] = make_float2(xa[m].z, xb[m].z);
-        buf[N - 2 - h] = make_float2(xa[m].w, xb[m].w);
+        *reinterpret_cast<float4*>(buf + h) = make_float4(xa[m].x, xb[m].x, xa[m].z, xb[m].z);
+        *reinterpret_cast<float4*>(buf + N - 2 - h) =
+            make_float4(xa[m].w, xb[m].w, xa[m].y, xb[m].y);
       }
       __syncwarp();
       warp_fft<N, N1, true>(buf, tw, lane);
@@ -507,10 +512,10 @@ __device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* 
       for (int m = 0; m < NV; ++m) {
         const float4 sc = __ldg(sc4 + lane + 32 * m);
         const int k = 4 * (lane + 32 * m);
-        buf[k] = make_float2(xa[m].x * sc.x, xb[m].x * sc.x);
-        buf[k + 1] = make_float2(xa[m].y * sc.y, xb[m].y * sc.y);
-        buf[k + 2] = make_float2(xa[m].z * sc.z, xb[m].z * sc.z);
-        buf[k + 3] = make_float2(xa[m].w * sc.w, xb[m].w * sc.w);
+        *reinterpret_cast<float4*>(buf + k) =
+            make_float4(xa[m].x * sc.x, xb[m].x * sc.x, xa[m].y * sc.y, xb[m].y * sc.y);
+        *reinterpret_cast<float4*>(buf + k + 2) =
+            make_float4(xa[m].z * sc.z, xb[m].z * sc.z, xa[m].w * sc.w, xb[m].w * sc.w);
       }
       __syncwarp();
       // Z[k] and Z[N-k] both depend on X[k] and X[N-k] only: each lane

@@ -52,14 +52,24 @@ __host__ __device__ inline int rows_per_item(int N) { return ELEMS / N > 0 ? ELE
 __host__ __device__ constexpr int reg_n1(int N) {
   return N == 256 ? 16 : N == 512 ? 16 : N == 768 ? 24 : N == 1024 ? 32 : 0;
 }
-// Warps (pairs of real rows) per work item of the register path: each warp
-// holds N + N1 + 1 complex values (odd stride: the buffers of different
-// warps start in different banks) in shared memory next to the N-entry
-// twiddle table, within 3 x ELEMS complex values.
+// Complex values per warp buffer of the register path: at least the
+// N + N1 - 1 the four-step exchange addresses, rounded up to 2 (mod 16) so
+// that every buffer starts 16-byte aligned and the transposed stores (four
+// rows of one column from two buffers per half-warp) touch distinct banks.
+__host__ __device__ constexpr int reg_buf(int N) {
+  return ((N + reg_n1(N) - 1 - 2 + 15) / 16) * 16 + 2;
+}
+// Twiddle table of the register path: exp(-2 pi i m / N) at index
+// m + m / 16 (one pad entry per 16, so the strided inter-pass reads
+// tw[n2 k1] spread over the banks).
+__host__ __device__ constexpr int reg_tw_index(int m) { return m + (m >> 4); }
+__host__ __device__ constexpr int reg_tw_size(int N) { return N + N / 16; }
+// Warps (pairs of real rows) per work item of the register path: the warp
+// buffers and the padded twiddle table within 3 x ELEMS complex values.
 __host__ __device__ constexpr int reg_warps(int N) {
   return reg_n1(N) == 0 ? 0
-                        : ((3 * ELEMS - N) / (N + reg_n1(N) + 1) < THREADS / 32
-                               ? (3 * ELEMS - N) / (N + reg_n1(N) + 1)
+                        : ((3 * ELEMS - reg_tw_size(N)) / reg_buf(N) < THREADS / 32
+                               ? (3 * ELEMS - reg_tw_size(N)) / reg_buf(N)
                                : THREADS / 32);
 }
 
