@@ -49,7 +49,21 @@ PHASE_FIELDS = {"vel_max": 1, "penalise": 6, "advect_diffuse": 4}
 
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of a phase, from the
 # ncu captures summarised in profiles/ (transform: sum over its four products).
-NCU_TRAFFIC = {}
+# DRAM bytes (read + write) per launch of each step kernel, ensemble64 FP32
+# engine, from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum,
+# averaged over the launches of two steps)
+NCU_TRAFFIC = {
+    ("ensemble64", "f32", "r_products"): 190.2e6,
+    ("ensemble64", "f32", "z_transforms"): 168.5e6,
+    ("ensemble64", "f32", "advect_diffuse"): 325.1e6,
+    ("ensemble64", "f32", "penalise"): 389.1e6,
+    ("ensemble64", "f32", "vel_max"): 74.0e6,
+}
+# remeshing (2048 x 1024 cells, 4.19 M particles): FP64 instructions per
+# particle of the two kernels together (80 + 48) and their DRAM bytes per call
+FP64_INSTR_PER_PARTICLE = 128.0
+FP64_PEAK_GINSTR = 625.0
+P2M_TRAFFIC = 673.2e6
 
 
 def ensemble_cases(workload, seed=4):
@@ -408,7 +422,7 @@ def run_gb300(args, world, rank, local):
     # DRAM bytes (read + write) of the dominant kernel's launches in one step,
     # from the ncu capture summarised in profiles/ (same workload and kernels)
     roof["traffic"] = NCU_TRAFFIC.get((args.workload, args.precision, dom))
-    roof["traffic_unit"] = "bytes per step"
+    roof["traffic_unit"] = "bytes per launch (ncu dram read + write)"
     stencil_bytes = sum(sum(PHASE_FIELDS.values()) * esize * c.nr * c.nz for c in cases)
     stencil_ms = sum(ph_ms[p] for p in PHASE_FIELDS)
     line = {
@@ -674,10 +688,19 @@ def run_remesh(args, world, rank, local):
                    "particles": n_part, "kernel": "MP4, unbounded",
                    "timing": "wall clock per call of the drop-in (it synchronises to check "
                              "particle displacement)"},
-        "roofline": {"bound": "hbm", "kernel": "particles_to_mesh (stencil + gather)",
-                     "achieved": alg / (p2m_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
-                     "frac": alg / (p2m_ms / 1e3) / 1e9 / hbm, "traffic": None,
-                     "peak_source": f"{src} hbm", "p2m_ms": p2m_ms,
+        # bit-exact with the reference's sequential FP64 sums, the two kernels
+        # are FP64-pipe bound: 80 FP64 instructions per particle (two IEEE
+        # divisions, eight MP4 weights) and 48 per mesh point (16 weight
+        # products, multiplies and adds), counted by ncu on this workload
+        "roofline": {"bound": "fp64", "kernel": "particles_to_mesh (stencil + gather)",
+                     "achieved": FP64_INSTR_PER_PARTICLE * n_part / (p2m_ms / 1e3) / 1e9,
+                     "peak": FP64_PEAK_GINSTR, "unit": "G FP64 instructions/s",
+                     "frac": FP64_INSTR_PER_PARTICLE * n_part / (p2m_ms / 1e3) / 1e9
+                     / FP64_PEAK_GINSTR,
+                     "traffic": P2M_TRAFFIC, "traffic_unit": "bytes per call (ncu dram read + write)",
+                     "peak_source": "nominal GB300 FP64, 1.25 TFLOP/s = 625 G DFMA/s",
+                     "p2m_ms": p2m_ms,
+                     "hbm_frac": alg / (p2m_ms / 1e3) / 1e9 / hbm,
                      "algorithmic_bytes": "32 B per particle"},
         "gpu_launches": 3 * args.steps,
         "clocks": clocks.summary(),
