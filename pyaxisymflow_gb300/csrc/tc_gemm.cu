@@ -83,19 +83,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// v already carries the elementwise factor of MODE_SCALE_SPLIT / MODE_SCALE.
-__device__ __forceinline__ void store_value(const TcJob& job, int row, int col, float v) {
-  const long long idx = (long long)row * job.ldc + col;
-  if (job.mode == MODE_PLAIN || job.mode == MODE_SCALE) {
-    job.c[idx] = v;
-    return;
-  }
-  float hi, lo;
-  tf32_split(v, hi, lo);
-  job.c[idx] = hi;
-  job.c_lo[idx] = lo;
-}
-
 // Persistent, warp-specialised kernel (one CTA per SM, tiles strided over the
 // grid): warp 0 issues TMA, warp 1 issues MMAs into one of two TMEM
 // accumulators (2 x 128 columns), warps 2-9 drain the other accumulator, so
@@ -222,7 +209,15 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (!__all_sync(0xffffffffu, ok && *reinterpret_cast<volatile int*>(err) == 0)) break;
       tc_fence_after();
       const int row0 = tr.y + 32 * q;
-      const bool scaled = job.mode == MODE_SCALE_SPLIT || job.mode == MODE_SCALE;
+      // the job's fields in registers for the whole tile (read through the
+      // reference inside the store loop, each store could alias them and
+      // forced a reload per row)
+      float* const c = job.c;
+      float* const c_lo = job.c_lo;
+      const float* const scl = job.scale;
+      const int M = job.M, Nc = job.N, ldc = job.ldc, mode = job.mode;
+      const bool scaled = mode == MODE_SCALE_SPLIT || mode == MODE_SCALE;
+      const bool split = mode == MODE_SPLIT || mode == MODE_SCALE_SPLIT;
 #pragma unroll 1
       for (int cc = half * CHUNKS; cc < (half + 1) * CHUNKS; ++cc) {
         const int col = tr.z + cc * 32 + lane;
@@ -234,9 +229,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
           for (int rr = 0; rr < 32; ++rr) {
             const int row = row0 + rr;
-            sv[rr] = (col < job.N && row < job.M)
-                         ? __ldg(job.scale + (long long)row * job.N + col)
-                         : 0.0f;
+            sv[rr] = (col < Nc && row < M) ? __ldg(scl + (long long)row * Nc + col) : 0.0f;
           }
         }
         uint32_t r[32];
@@ -246,13 +239,23 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
         for (int j = 0; j < 32; ++j) stg[lane * 33 + j] = __uint_as_float(r[j]);
         __syncwarp();
-        if (col < job.N) {
+        if (col < Nc) {
 #pragma unroll
           for (int rr = 0; rr < 32; ++rr) {
             const int row = row0 + rr;
             float v = stg[rr * 33 + lane];
             if (scaled) v *= sv[rr];
-            if (row < job.M) store_value(job, row, col, v);
+            if (row < M) {
+              const long long idx = (long long)row * ldc + col;
+              if (split) {
+                float hi, lo;
+                tf32_split(v, hi, lo);
+                c[idx] = hi;
+                c_lo[idx] = lo;
+              } else {
+                c[idx] = v;
+              }
+            }
           }
         }
         __syncwarp();
