@@ -168,6 +168,21 @@ __global__ void __launch_bounds__(256) kill_reset_kernel(const axi_case* __restr
     f[SF_BLENDW] = (float)k.blend_w;
   }
   const int band = (nr - wd) * nz;  // first outer row
+  // output pointers in registers (a store through a pointer read from the
+  // case record would force the record to be re-read after it)
+  float* const whi = static_cast<float*>(k.omega_hi);
+  float* const wlo = static_cast<float*>(k.omega_lo);
+  auto put = [&](int c, T v) {
+    w[c] = v;
+    if constexpr (sizeof(T) == 4) {
+      if (whi) {
+        float hi, lo;
+        axi_tc::tf32_split((float)v, hi, lo);
+        whi[c] = hi;
+        wlo[c] = lo;
+      }
+    }
+  };
   // edge columns 0 .. w - 1 and nz - w .. nz - 1 of the outer rows (block 0):
   // the z-tapered value of row nr - w, rounded to T as the reference stores it
   const int t = threadIdx.x;
@@ -179,22 +194,22 @@ __global__ void __launch_bounds__(256) kill_reset_kernel(const axi_case* __restr
                   : (double)(T)(cz1[t - wd] * (double)w[band + nz - wd]);
   __syncthreads();
   if (edge) {
-    for (int q = 0; q < wd; ++q) store_omega<T>(k, band + q * nz + je, (T)(cr[q] * esrc));
-    store_omega<T>(k, je, T(0));
+    for (int q = 0; q < wd; ++q) put(band + q * nz + je, (T)(cr[q] * esrc));
+    put(je, T(0));
   }
   const int n_units = nz + (nr - wd - 1 > 0 ? nr - wd - 1 : 0);
   for (int u = 2 * wd + blockIdx.x * blockDim.x + t; u < n_units; u += gridDim.x * blockDim.x) {
     if (u < nz) {
       const int j = u - wd;  // inner column w .. nz - w - 1
       const double src = (double)w[band + j];
-      for (int q = 0; q < wd; ++q) store_omega<T>(k, band + q * nz + j, (T)(cr[q] * src));
-      store_omega<T>(k, j, T(0));
+      for (int q = 0; q < wd; ++q) put(band + q * nz + j, (T)(cr[q] * src));
+      put(j, T(0));
     } else {
       const int row = (1 + u - nz) * nz;  // rows 1 .. nr - w - 1
       const double left = (double)w[row + wd - 1];
       const double right = (double)w[row + nz - wd];
-      for (int q = 0; q < wd; ++q) store_omega<T>(k, row + q, (T)(cz0[q] * left));
-      for (int q = 0; q < wd; ++q) store_omega<T>(k, row + nz - wd + q, (T)(cz1[q] * right));
+      for (int q = 0; q < wd; ++q) put(row + q, (T)(cz0[q] * left));
+      for (int q = 0; q < wd; ++q) put(row + nz - wd + q, (T)(cz1[q] * right));
     }
   }
 }
@@ -934,6 +949,12 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) advect_diffuse_ker
     const bool sediment = (k.flags & AXI_CASE_SEDIMENTING) != 0;
     T cd_part = T(0);
     {
+      // output pointers in registers (stores through pointers read from the
+      // case record would force the record to be re-read after each store)
+      T* const wout = F<T>(k.omega);
+      float* const whi = static_cast<float*>(k.omega_hi);
+      float* const wlo = static_cast<float*>(k.omega_lo);
+      T* const chi = F<T>(k.chi);
       const T zc = scalar<T>(k, SF_ZCM);
       const T rbody = scalar<T>(k, SF_RBODY);
       const T blendw = scalar<T>(k, SF_BLENDW);
@@ -955,13 +976,21 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) advect_diffuse_ker
                           (n_ - s_) * rowf[0][pr + 1] - c_ * rowf[1][pr + 1];
             v = v + c2 * lap;
           }
-          store_omega<T>(k, c, v);
+          wout[c] = v;
+          if constexpr (sizeof(T) == 4) {
+            if (whi) {
+              float hi, lo;
+              axi_tc::tf32_split((float)v, hi, lo);
+              whi[c] = hi;
+              wlo[c] = lo;
+            }
+          }
           if (sediment) {
             // mask at the body position of this step (falling_rigid_sphere.py:156-157),
             // then the drag integrand with the new mask (:164-173)
             const T rr = rowf[2][pr + 1];
             const T ch = sphere_mask<T>(zcol, rr, zc, rbody, blendw);
-            F<T>(k.chi)[c] = ch;
+            chi[c] = ch;
             cd_part += rr * ch * sz[ad_box(pr, qm)];
           }
         }
