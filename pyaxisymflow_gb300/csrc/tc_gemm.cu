@@ -133,8 +133,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       bool ok = true;
       for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
         const int4 tr = tiles[t];
-        const TcJob& job = jobs[tr.x];
-        const int nk = (job.K + BKF - 1) / BKF;
+        const TcJob& job = jobs[tr.x];  // only the tensor maps' addresses are used
+        const int nk = tr.w;
         for (int kb = 0; kb < nk; ++kb, ++g) {
           const int s = g % NSTAGE, use = g / NSTAGE;
           if (use > 0 && !mbar_wait(empty0 + 8 * s, (use - 1) & 1, err, ERR_PRODUCER)) {
@@ -160,9 +160,12 @@ __global__ void __launch_bounds__(THREADS, 1)
       constexpr uint32_t idesc = idesc_tf32(BM, BN);
       int g = 0, it = 0;
       bool ok = true;
+      // k-block count of the next tile, loaded one tile ahead (its latency
+      // would otherwise sit between two tiles' MMAs)
+      int nk_next = blockIdx.x < n_tiles ? tiles[blockIdx.x].w : 0;
       for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x, ++it) {
-        const TcJob& job = jobs[tiles[t].x];
-        const int nk = (job.K + BKF - 1) / BKF;
+        const int nk = nk_next;
+        if (t + (int)gridDim.x < n_tiles) nk_next = tiles[t + gridDim.x].w;
         const int buf = it & 1, ause = it >> 1;
         if (ause > 0 && !mbar_wait(acce0 + 8 * buf, (ause - 1) & 1, err, ERR_MMA)) break;
         tc_fence_after();
@@ -204,18 +207,19 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
       const int4 tr = tiles[t];
       const TcJob& job = jobs[tr.x];
+      // the job's fields in registers for the whole tile, loaded while the
+      // accumulator is still being computed (read through the reference
+      // inside the store loop, each store could alias them and forced a
+      // reload per row)
+      float* const c = job.c;
+      float* const c_lo = job.c_lo;
+      const float* const scl = job.scale;
+      const int M = job.M, Nc = job.N, ldc = job.ldc, mode = job.mode;
       const int buf = it & 1;
       const bool ok = mbar_wait(accf0 + 8 * buf, (it >> 1) & 1, err, ERR_EPILOGUE);
       if (!__all_sync(0xffffffffu, ok && *reinterpret_cast<volatile int*>(err) == 0)) break;
       tc_fence_after();
       const int row0 = tr.y + 32 * q;
-      // the job's fields in registers for the whole tile (read through the
-      // reference inside the store loop, each store could alias them and
-      // forced a reload per row)
-      float* const c = job.c;
-      float* const c_lo = job.c_lo;
-      const float* const scl = job.scale;
-      const int M = job.M, Nc = job.N, ldc = job.ldc, mode = job.mode;
       const bool scaled = mode == MODE_SCALE_SPLIT || mode == MODE_SCALE;
       const bool split = mode == MODE_SPLIT || mode == MODE_SCALE_SPLIT;
 #pragma unroll 1
@@ -311,6 +315,7 @@ int encode_operand(CUtensorMap* map, const float* base, int rows, int K, int ld)
 }
 
 void order_tiles_by_k(int4* tiles, int n, const TcJob* jobs) {
+  for (int i = 0; i < n; ++i) tiles[i].w = (jobs[tiles[i].x].K + BKF - 1) / BKF;
   std::stable_sort(tiles, tiles + n,
                    [jobs](const int4& a, const int4& b) { return jobs[a.x].K > jobs[b.x].K; });
 }
@@ -457,7 +462,7 @@ extern "C" int axi_tf32x3_gemm(float* C, const float* A, const float* B, int M, 
   std::string tiles;
   for (int m0 = 0; m0 < M; m0 += axi_tc::BM)
     for (int n0 = 0; n0 < N; n0 += axi_tc::BN) {
-      int4 t = make_int4(0, m0, n0, 0);
+      int4 t = make_int4(0, m0, n0, (K + axi_tc::BKF - 1) / axi_tc::BKF);
       tiles.append(reinterpret_cast<const char*>(&t), sizeof(t));
     }
   const int n_tiles = (int)(tiles.size() / sizeof(int4));

@@ -84,12 +84,14 @@ __device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
 // for 128-row x BKF-float boxes with the ROW_BYTES swizzle. Returns AXI status.
 int encode_operand(CUtensorMap* map, const float* base, int rows, int K, int ld);
 
-// Host: order a tile table (job, m0, n0, -) longest main loop (largest K)
-// first, stable within equal K. The persistent CTAs take tiles with a fixed
-// stride, so the long tiles are spread over all SMs before the short ones.
+// Host: complete a tile table (job, m0, n0, -) with each tile's k-block
+// count (w = ceil(K / BKF), which the kernel reads instead of the job) and
+// order it longest main loop (largest K) first, stable within equal K. The
+// persistent CTAs take tiles with a fixed stride, so the long tiles are
+// spread over all SMs before the short ones.
 void order_tiles_by_k(int4* tiles, int n, const TcJob* jobs);
 
-// Host: launch the grouped kernel over `n_tiles` (job, m0, n0) tiles.
+// Host: launch the grouped kernel over `n_tiles` (job, m0, n0, k-blocks) tiles.
 int launch(const TcJob* jobs_dev, const int4* tiles_dev, int n_tiles, int* err_dev,
            cudaStream_t s);
 
