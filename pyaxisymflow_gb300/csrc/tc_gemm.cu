@@ -75,6 +75,10 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int m, int n) {
          (static_cast<uint32_t>(m >> 4) << 24);
 }
 
+__device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* m) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(m)) : "memory");
+}
+
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -135,6 +139,14 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int4 tr = tiles[t];
         const TcJob& job = jobs[tr.x];  // only the tensor maps' addresses are used
         const int nk = tr.w;
+        if (t + (int)gridDim.x < n_tiles) {
+          // the next tile's four tensor maps, fetched while this tile loads
+          const TcJob& nj = jobs[tiles[t + gridDim.x].x];
+          prefetch_tensormap(&nj.a_hi);
+          prefetch_tensormap(&nj.a_lo);
+          prefetch_tensormap(&nj.b_hi);
+          prefetch_tensormap(&nj.b_lo);
+        }
         for (int kb = 0; kb < nk; ++kb, ++g) {
           const int s = g % NSTAGE, use = g / NSTAGE;
           if (use > 0 && !mbar_wait(empty0 + 8 * s, (use - 1) & 1, err, ERR_PRODUCER)) {
