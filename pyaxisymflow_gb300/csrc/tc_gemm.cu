@@ -229,7 +229,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int M = job.M, Nc = job.N, ldc = job.ldc, mode = job.mode;
       const int buf = it & 1;
       const bool ok = mbar_wait(accf0 + 8 * buf, (it >> 1) & 1, err, ERR_EPILOGUE);
-      if (!__all_sync(0xffffffffu, ok && *reinterpret_cast<volatile int*>(err) == 0)) break;
+      // all lanes leave together; a failure elsewhere in the grid surfaces at
+      // the next wait (the error word is read there) and on the host
+      if (!__all_sync(0xffffffffu, ok)) break;
       tc_fence_after();
       const int row0 = tr.y + 32 * q;
       const bool scaled = mode == MODE_SCALE_SPLIT || mode == MODE_SCALE;

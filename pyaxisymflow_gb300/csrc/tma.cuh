@@ -59,16 +59,21 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Bounded wait on an mbarrier phase. False on timeout (error recorded) or when
-// another thread of the grid has already failed.
+// another thread of the grid has already failed. The error word (an L2 round
+// trip) and the clock are read once every 64 polls, so a phase that completes
+// while the thread waits is seen at the next poll; each try_wait suspends for
+// at most a hardware time limit, which keeps the loop bounded.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
-  for (;;) {
+  for (unsigned int i = 1;; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (*reinterpret_cast<volatile int*>(err) != 0) return false;
-    if (globaltimer() - t0 > WAIT_NS) {
-      atomicCAS(err, 0, code);
-      return false;
+    if ((i & 63u) == 0) {
+      if (*reinterpret_cast<volatile int*>(err) != 0) return false;
+      if (globaltimer() - t0 > WAIT_NS) {
+        atomicCAS(err, 0, code);
+        return false;
+      }
     }
   }
 }
