@@ -959,6 +959,18 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) advect_diffuse_ker
       const T rbody = scalar<T>(k, SF_RBODY);
       const T blendw = scalar<T>(k, SF_BLENDW);
       const T zcol = (sediment && gjm < nz) ? CF<T>(k.zw)[gjm] : T(0);
+      // a tile farther than radius + 2 w from the body centre (z_cm, 0) has
+      // mask 0 at every cell (phi < -w) and adds nothing to the drag: the
+      // per-cell mask is skipped there (the same values)
+      bool near = sediment;
+      if (sediment) {
+        const T* zw = CF<T>(k.zw);
+        const T zlo = zw[j0], zhi = zw[min(j0 + TX, nz) - 1];
+        const T rlo = rowf[2][1];  // r of row i0
+        const T dz = zc < zlo ? zlo - zc : (zc > zhi ? zc - zhi : T(0));
+        const T reach = rbody + T(2) * blendw;
+        near = dz * dz + rlo * rlo <= reach * reach;
+      }
       const bool jin = gjm < nz, jint = gjm >= 1 && gjm < nz - 1;
       const int p0 = AD_RC * grp;
       int d = ad_tp(p0, qm);
@@ -988,10 +1000,14 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) advect_diffuse_ker
           if (sediment) {
             // mask at the body position of this step (falling_rigid_sphere.py:156-157),
             // then the drag integrand with the new mask (:164-173)
-            const T rr = rowf[2][pr + 1];
-            const T ch = sphere_mask<T>(zcol, rr, zc, rbody, blendw);
-            chi[c] = ch;
-            cd_part += rr * ch * sz[ad_box(pr, qm)];
+            if (near) {
+              const T rr = rowf[2][pr + 1];
+              const T ch = sphere_mask<T>(zcol, rr, zc, rbody, blendw);
+              chi[c] = ch;
+              cd_part += rr * ch * sz[ad_box(pr, qm)];
+            } else {
+              chi[c] = T(0);
+            }
           }
         }
         s_ = c_;
