@@ -109,15 +109,33 @@ __device__ __forceinline__ void store_split4(const DctJob& job, int k, int i, co
   *reinterpret_cast<float4*>(job.out_lo + o) = make_float4(lo[0], lo[1], lo[2], lo[3]);
 }
 
+// Bulk prefetch of `bytes` (a multiple of 16, 16-byte aligned) into L2.
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 __global__ void __launch_bounds__(THREADS) dct_rows_kernel(const DctJob* __restrict__ jobs,
                                                            const int4* __restrict__ items,
-                                                           int forward) {
+                                                           int n_items, int ahead, int forward) {
   extern __shared__ __align__(16) float2 dsm[];
   float2* a = dsm;
   float2* b = dsm + ELEMS;
   __shared__ DctJob sjob;
   const int4 it = items[blockIdx.x];
   if (threadIdx.x == 0) sjob = jobs[it.x];
+  if (threadIdx.x == 32 && blockIdx.x + ahead < n_items) {
+    // the rows of the item one resident wave ahead (`ahead` blocks fit on
+    // the GPU at once), fetched into L2 while this item is transformed: the
+    // block that takes it finds its rows there instead of in DRAM. Rows of
+    // an item are contiguous.
+    const int4 nx = items[blockIdx.x + ahead];
+    const DctJob& nj = jobs[nx.x];
+    const int nrows = min(rows_for(nj.N), nj.rows - nx.y);
+    const uint32_t bytes = (uint32_t)nrows * (uint32_t)nj.N * 4u;
+    const long long off = (long long)nx.y * nj.N;
+    prefetch_l2(nj.in + off, bytes);
+    if (!forward && nj.row_scale) prefetch_l2(nj.row_scale + off, bytes);
+  }
   __syncthreads();
   // the twiddle table of this row length, staged once per block at the end
   // of shared memory (every thread takes the global pointer before thread 0
@@ -572,16 +590,6 @@ __device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* 
 
 }  // namespace
 
-// Rows per work item: specialised lengths pack two real rows per complex row.
-int rows_for(int N) {
-  if (reg_n1(N)) return 2 * reg_warps(N);
-  switch (N) {
-    case 1536: case 2048:
-      return 2 * (ELEMS / N);
-    default:
-      return rows_per_item(N);
-  }
-}
 
 bool plan_radices(int N, int* radix, int* nstages) {
   if (N < 2 || (N & 1) || N > ELEMS) return false;
@@ -606,7 +614,16 @@ int launch(const DctJob* jobs_dev, const int4* items_dev, int n_items, bool forw
     return AXI_ERR_CUDA;
   }
   if (n_items <= 0) return AXI_OK;
-  dct_rows_kernel<<<n_items, THREADS, SMEM_BYTES, s>>>(jobs_dev, items_dev, forward ? 1 : 0);
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    int b = 0;
+    per_sm = (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, dct_rows_kernel, THREADS,
+                                                           SMEM_BYTES) == cudaSuccess && b > 0)
+                 ? b
+                 : 1;
+  }
+  dct_rows_kernel<<<n_items, THREADS, SMEM_BYTES, s>>>(jobs_dev, items_dev, n_items,
+                                                       per_sm * axi::sm_count(), forward ? 1 : 0);
   return axi::launch_status("dct_rows");
 }
 

@@ -73,9 +73,13 @@ __host__ __device__ constexpr int reg_warps(int N) {
                                : THREADS / 32);
 }
 
-// Host: rows per work item for row length N (lengths with a specialised
-// kernel pack two real rows per complex transform).
-int rows_for(int N);
+// Rows per work item for row length N (lengths with a specialised kernel
+// pack two real rows per complex transform).
+__host__ __device__ inline int rows_for(int N) {
+  if (reg_n1(N)) return 2 * reg_warps(N);
+  if (N == 1536 || N == 2048) return 2 * (ELEMS / N);
+  return rows_per_item(N);
+}
 
 // Host: Stockham radices of N (4s, then a 2, then 3s); false if N has
 // another factor or needs more than MAX_STAGES stages.
