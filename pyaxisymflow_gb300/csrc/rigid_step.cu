@@ -301,6 +301,14 @@ struct BoxRing {
       axi_tma::tma_load_2d(axi_tma::smem_u32(box(slot, q)), maps + MAP_COUNT * tr.x + which[q],
                            tr.z - 4, tr.y + row0, bar);
   }
+  // thread 0: ask L2 for the boxes of tile tr (a hint: no shared memory, no
+  // barrier; the box origin clamped into the grid)
+  __device__ void prefetch(const CUtensorMap* maps, const int4& tr, const int (&which)[NBOX],
+                           int row0) const {
+    for (int q = 0; q < NBOX; ++q)
+      axi_tma::tma_prefetch_2d(maps + MAP_COUNT * tr.x + which[q], max(tr.z - 4, 0),
+                               max(tr.y + row0, 0));
+  }
   // Block-wide: thread 0 waits (bounded) for the boxes of iteration `it`,
   // the other threads wait at the barrier (no issue slots spent polling);
   // false on failure, for every thread.
@@ -500,7 +508,7 @@ template <typename T>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 2) penalise_kernel(const axi_case* __restrict__ cases,
                                                       const int4* __restrict__ tiles, int n_tiles,
                                                       const CUtensorMap* __restrict__ maps,
-                                                      int* __restrict__ err) {
+                                                      int* __restrict__ err, int ahead) {
   extern __shared__ unsigned char pn_raw[];
   __shared__ __align__(8) uint64_t bars[PN_NBUF];
   __shared__ double red[2][NT / 32];
@@ -524,6 +532,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 2) penalise_kernel(co
         ring.issue(maps, tiles[tn], which, -2, (it + PN_NBUF - 1) % PN_NBUF);
         ++issued;
       }
+      // the tile one resident wave ahead: its boxes wait in L2
+      if (t + ahead < n_tiles) ring.prefetch(maps, tiles[t + ahead], which, -2);
     }
     const int4 tr = tiles[t];
     const axi_case& k = cases[tr.x];
@@ -775,7 +785,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) advect_diffuse_ker
                                                             const int4* __restrict__ tiles,
                                                             int n_tiles,
                                                             const CUtensorMap* __restrict__ maps,
-                                                            int* __restrict__ err) {
+                                                            int* __restrict__ err, int ahead) {
   extern __shared__ unsigned char ad_raw[];
   __shared__ __align__(8) uint64_t bars[AD_NBUF];
   __shared__ double red[2][NT / 32];
@@ -798,6 +808,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) advect_diffuse_ker
         ring.issue(maps, tiles[tn], which, -AD_H, (it + AD_NBUF - 1) % AD_NBUF);
         ++issued;
       }
+      // the tile one resident wave ahead: its boxes wait in L2
+      if (t + ahead < n_tiles) ring.prefetch(maps, tiles[t + ahead], which, -AD_H);
     }
     const int4 tr = tiles[t];
     const axi_case& k = cases[tr.x];
@@ -1410,6 +1422,8 @@ struct StencilGrid {
     }
     return n[phase];
   }
+  // blocks of the phase resident on the GPU at once
+  static int resident(int phase) { return per_sm(phase) * axi::sm_count(); }
   static int get(int phase, int n_tiles) {
     // ring depth 1: one block per tile
     if ((phase == PH_PENALISE && PN_NBUF == 1) || (phase == PH_ADVECT_DIFFUSE && AD_NBUF == 1))
@@ -1455,13 +1469,13 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
     case PH_PENALISE:
       AXI_TRY(stencil_attrs<T>());
       penalise_kernel<T><<<StencilGrid<T>::get(PH_PENALISE, nt), NT, penalise_smem<T>(), s>>>(
-          v.cases, v.stencil, nt, v.maps, v.err);
+          v.cases, v.stencil, nt, v.maps, v.err, StencilGrid<T>::resident(PH_PENALISE));
       break;
     case PH_ADVECT_DIFFUSE:
       AXI_TRY(stencil_attrs<T>());
       advect_diffuse_kernel<T>
           <<<StencilGrid<T>::get(PH_ADVECT_DIFFUSE, nt), NT, advect_diffuse_smem<T>(), s>>>(
-              v.cases, v.stencil, nt, v.maps, v.err);
+              v.cases, v.stencil, nt, v.maps, v.err, StencilGrid<T>::resident(PH_ADVECT_DIFFUSE));
       break;
     case PH_TRANSFORM_PART0:
     case PH_TRANSFORM_PART0 + 1:

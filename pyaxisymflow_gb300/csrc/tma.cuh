@@ -87,6 +87,14 @@ __device__ __forceinline__ bool mbar_wait_drain(uint32_t bar, uint32_t parity) {
   return true;
 }
 
+// L2 prefetch of a box (no shared memory, no barrier); c0 as for a load.
+__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int c0, int c1) {
+  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(c0), "r"(c1)
+               : "memory");
+}
+
 // Box load: c0 is the innermost (contiguous) coordinate. Out-of-range
 // elements of the box are filled with zeros; c0 * element size must be a
 // multiple of 16 bytes.
