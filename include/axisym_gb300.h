@@ -258,6 +258,22 @@ int axi_advect_particles_prepare_f64(double* z_particles, double* r_particles,
                                      double* vort_particles, const double* vorticity,
                                      const double* u_z, const double* u_r, int nr, int nz,
                                      double dt, void* stream);
+/* ---------------------------------------------------------------------
+ * Level-set reinitialisation: the signed distance to the zero contour of phi
+ * (nr, nz, spacing dx) within `narrow`, the role of
+ * skfmm.distance(phi, dx=dx, narrow=narrow) at
+ * examples/SoftSphereStreaming/soft_sphere_streaming.py:197. The contour is
+ * the marching-squares reconstruction of phi (crossings linearly
+ * interpolated on cell edges); points within `narrow` of it get the exact
+ * distance to it, with the sign of phi, and in_band = 1; the others keep
+ * phi and get in_band = 0 (the reference's masked points, restored from the
+ * previous values at :198-199). in_band may be NULL. `out` must not alias
+ * `phi`; `work` is device scratch of axi_level_set_work_bytes(nr, nz) bytes;
+ * the band is at most 4096 cells wide.
+ * ------------------------------------------------------------------ */
+int64_t axi_level_set_work_bytes(int nr, int nz);
+int axi_level_set_distance_f64(double* out, const double* phi, int nr, int nz, double dx,
+                               double narrow, unsigned char* in_band, void* work, void* stream);
 /* elasto_kernels/extrapolate_eta_using_least_squares_unb.py:7-30 with
  * elasto_kernels/extrapolate_using_least_squares.py:33-38 folded in: builds the
  * axis-mirrored (2*nr, nz) level set, masked eta and flags (phi < 0, phi <

@@ -48,6 +48,8 @@ def _signatures():
         "axi_p2m_mp4_work_bytes": (I64, [I, I]),
         "axi_particles_to_mesh_2d_mp4_f64": (I, [P, P, P, P, I, I, D, D, I, P, P]),
         "axi_p2m_status": (I, [P, I, I, P, P]),
+        "axi_level_set_work_bytes": (I64, [I, I]),
+        "axi_level_set_distance_f64": (I, [P, P, I, I, D, D, P, P, P]),
         "axi_advect_particles_prepare_f64": (I, [P, P, P, P, P, P, I, I, D, P]),
         "axi_extrapolate_lsq_first_order_f64": (I, [P, P, P, P, P, P, I, I, I, P, P, P]),
         "axi_extrapolate_eta_with_least_squares_f64": (

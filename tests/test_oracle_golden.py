@@ -255,3 +255,25 @@ def test_oracle_particles_to_mesh_matches_compiled_reference():
             ref(px.ctypes.data, py.ctypes.data, v.ctypes.data, a.ctypes.data, n0, n1, dx, dx)
             ora(px, py, v, b, dx, dx)
             np.testing.assert_array_equal(a, b)
+
+
+def test_level_set_oracle_recovers_circle_distance():
+    """The level-set distance restatement (the device algorithm) recovers the
+    exact distance to a circle from a distorted level set with the same zero
+    contour (parity with scikit-fmm is unpinned: it is not installed)."""
+    from oracle import levelset
+    n, dx = 48, 1.0 / 48
+    y, x = np.meshgrid(np.arange(n) * dx, np.arange(n) * dx, indexing="ij")
+    rad = 0.27
+    exact = rad - np.sqrt((x - 0.51) ** 2 + (y - 0.47) ** 2)
+    distorted = exact * (1.5 + 0.4 * np.sin(7 * x) * np.cos(5 * y))  # same zero set
+    narrow = 5 * dx
+    d, band = levelset.distance(distorted, dx, narrow)
+    inside = np.abs(exact) <= narrow - 0.1 * dx
+    assert band[inside].all()
+    assert not band[np.abs(exact) > narrow + 0.1 * dx].any()
+    err = np.abs(d - exact)[band]
+    assert err.max() < 0.05 * dx
+    assert np.array_equal(np.sign(d[band]), np.sign(exact[band]))
+    # outside the band the values are kept
+    assert np.array_equal(d[~band], distorted[~band])
