@@ -248,6 +248,17 @@ int axi_particles_to_mesh_2d_mp4_f64(const double* particle_positions_x,
                                      const double* input_field_at_particle_positions,
                                      double* output_field_at_mesh, int n0, int n1, double dx,
                                      double dy, int periodic, void* work, void* stream);
+/* axi_mesh_to_particles_2d_mp4_f64 replaces mesh_to_particles_2D_mp4
+ * (periodic = 1) and mesh_to_particles_2D_unbounded_mp4 (periodic = 0) of the
+ * compiled pyaxisymflow.core.mesh_to_particles
+ * (core/src/mesh_to_particles.hpp, core/src/interpolation/mesh_to_particles_2D.hpp):
+ * two mesh fields (n0, n1) interpolated with the MP4 kernel at the particle
+ * positions (p0, p1), bit-identical to the reference. */
+int axi_mesh_to_particles_2d_mp4_f64(const double* input_field_x, const double* input_field_y,
+                                     int n0, int n1, const double* particle_positions_x,
+                                     const double* particle_positions_y, double* output_field_x,
+                                     double* output_field_y, int p0, int p1, double dx, double dy,
+                                     int periodic, void* stream);
 /* *displaced (host) = 1 when the last interpolation using `work` met a
  * particle a cell or more from its mesh point (result invalid). Synchronises. */
 int axi_p2m_status(const void* work, int n0, int n1, int* displaced, void* stream);

@@ -3,8 +3,9 @@
 * oracle/_ref/libref_lsq.so: the reference's own least-squares core compiled
   from its sources in place (core/src/extrapolate_using_least_squares.hpp)
   through oracle/ref_shim.cpp.
-* oracle/_ref/libref_p2m.so: the reference's particle-to-mesh interpolation
-  (core/src/particles_to_mesh.hpp) through oracle/ref_p2m_shim.cpp.
+* oracle/_ref/libref_p2m.so: the reference's particle-to-mesh and
+  mesh-to-particle interpolation (core/src/particles_to_mesh.hpp,
+  core/src/mesh_to_particles.hpp) through oracle/ref_p2m_shim.cpp.
 Built only where the reference sources exist; never shipped.
 """
 import os

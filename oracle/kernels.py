@@ -767,6 +767,65 @@ def particles_to_mesh_2D_unbounded_mp4(particle_positions_x, particle_positions_
                            delta_x, delta_y, periodic=False)
 
 
+def _mesh_to_particles_mp4(in_x, in_y, px, py, out_x, out_y, dx, dy, periodic):
+    """core/src/interpolation/mesh_to_particles_2D.hpp:11-183 (periodic) and
+    :185-420 (unbounded): per particle, each stencil row is summed along x
+    from 0.0 in the order sx = -2 .. 1, then the rows are weighted along y and
+    summed from 0.0 in the order sy = -2 .. 1. The unbounded form clips the
+    stencil at the mesh edges (:313-344) but accumulates all four rows."""
+    n0, n1 = np.asarray(in_x).shape
+    fx = np.asarray(in_x, dtype=np.float64).reshape(-1)
+    fy = np.asarray(in_y, dtype=np.float64).reshape(-1)
+    hx, wx = _mp4_stencil(np.asarray(px, dtype=np.float64).reshape(-1) / dx)
+    hy, wy = _mp4_stencil(np.asarray(py, dtype=np.float64).reshape(-1) / dy)
+    n = hx.size
+    ps_x = np.zeros((n, 4))
+    ps_y = np.zeros((n, 4))
+    for sy in range(-2, 2):
+        my = hy + sy
+        acc_x = np.zeros(n)
+        acc_y = np.zeros(n)
+        for sx in range(-2, 2):
+            mx = hx + sx
+            if periodic:
+                # (h + s + n) % n, wrapped like a mathematical modulo
+                idx = ((mx + n1) % n1) + n1 * ((my + n0) % n0)
+                ok = np.ones(n, dtype=bool)
+            else:
+                ok = (mx >= 0) & (mx < n1) & (my >= 0) & (my < n0)
+                idx = np.where(ok, mx + n1 * my, 0)
+            w = wx[:, sx + 2]
+            acc_x = np.where(ok, acc_x + w * fx[idx], acc_x)
+            acc_y = np.where(ok, acc_y + w * fy[idx], acc_y)
+        ps_x[:, sy + 2] = acc_x
+        ps_y[:, sy + 2] = acc_y
+    rx = np.zeros(n)
+    ry = np.zeros(n)
+    for k in range(4):
+        rx = rx + wy[:, k] * ps_x[:, k]
+        ry = ry + wy[:, k] * ps_y[:, k]
+    out_x[...] = rx.reshape(out_x.shape)
+    out_y[...] = ry.reshape(out_y.shape)
+
+
+def mesh_to_particles_2D_mp4(input_field_x, input_field_y, particle_positions_x,
+                             particle_positions_y, output_field_x, output_field_y,
+                             delta_x, delta_y):
+    """core/src/mesh_to_particles.hpp (mesh_to_particles_2D_mp4, periodic)."""
+    _mesh_to_particles_mp4(input_field_x, input_field_y, particle_positions_x,
+                           particle_positions_y, output_field_x, output_field_y,
+                           delta_x, delta_y, periodic=True)
+
+
+def mesh_to_particles_2D_unbounded_mp4(input_field_x, input_field_y, particle_positions_x,
+                                       particle_positions_y, output_field_x, output_field_y,
+                                       delta_x, delta_y):
+    """core/src/mesh_to_particles.hpp (mesh_to_particles_2D_unbounded_mp4)."""
+    _mesh_to_particles_mp4(input_field_x, input_field_y, particle_positions_x,
+                           particle_positions_y, output_field_x, output_field_y,
+                           delta_x, delta_y, periodic=False)
+
+
 def _advect_vorticity_via_particles(z_particles, r_particles, vort_particles, vorticity,
                                     Z_double, R_double, grid_size_r, u_z, u_r, dx, dt,
                                     p2m):

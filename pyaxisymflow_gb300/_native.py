@@ -48,6 +48,7 @@ def _signatures():
         "axi_p2m_mp4_work_bytes": (I64, [I, I]),
         "axi_particles_to_mesh_2d_mp4_f64": (I, [P, P, P, P, I, I, D, D, I, P, P]),
         "axi_p2m_status": (I, [P, I, I, P, P]),
+        "axi_mesh_to_particles_2d_mp4_f64": (I, [P, P, I, I, P, P, P, P, I, I, D, D, I, P]),
         "axi_level_set_work_bytes": (I64, [I, I]),
         "axi_level_set_distance_f64": (I, [P, P, I, I, D, D, P, P, P]),
         "axi_advect_particles_prepare_f64": (I, [P, P, P, P, P, P, I, I, D, P]),

@@ -19,6 +19,11 @@
 
 namespace {
 
+// the four MP4 weights of one particle along one axis
+struct alignas(16) Weights4 {
+  double v[4];
+};
+
 struct P2MLayout {
   size_t h, wx, wy, flag, total;
 };
@@ -32,9 +37,9 @@ P2MLayout p2m_layout(int n0, int n1) {
   L.h = o;
   o = align_up(o + n * sizeof(int2), 256);
   L.wx = o;
-  o = align_up(o + n * 4 * sizeof(double), 256);
+  o = align_up(o + n * sizeof(Weights4), 256);
   L.wy = o;
-  o = align_up(o + n * 4 * sizeof(double), 256);
+  o = align_up(o + n * sizeof(Weights4), 256);
   L.flag = o;
   o = align_up(o + 16, 256);
   L.total = o;
@@ -69,7 +74,7 @@ __device__ __forceinline__ int mp4_stencil(double pos, double w[4]) {
 
 __global__ void p2m_stencil_kernel(const double* __restrict__ px, const double* __restrict__ py,
                                    int n0, int n1, double dx, double dy, int2* __restrict__ H,
-                                   double4* __restrict__ WX, double4* __restrict__ WY,
+                                   Weights4* __restrict__ WX, Weights4* __restrict__ WY,
                                    int* __restrict__ flag) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= (long long)n0 * n1) return;
@@ -78,8 +83,8 @@ __global__ void p2m_stencil_kernel(const double* __restrict__ px, const double* 
   const int hx = mp4_stencil(__ddiv_rn(px[p], dx), wx);
   const int hy = mp4_stencil(__ddiv_rn(py[p], dy), wy);
   H[p] = make_int2(hx, hy);
-  WX[p] = make_double4(wx[0], wx[1], wx[2], wx[3]);
-  WY[p] = make_double4(wy[0], wy[1], wy[2], wy[3]);
+  WX[p] = Weights4{{wx[0], wx[1], wx[2], wx[3]}};
+  WY[p] = Weights4{{wy[0], wy[1], wy[2], wy[3]}};
   if (hx - i < 0 || hx - i > 1 || hy - j < 0 || hy - j > 1) atomicOr(flag, 1);
 }
 
@@ -104,12 +109,8 @@ __device__ __forceinline__ int candidates(int m, int n, bool periodic, int out[5
   return c;
 }
 
-__device__ __forceinline__ double comp(const double4& w, int k) {
-  return k == 0 ? w.x : k == 1 ? w.y : k == 2 ? w.z : w.w;
-}
-
 __global__ void p2m_gather_kernel(const double* __restrict__ vin, const int2* __restrict__ H,
-                                  const double4* __restrict__ WX, const double4* __restrict__ WY,
+                                  const Weights4* __restrict__ WX, const Weights4* __restrict__ WY,
                                   double* __restrict__ out, int n0, int n1, int periodic) {
   const int mi = blockIdx.x * blockDim.x + threadIdx.x;
   const int mj = blockIdx.y;
@@ -132,11 +133,65 @@ __global__ void p2m_gather_kernel(const double* __restrict__ vin, const int2* __
         if (sy < -n0 / 2) sy += n0;
       }
       if (sx < -2 || sx > 1 || sy < -2 || sy > 1) continue;
-      const double w = __dmul_rn(comp(WY[p], sy + 2), comp(WX[p], sx + 2));
+      const double w = __dmul_rn(WY[p].v[sy + 2], WX[p].v[sx + 2]);
       acc = __dadd_rn(acc, __dmul_rn(w, vin[p]));
     }
   }
   out[(long long)mj * n1 + mi] = acc;
+}
+
+// Mesh-to-particle MP4 interpolation of two fields
+// (core/src/interpolation/mesh_to_particles_2D.hpp:11-183 periodic, :185-420
+// unbounded): one thread per particle, the reference's sums in its order
+// (each stencil row summed along x from 0.0, then the rows weighted along y
+// from 0.0), unfused double operations. The unbounded form clips the stencil
+// at the mesh edges but still accumulates all four rows (the clipped rows
+// add a zero), as the reference does. Periodic indices wrap like the
+// reference's (h + s + n) % n, also for particles more than a period away
+// (where the reference's index would be negative).
+__device__ __forceinline__ int wrap_index(int a, int n) {
+  a %= n;
+  return a < 0 ? a + n : a;
+}
+
+__global__ void m2p_mp4_kernel(const double* __restrict__ in_x, const double* __restrict__ in_y,
+                               int n0, int n1, const double* __restrict__ px,
+                               const double* __restrict__ py, double* __restrict__ out_x,
+                               double* __restrict__ out_y, long long n_particles, double dx,
+                               double dy, int periodic) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_particles) return;
+  double wx[4], wy[4];
+  const int hx = mp4_stencil(__ddiv_rn(px[p], dx), wx);
+  const int hy = mp4_stencil(__ddiv_rn(py[p], dy), wy);
+  int sx0 = -2, sx1 = 2, sy0 = -2, sy1 = 2;
+  if (!periodic && (hx - 2 < 0 || hy - 2 < 0 || hx + 2 > n1 || hy + 2 > n0)) {
+    sx0 = max(-2, -hx);
+    sy0 = max(-2, -hy);
+    sx1 = min(2, n1 - hx);
+    sy1 = min(2, n0 - hy);
+  }
+  double ps_x[4] = {0.0, 0.0, 0.0, 0.0}, ps_y[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int sy = sy0; sy < sy1; ++sy) {
+    const long long row = (long long)n1 * (periodic ? wrap_index(hy + sy + n0, n0) : hy + sy);
+    double a = 0.0, b = 0.0;
+    for (int sx = sx0; sx < sx1; ++sx) {
+      const long long m = row + (periodic ? wrap_index(hx + sx + n1, n1) : hx + sx);
+      const double w = wx[sx + 2];
+      a = __dadd_rn(a, __dmul_rn(w, in_x[m]));
+      b = __dadd_rn(b, __dmul_rn(w, in_y[m]));
+    }
+    ps_x[sy + 2] = a;
+    ps_y[sy + 2] = b;
+  }
+  double acc_x = 0.0, acc_y = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    acc_x = __dadd_rn(acc_x, __dmul_rn(wy[k], ps_x[k]));
+    acc_y = __dadd_rn(acc_y, __dmul_rn(wy[k], ps_y[k]));
+  }
+  out_x[p] = acc_x;
+  out_y[p] = acc_y;
 }
 
 // kernels/advect_particle.py:20-28 (and :53-61): particles on the mirrored
@@ -190,8 +245,8 @@ extern "C" int axi_particles_to_mesh_2d_mp4_f64(const double* px, const double* 
   const P2MLayout L = p2m_layout(n0, n1);
   char* wb = static_cast<char*>(work);
   int2* H = reinterpret_cast<int2*>(wb + L.h);
-  double4* WX = reinterpret_cast<double4*>(wb + L.wx);
-  double4* WY = reinterpret_cast<double4*>(wb + L.wy);
+  Weights4* WX = reinterpret_cast<Weights4*>(wb + L.wx);
+  Weights4* WY = reinterpret_cast<Weights4*>(wb + L.wy);
   int* flag = reinterpret_cast<int*>(wb + L.flag);
   cudaStream_t s = axi::as_stream(stream);
   if (cudaMemsetAsync(flag, 0, sizeof(int), s) != cudaSuccess)
@@ -231,4 +286,28 @@ extern "C" int axi_advect_particles_prepare_f64(double* z_particles, double* r_p
   particles_prepare_kernel<<<dim3((nz + 127) / 128, 2 * nr), 128, 0, axi::as_stream(stream)>>>(
       z_particles, r_particles, vort_particles, vorticity, u_z, u_r, nr, nz, dt);
   return axi::launch_status("advect_particles");
+}
+
+extern "C" int axi_mesh_to_particles_2d_mp4_f64(const double* input_field_x,
+                                                const double* input_field_y, int n0, int n1,
+                                                const double* particle_positions_x,
+                                                const double* particle_positions_y,
+                                                double* output_field_x, double* output_field_y,
+                                                int p0, int p1, double dx, double dy,
+                                                int periodic, void* stream) {
+  axi::clear_error();
+  const void* ptrs[] = {input_field_x, input_field_y, particle_positions_x, particle_positions_y,
+                        output_field_x, output_field_y};
+  for (const void* p : ptrs) AXI_TRY(axi::check_ptr("mesh_to_particles", p, "field"));
+  if (n0 <= 0 || n1 <= 0 || p0 <= 0 || p1 <= 0 || !(dx > 0.0) || !(dy > 0.0) ||
+      (long long)n0 * n1 >= (1LL << 31)) {
+    axi::set_error("mesh_to_particles: mesh %d x %d, particles %d x %d or spacing invalid", n0,
+                   n1, p0, p1);
+    return AXI_ERR_INVALID;
+  }
+  const long long n = (long long)p0 * p1;
+  m2p_mp4_kernel<<<(unsigned)((n + 255) / 256), 256, 0, axi::as_stream(stream)>>>(
+      input_field_x, input_field_y, n0, n1, particle_positions_x, particle_positions_y,
+      output_field_x, output_field_y, n, dx, dy, periodic);
+  return axi::launch_status("mesh_to_particles");
 }

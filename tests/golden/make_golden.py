@@ -457,6 +457,35 @@ def p2m_vectors():
     return out
 
 
+def m2p_vectors():
+    """Mesh-to-particle (MP4) interpolation computed by the reference's C++
+    (core/src/mesh_to_particles.hpp, compiled into oracle/_ref/libref_p2m.so):
+    periodic and unbounded forms, particles scattered in and around the mesh,
+    particle arrays shaped differently from the mesh."""
+    lib = ctypes.CDLL(os.path.join(REPO, "oracle", "_ref", "libref_p2m.so"))
+    P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    for f in (lib.ref_m2p_2d_mp4, lib.ref_m2p_2d_unbounded_mp4):
+        f.argtypes = [P, P, I, I, P, P, P, P, I, I, D, D]
+    rng = np.random.default_rng(12)
+    out = {}
+    # (tag, mesh n0, n1, particles p0, p1, dx, margin around the mesh in cells)
+    for tag, n0, n1, p0, p1, dx, margin in (("a", 16, 24, 16, 24, 0.1, 2.5),
+                                            ("b", 48, 32, 20, 28, 1.0 / 48, 0.0),
+                                            ("c", 12, 40, 30, 10, 0.05, 1.0)):
+        fx, fy = rng.standard_normal((n0, n1)), rng.standard_normal((n0, n1))
+        px = rng.uniform(-margin, n1 + margin, (p0, p1)) * dx
+        py = rng.uniform(-margin, n0 + margin, (p0, p1)) * dx
+        out[f"{tag}/fx"], out[f"{tag}/fy"], out[f"{tag}/px"], out[f"{tag}/py"] = fx, fy, px, py
+        out[f"{tag}/dx"] = np.array(dx)
+        for name, fn in (("periodic", lib.ref_m2p_2d_mp4),
+                         ("unbounded", lib.ref_m2p_2d_unbounded_mp4)):
+            ox, oy = np.zeros((p0, p1)), np.zeros((p0, p1))
+            fn(fx.ctypes.data, fy.ctypes.data, n0, n1, px.ctypes.data, py.ctypes.data,
+               ox.ctypes.data, oy.ctypes.data, p0, p1, dx, dx)
+            out[f"{tag}/{name}_x"], out[f"{tag}/{name}_y"] = ox, oy
+    return out
+
+
 def main(ref_root):
     _install_reference(ref_root)
     ref = _ref_kernels()
@@ -465,6 +494,7 @@ def main(ref_root):
     np.savez_compressed(os.path.join(HERE, "solvers.npz"), **solver_vectors(ref))
     np.savez_compressed(os.path.join(HERE, "lsq.npz"), **lsq_vectors(extrap_first_order))
     np.savez_compressed(os.path.join(HERE, "p2m.npz"), **p2m_vectors())
+    np.savez_compressed(os.path.join(HERE, "m2p.npz"), **m2p_vectors())
     np.savez_compressed(os.path.join(HERE, "steps.npz"), **step_vectors(ref))
     np.savez_compressed(os.path.join(HERE, "soft.npz"), **soft_vectors(ref))
     print("golden vectors written to", HERE)
@@ -472,7 +502,11 @@ def main(ref_root):
 
 if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    if len(sys.argv) > 2 and sys.argv[2] == "p2m":
+    if len(sys.argv) > 2 and sys.argv[2] == "m2p":
+        # only the mesh-to-particle vectors (needs oracle/_ref/libref_p2m.so)
+        np.savez_compressed(os.path.join(HERE, "m2p.npz"), **m2p_vectors())
+        print("m2p vectors written to", HERE)
+    elif len(sys.argv) > 2 and sys.argv[2] == "p2m":
         # only the particle remeshing vectors
         _install_reference(root)
         np.savez_compressed(os.path.join(HERE, "p2m.npz"), **p2m_vectors())

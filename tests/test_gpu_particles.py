@@ -73,3 +73,38 @@ def test_advect_vorticity_via_particles_matches_oracle_larger(nr, nz):
             ref_fn(zp, rp, vp, w_ref, Zd, Rd, nr, uz, ur, dx, dt)
             fn(zt, rt, vt, w, Zt, Rt, nr, ut, vr, dx, dt)
         np.testing.assert_array_equal(w.cpu().numpy(), w_ref)
+
+
+@pytest.mark.parametrize("tag", ["a", "b", "c"])
+def test_mesh_to_particles_matches_reference_golden(golden, tag):
+    """Mesh-to-particle MP4 (periodic and unbounded) on the device against
+    the reference's C++ results, bit for bit: particles in and around the
+    mesh, particle arrays shaped differently from the mesh."""
+    from pyaxisymflow_gb300.core.mesh_to_particles import (mesh_to_particles_2D_mp4,
+                                                           mesh_to_particles_2D_unbounded_mp4)
+    g = golden("m2p")
+    fx, fy, px, py = (torch.tensor(g[f"{tag}/{k}"], device="cuda")
+                      for k in ("fx", "fy", "px", "py"))
+    dx = float(g[f"{tag}/dx"])
+    for name, fn in (("periodic", mesh_to_particles_2D_mp4),
+                     ("unbounded", mesh_to_particles_2D_unbounded_mp4)):
+        ox, oy = torch.zeros_like(px), torch.zeros_like(px)
+        fn(fx, fy, px, py, ox, oy, dx, dx)
+        assert np.array_equal(ox.cpu().numpy(), g[f"{tag}/{name}_x"]), name
+        assert np.array_equal(oy.cpu().numpy(), g[f"{tag}/{name}_y"]), name
+
+
+def test_mesh_to_particles_matches_oracle_at_size():
+    from oracle import kernels as K
+    from pyaxisymflow_gb300.core.mesh_to_particles import mesh_to_particles_2D_unbounded_mp4
+    rng = np.random.default_rng(21)
+    n0, n1, dx = 256, 384, 1.0 / 256
+    fx, fy = rng.standard_normal((n0, n1)), rng.standard_normal((n0, n1))
+    px = rng.uniform(-1, n1 + 1, (300, 200)) * dx
+    py = rng.uniform(-1, n0 + 1, (300, 200)) * dx
+    ox, oy = np.zeros(px.shape), np.zeros(px.shape)
+    K.mesh_to_particles_2D_unbounded_mp4(fx, fy, px, py, ox, oy, dx, dx)
+    t = [torch.tensor(a, device="cuda") for a in (fx, fy, px, py)]
+    gx, gy = torch.zeros_like(t[2]), torch.zeros_like(t[2])
+    mesh_to_particles_2D_unbounded_mp4(*t, gx, gy, dx, dx)
+    assert np.array_equal(gx.cpu().numpy(), ox) and np.array_equal(gy.cpu().numpy(), oy)

@@ -277,3 +277,19 @@ def test_level_set_oracle_recovers_circle_distance():
     assert np.array_equal(np.sign(d[band]), np.sign(exact[band]))
     # outside the band the values are kept
     assert np.array_equal(d[~band], distorted[~band])
+
+
+def test_m2p_oracle_matches_reference_golden(golden):
+    """Mesh-to-particle MP4 restatement against vectors computed by the
+    reference's C++ (core/src/mesh_to_particles.hpp), bit for bit."""
+    from oracle import kernels as K
+    g = golden("m2p")
+    for tag in ("a", "b", "c"):
+        fx, fy, px, py = (g[f"{tag}/{k}"] for k in ("fx", "fy", "px", "py"))
+        dx = float(g[f"{tag}/dx"])
+        for name, fn in (("periodic", K.mesh_to_particles_2D_mp4),
+                         ("unbounded", K.mesh_to_particles_2D_unbounded_mp4)):
+            ox, oy = np.zeros(px.shape), np.zeros(px.shape)
+            fn(fx, fy, px, py, ox, oy, dx, dx)
+            assert np.array_equal(ox, g[f"{tag}/{name}_x"]), (tag, name)
+            assert np.array_equal(oy, g[f"{tag}/{name}_y"]), (tag, name)
