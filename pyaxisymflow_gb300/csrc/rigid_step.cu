@@ -1299,6 +1299,11 @@ int build_tc_jobs(const axi_case& k, axi_tc::TcJob job[4], bool dct) {
     AXI_TRY(axi_tc::encode_operand(&job[3].b_lo, w[1], nz, nr, nr));
     job[3].c = static_cast<float*>(k.psi); job[3].M = nr; job[3].N = nz;
     job[3].K = nr; job[3].ldc = nz; job[3].mode = axi_tc::MODE_PLAIN;
+    // both products store their tiles by TMA (outputs 16-byte aligned, nz % 4 == 0)
+    if (!axi_tc::encode_output(&job[1]) || !axi_tc::encode_output(&job[3])) {
+      axi::set_error("plan: tensor-core output map rejected (nz %d)", nz);
+      return AXI_ERR_INVALID;
+    }
     return AXI_OK;
   }
   // stage 0
@@ -1330,6 +1335,10 @@ int build_tc_jobs(const axi_case& k, axi_tc::TcJob job[4], bool dct) {
   AXI_TRY(axi_tc::encode_operand(&job[3].b_lo, w[1], nz, nr, nr));
   job[3].c = static_cast<float*>(k.psi); job[3].c_lo = nullptr; job[3].M = nr; job[3].N = nz;
   job[3].K = nr; job[3].ldc = nz; job[3].mode = axi_tc::MODE_PLAIN;
+  if (!axi_tc::encode_output(&job[3])) {
+    axi::set_error("plan: tensor-core output map rejected (nz %d)", nz);
+    return AXI_ERR_INVALID;
+  }
   return AXI_OK;
 }
 

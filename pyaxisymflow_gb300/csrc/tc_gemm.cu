@@ -75,6 +75,25 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int m, int n) {
          (static_cast<uint32_t>(m >> 4) << 24);
 }
 
+// TMA store of a 2-D box from shared memory (c0: innermost coordinate,
+// 128-byte aligned here) in this thread's bulk group, then committed.
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, uint32_t src, int c0,
+                                             int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];\n\t"
+      "cp.async.bulk.commit_group;" ::"l"(reinterpret_cast<uint64_t>(map)),
+      "r"(c0), "r"(c1), "r"(src)
+      : "memory");
+}
+// this thread's bulk stores have read their shared-memory source
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+// this thread's bulk stores are complete
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
 __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* m) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(m)) : "memory");
 }
@@ -97,11 +116,13 @@ __global__ void __launch_bounds__(THREADS, 1)
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + NSTAGE * STAGE_BYTES);
+  // epilogue staging first (1024-byte aligned, as the swizzled store boxes
+  // need), then the barriers
+  float* stage_out = reinterpret_cast<float*>(smem + NSTAGE * STAGE_BYTES);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + NSTAGE * STAGE_BYTES + EPI_STAGE_BYTES);
   // full[NSTAGE], empty[NSTAGE], acc_full[2], acc_empty[2], quiet
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * NSTAGE + 5);
   int* progress = reinterpret_cast<int*>(tmem_slot + 1);  // [0] loads issued, [1] consumed
-  float* stage_out = reinterpret_cast<float*>(smem + NSTAGE * STAGE_BYTES + 256);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + NSTAGE);
   const uint32_t accf0 = smem_u32(bars + 2 * NSTAGE), acce0 = smem_u32(bars + 2 * NSTAGE + 2);
@@ -227,6 +248,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       float* const c_lo = job.c_lo;
       const float* const scl = job.scale;
       const int M = job.M, Nc = job.N, ldc = job.ldc, mode = job.mode;
+      const bool tma_out = job.c_tma != 0;
+      const CUtensorMap* const cmap = &job.c_map;
       const int buf = it & 1;
       const bool ok = mbar_wait(accf0 + 8 * buf, (it >> 1) & 1, err, ERR_EPILOGUE);
       // all lanes leave together; a failure elsewhere in the grid surfaces at
@@ -252,6 +275,23 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         uint32_t r[32];
         tmem_ld32(tmem + buf * BN + (static_cast<uint32_t>(32 * q) << 16) + cc * 32, r);
+        if (tma_out) {
+          // the warp's 32 x 32 block as one TMA store: row `lane` of the box,
+          // 16-byte chunk c at position c ^ (lane % 8) (128-byte swizzle,
+          // conflict-free), after the warp's previous store has read the box
+          char* box = reinterpret_cast<char*>(stage_out) + (warp - 2) * 4096;
+          if (lane == 0) bulk_wait_read();
+          __syncwarp();
+#pragma unroll
+          for (int c = 0; c < 8; ++c)
+            *reinterpret_cast<float4*>(box + lane * 128 + ((c ^ (lane & 7)) << 4)) =
+                make_float4(__uint_as_float(r[4 * c]), __uint_as_float(r[4 * c + 1]),
+                            __uint_as_float(r[4 * c + 2]), __uint_as_float(r[4 * c + 3]));
+          axi_tma::fence_proxy_async_smem();
+          __syncwarp();
+          if (lane == 0) tma_store_2d(cmap, smem_u32(box), tr.z + cc * 32, row0);
+          continue;
+        }
         // transpose the warp's 32 x 32 block so each store instruction writes
         // 32 consecutive columns of one row
 #pragma unroll
@@ -283,6 +323,10 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(acce0 + 8 * buf)
                                   : "memory");
     }
+    // every TMA store of this warp complete before the block's shared
+    // memory goes away
+    if (lane == 0) bulk_wait_all();
+    __syncwarp();
   }
   __syncthreads();
   if (threadIdx.x == 0 && progress[1] < progress[0]) {
@@ -326,6 +370,23 @@ int encode_operand(CUtensorMap* map, const float* base, int rows, int K, int ld)
     return AXI_ERR_CUDA;
   }
   return AXI_OK;
+}
+
+bool encode_output(TcJob* job) {
+  auto fn = encode_fn();
+  if (!fn || job->mode != MODE_PLAIN || (reinterpret_cast<uintptr_t>(job->c) & 15) != 0 ||
+      job->ldc % 4 != 0 || job->ldc < job->N)
+    return false;
+  const cuuint64_t dims[2] = {static_cast<cuuint64_t>(job->N), static_cast<cuuint64_t>(job->M)};
+  const cuuint64_t strides[1] = {static_cast<cuuint64_t>(job->ldc) * 4};
+  const cuuint32_t box[2] = {32, 32};
+  const cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(&job->c_map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, job->c, dims, strides, box,
+                  estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return false;
+  job->c_tma = 1;
+  return true;
 }
 
 void order_tiles_by_k(int4* tiles, int n, const TcJob* jobs) {
@@ -473,6 +534,7 @@ extern "C" int axi_tf32x3_gemm(float* C, const float* A, const float* B, int M, 
   job.K = K;
   job.ldc = N;
   job.mode = axi_tc::MODE_PLAIN;
+  axi_tc::encode_output(&job);  // TMA stores where the output allows them
   std::string tiles;
   for (int m0 = 0; m0 < M; m0 += axi_tc::BM)
     for (int n0 = 0; n0 < N; n0 += axi_tc::BN) {

@@ -17,10 +17,11 @@
 //                        TMEM; tcgen05.commit releases stages and accumulators
 //   warps 2-9            epilogue: tcgen05.ld (warp w reads TMEM lanes
 //                        32 (w % 4) .., warps 2-5 columns 0-63, warps 6-9
-//                        columns 64-127), a per-warp shared-memory transpose for
-//                        row-contiguous stores, and the stage-specific store
-//                        (plain, hi/lo split, or scaled then split); it drains
-//                        one accumulator while the MMAs fill the other
+//                        columns 64-127); plain outputs go out as one TMA store
+//                        per 32 x 32 block (128-byte swizzled shared-memory
+//                        box), the split and scaled forms through a per-warp
+//                        shared-memory transpose and row-contiguous stores; it
+//                        drains one accumulator while the MMAs fill the other
 // Every mbarrier wait is bounded by a 1 s wall-clock limit; on expiry the
 // kernel records an error code, drains its outstanding copies (bounded),
 // frees its TMEM and returns.
@@ -51,7 +52,11 @@ constexpr int TILE_BYTES = BM * BKF * 4;        // 16 KB per operand tile
 constexpr int STAGE_BYTES = 4 * TILE_BYTES;     // A_hi, A_lo, B_hi, B_lo
 constexpr int EPI_WARPS = 8;                    // two per TMEM lane quarter
 constexpr int THREADS = 32 * (2 + EPI_WARPS);   // TMA warp, MMA warp, 8 epilogue warps
-constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 + 256 + EPI_WARPS * 32 * 33 * 4;
+// epilogue staging: a 32 x 33-float transpose per warp, or (TMA stores) a
+// 32 x 32-float 128-byte-swizzled box per warp at 4 KB strides
+constexpr int EPI_STAGE_BYTES = EPI_WARPS * 32 * 33 * 4;
+static_assert(EPI_WARPS * 4096 <= EPI_STAGE_BYTES, "TMA store boxes fit the staging region");
+constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 + EPI_STAGE_BYTES + 256;
 
 enum { MODE_PLAIN = 0, MODE_SPLIT = 1, MODE_SCALE_SPLIT = 2, MODE_SCALE = 3 };
 enum { ERR_PRODUCER = 1, ERR_MMA = 2, ERR_EPILOGUE = 3, ERR_DRAIN = 4 };
@@ -60,11 +65,15 @@ enum { ERR_PRODUCER = 1, ERR_MMA = 2, ERR_EPILOGUE = 3, ERR_DRAIN = 4 };
 // and live in global memory next to the job.
 struct TcJob {
   CUtensorMap a_hi, a_lo, b_hi, b_lo;
+  CUtensorMap c_map;   // MODE_PLAIN with c_tma: the output in 32 x 32 boxes for TMA stores
   float* c;            // output (MODE_PLAIN) or its hi part
   float* c_lo;         // lo part (split modes)
   const float* scale;  // elementwise factor, row-major (M, N) (MODE_SCALE*)
   int M, N, K, ldc;
   int mode;
+  int c_tma;           // 1: the epilogue stores tiles through c_map. Every job of
+                       // one launch must agree (the two store paths lay out the
+                       // epilogue's shared memory differently).
 };
 
 // Nearest TF32 value of x (10 explicit mantissa bits, ties away from zero):
@@ -85,6 +94,12 @@ __device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
 // Host: encode a 2-D K-major FP32 operand (rows x K, row stride ld floats)
 // for 128-row x BKF-float boxes with the ROW_BYTES swizzle. Returns AXI status.
 int encode_operand(CUtensorMap* map, const float* base, int rows, int K, int ld);
+
+// Host: encode the output of a MODE_PLAIN job (rows x cols, row stride ld
+// floats) for 32 x 32-float TMA stores with the 128-byte swizzle; sets
+// job->c_tma. False (job untouched) when the output cannot be stored that way
+// (base not 16-byte aligned or ld not a multiple of 4).
+bool encode_output(TcJob* job);
 
 // Host: complete a tile table (job, m0, n0, -) with each tile's k-block
 // count (w = ceil(K / BKF), which the kernel reads instead of the job) and

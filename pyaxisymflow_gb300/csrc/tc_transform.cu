@@ -166,6 +166,13 @@ extern "C" int axi_tc_transform_plan(const axi_tc_transform* t, int n, void* pla
     j[3].c = k.out; j[3].M = nr; j[3].N = nz; j[3].K = nr; j[3].ldc = nz;
     j[3].mode = axi_tc::MODE_PLAIN;
   }
+  // stage 3 stores its tiles by TMA when every case's output allows it (the
+  // jobs of one launch must agree)
+  bool all_tma = true;
+  for (int q = 0; q < n && all_tma; ++q)
+    all_tma = axi_tc::encode_output(&reinterpret_cast<axi_tc::TcJob*>(&buf[L.jobs])[4 * q + 3]);
+  if (!all_tma)
+    for (int q = 0; q < n; ++q) reinterpret_cast<axi_tc::TcJob*>(&buf[L.jobs])[4 * q + 3].c_tma = 0;
   for (int st = 0; st < 4; ++st) {
     int4* tt = reinterpret_cast<int4*>(&buf[L.tiles[st]]);
     int qq = 0;
