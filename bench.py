@@ -51,12 +51,12 @@ PHASE_FIELDS = {"vel_max": 1, "penalise": 6, "advect_diffuse": 4}
 # ncu captures summarised in profiles/ (transform: sum over its four products).
 # DRAM bytes (read + write) per launch of each step kernel, ensemble64 FP32
 # engine, from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum,
-# averaged over the launches of two steps)
+# averaged over the launches of three steps)
 NCU_TRAFFIC = {
-    ("ensemble64", "f32", "r_products"): 190.2e6,
-    ("ensemble64", "f32", "z_transforms"): 168.5e6,
-    ("ensemble64", "f32", "advect_diffuse"): 325.1e6,
-    ("ensemble64", "f32", "penalise"): 389.1e6,
+    ("ensemble64", "f32", "r_products"): 193.4e6,
+    ("ensemble64", "f32", "z_transforms"): 178.7e6,
+    ("ensemble64", "f32", "advect_diffuse"): 325.6e6,
+    ("ensemble64", "f32", "penalise"): 389.4e6,
     ("ensemble64", "f32", "vel_max"): 74.0e6,
 }
 # remeshing (2048 x 1024 cells, 4.19 M particles): FP64 instructions per
