@@ -140,8 +140,10 @@ __device__ __forceinline__ unsigned int dev_tiles_of(const axi_case& k) {
 constexpr int KILL_BLOCKS = 4;  // blocks per case (grid x)
 
 template <typename T>
-__global__ void __launch_bounds__(256) kill_reset_kernel(const axi_case* __restrict__ cases) {
+__global__ void __launch_bounds__(256) kill_reset_kernel(const axi_case* __restrict__ cases,
+                                                         unsigned int* __restrict__ vm_done) {
   const axi_case& k = cases[blockIdx.y];
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *vm_done = 0u;  // vel_max arrivals
   T* w = F<T>(k.omega);
   const int nr = k.nr, nz = k.nz, wd = k.kill_width;
   // taper factors sin(pi (Z - dx/2) / 2 / (w - 1) / dx) etc., evaluated once on
@@ -350,14 +352,48 @@ __device__ __forceinline__ int ring_prologue(const Ring& ring, const CUtensorMap
 
 // ---------------------------------------------------------------------------
 // vel_max: max over the case of |u_z| + |u_r| (flow_past_sphere.py:150-153),
-// one atomic maximum per tile. step_dt_kernel turns it into dt (one thread
-// per case), so no tile waits on a per-case counter.
+// one atomic maximum per tile; the last block to finish (a grid-wide arrival
+// count, reset by kill_reset each step) turns every case's maximum into dt,
+// so no tile waits on another.
 // ---------------------------------------------------------------------------
 template <typename T>
 __device__ __forceinline__ unsigned long long order_bits(T v) {
   // non-negative values order like their bit patterns; a NaN sorts above +inf
   return sizeof(T) == 8 ? (unsigned long long)__double_as_longlong((double)v)
                         : (unsigned long long)__float_as_uint((float)v);
+}
+
+// dt = min(diffusive limit, CFL / max(|u_z| + |u_r|)) (flow_past_sphere.py:150-155)
+// from the maximum that vel_max left in the state block. Every block that
+// needs dt evaluates it from the same bits, so all get the same value.
+template <typename T>
+__device__ __forceinline__ double step_dt(const axi_case& k, double* umax_out = nullptr) {
+  const unsigned long long mb =
+      *reinterpret_cast<const volatile unsigned long long*>(&k.state[AXI_ST_UMAX]);
+  const double umax = sizeof(T) == 8 ? __longlong_as_double((long long)mb)
+                                     : (double)__uint_as_float((unsigned int)mb);
+  if (umax_out) *umax_out = umax;
+  return fmin(k.dt_diff, (k.cfl * k.dx) / (umax + k.eps));
+}
+
+// dt and the dt-dependent constants of the step for one case (double state
+// words and the float copies), once vel_max has its maximum.
+template <typename T>
+__device__ __forceinline__ void finish_step_dt(const axi_case& k) {
+  double umax;
+  const double dt = step_dt<T>(k, &umax);
+  if (!(umax <= 1.7976931348623157e308))
+    atomicOr(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_STATUS]), 1u << AXI_ERR_NONFINITE);
+  k.state[AXI_ST_DT] = dt;
+  k.state[AXI_ST_LAMDT] = k.lam * dt;
+  k.state[AXI_ST_ADV] = -dt / k.dx;
+  k.state[AXI_ST_C1] = 0.5 * k.nu * dt;
+  k.state[AXI_ST_C2] = k.nu * dt;
+  float* f = fslots(k);
+  f[SF_LAMDT] = (float)(k.lam * dt);
+  f[SF_ADV] = (float)(-dt / k.dx);
+  f[SF_C1] = (float)(0.5 * k.nu * dt);
+  f[SF_C2] = (float)(k.nu * dt);
 }
 
 template <typename T>
@@ -371,7 +407,8 @@ template <typename T>
 __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict__ cases,
                                                      const int4* __restrict__ tiles, int n_tiles,
                                                      const CUtensorMap* __restrict__ maps,
-                                                     int* __restrict__ err) {
+                                                     int* __restrict__ err, int n_cases,
+                                                     unsigned int* __restrict__ done) {
   extern __shared__ unsigned char vm_raw[];
   __shared__ __align__(8) uint64_t bars[VM_NBUF];
   __shared__ unsigned long long wm[2][NT / 32];
@@ -442,6 +479,19 @@ __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict_
     }
   }
   if (!ok && threadIdx.x == 0) ring.drain(it, issued, err);
+  // every block arrives (a failed one too); the last one sees every tile's
+  // atomic maximum and computes dt for all cases
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    for (int c = threadIdx.x; c < n_cases; c += NT) finish_step_dt<T>(cases[c]);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -452,42 +502,6 @@ __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict_
 // drag integrand); the curl of the difference then updates omega of the
 // owned cells.
 // ---------------------------------------------------------------------------
-// dt = min(diffusive limit, CFL / max(|u_z| + |u_r|)) (flow_past_sphere.py:150-155)
-// from the maximum that vel_max left in the state block. Every block that
-// needs dt evaluates it from the same bits, so all get the same value.
-template <typename T>
-__device__ __forceinline__ double step_dt(const axi_case& k, double* umax_out = nullptr) {
-  const unsigned long long mb =
-      *reinterpret_cast<const volatile unsigned long long*>(&k.state[AXI_ST_UMAX]);
-  const double umax = sizeof(T) == 8 ? __longlong_as_double((long long)mb)
-                                     : (double)__uint_as_float((unsigned int)mb);
-  if (umax_out) *umax_out = umax;
-  return fmin(k.dt_diff, (k.cfl * k.dx) / (umax + k.eps));
-}
-
-// One thread per case: dt and the dt-dependent constants of the step (double
-// state words and the float copies), between vel_max and penalise.
-template <typename T>
-__global__ void step_dt_kernel(const axi_case* __restrict__ cases, int n_cases) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n_cases) return;
-  const axi_case& k = cases[c];
-  double umax;
-  const double dt = step_dt<T>(k, &umax);
-  if (!(umax <= 1.7976931348623157e308))
-    atomicOr(reinterpret_cast<unsigned int*>(&k.state[AXI_ST_STATUS]), 1u << AXI_ERR_NONFINITE);
-  k.state[AXI_ST_DT] = dt;
-  k.state[AXI_ST_LAMDT] = k.lam * dt;
-  k.state[AXI_ST_ADV] = -dt / k.dx;
-  k.state[AXI_ST_C1] = 0.5 * k.nu * dt;
-  k.state[AXI_ST_C2] = k.nu * dt;
-  float* f = fslots(k);
-  f[SF_LAMDT] = (float)(k.lam * dt);
-  f[SF_ADV] = (float)(-dt / k.dx);
-  f[SF_C1] = (float)(0.5 * k.nu * dt);
-  f[SF_C2] = (float)(k.nu * dt);
-}
-
 template <typename T>
 __device__ __forceinline__ void penalise_point(T uz, T ur, T lc, T ubody, T& pz, T& pr) {
   const T inv = T(1) / (T(1) + lc);
@@ -1447,7 +1461,8 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
   const int nt = info->n_stencil_tiles, ng = info->n_gemm_tiles;
   switch (phase) {
     case PH_KILL:
-      kill_reset_kernel<T><<<dim3(KILL_BLOCKS, info->n_cases), 256, 0, s>>>(v.cases);
+      kill_reset_kernel<T><<<dim3(KILL_BLOCKS, info->n_cases), 256, 0, s>>>(
+          v.cases, reinterpret_cast<unsigned int*>(v.err + 1));
       break;
     case PH_TRANSFORM:
       if (v.dct_jobs) {
@@ -1472,8 +1487,8 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
     case PH_VEL_MAX:
       AXI_TRY(stencil_attrs<T>());
       vel_max_kernel<T><<<StencilGrid<T>::get(PH_VEL_MAX, nt), NT, vel_max_smem<T>(), s>>>(
-          v.cases, v.stencil, nt, v.maps, v.err);
-      step_dt_kernel<T><<<(info->n_cases + 127) / 128, 128, 0, s>>>(v.cases, info->n_cases);
+          v.cases, v.stencil, nt, v.maps, v.err, info->n_cases,
+          reinterpret_cast<unsigned int*>(v.err + 1));
       break;
     case PH_PENALISE:
       AXI_TRY(stencil_attrs<T>());
