@@ -718,8 +718,18 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 2) penalise_kernel(co
 template <typename T>
 __device__ __forceinline__ T face_flux(T fm1, T f0, T f1, T f2, T um1, T u0, T u1, T u2) {
   const T third = T(1) / T(3), five6 = T(5) / T(6), sixth = T(1) / T(6);
-  if (u0 > -u1) return third * f1 * u1 + five6 * f0 * u0 - sixth * fm1 * um1;
-  return third * f0 * u0 + five6 * f1 * u1 - sixth * f2 * u2;
+  if constexpr (sizeof(T) == 4) {
+    // FP32 engine: the flux values f u formed once, shared by both upwind
+    // branches and (after inlining) by the neighbouring faces of a point
+    const T gm1 = fm1 * um1, g0 = f0 * u0, g1 = f1 * u1, g2 = f2 * u2;
+    const T a = third * g1 + five6 * g0 - sixth * gm1;
+    const T b = third * g0 + five6 * g1 - sixth * g2;
+    return u0 > -u1 ? a : b;
+  } else {
+    // the reference's products and order (bit-exact with the FP64 oracle)
+    if (u0 > -u1) return third * f1 * u1 + five6 * f0 * u0 - sixth * fm1 * um1;
+    return third * f0 * u0 + five6 * f1 * u1 - sixth * f2 * u2;
+  }
 }
 
 // Smoothed Heaviside of a sphere level set (kernels/smooth_Heaviside.py:10-14,
