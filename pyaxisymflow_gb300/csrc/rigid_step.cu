@@ -715,16 +715,21 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 2) penalise_kernel(co
 // ---------------------------------------------------------------------------
 // ENO3 face flux (pyst_kernels/advection_flux.py:9-163)
 // ---------------------------------------------------------------------------
+// FP32 engine: the face flux from the flux values g = f u of the four points
+// (formed once, shared by both upwind branches and by neighbouring faces)
+template <typename T>
+__device__ __forceinline__ T face_flux_g(T gm1, T g0, T g1, T g2, T u0, T u1) {
+  const T third = T(1) / T(3), five6 = T(5) / T(6), sixth = T(1) / T(6);
+  const T a = third * g1 + five6 * g0 - sixth * gm1;
+  const T b = third * g0 + five6 * g1 - sixth * g2;
+  return u0 > -u1 ? a : b;
+}
+
 template <typename T>
 __device__ __forceinline__ T face_flux(T fm1, T f0, T f1, T f2, T um1, T u0, T u1, T u2) {
   const T third = T(1) / T(3), five6 = T(5) / T(6), sixth = T(1) / T(6);
   if constexpr (sizeof(T) == 4) {
-    // FP32 engine: the flux values f u formed once, shared by both upwind
-    // branches and (after inlining) by the neighbouring faces of a point
-    const T gm1 = fm1 * um1, g0 = f0 * u0, g1 = f1 * u1, g2 = f2 * u2;
-    const T a = third * g1 + five6 * g0 - sixth * gm1;
-    const T b = third * g0 + five6 * g1 - sixth * g2;
-    return u0 > -u1 ? a : b;
+    return face_flux_g(fm1 * um1, f0 * u0, f1 * u1, f2 * u2, u0, u1);
   } else {
     // the reference's products and order (bit-exact with the FP64 oracle)
     if (u0 > -u1) return third * f1 * u1 + five6 * f0 * u0 - sixth * fm1 * um1;
@@ -894,11 +899,23 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) advect_diffuse_ker
       T fm2 = sw[c - 2 * L], fm1 = sw[c - L], f0 = sw[c], f1 = sw[c + L];
       T um2 = sr[c - 2 * L], um1 = sr[c - L], u0 = sr[c], u1 = sr[c + L];
       T yb = face_flux(fm2, fm1, f0, f1, um2, um1, u0, u1);
+      // FP32: the flux values of the window rows carried along (one new
+      // product per row); unused, and removed, in the FP64 engine
+      T gm1 = fm1 * um1, g0 = f0 * u0, g1 = f1 * u1;
 #pragma unroll 1
       for (int m = 0; m < AD_RA; ++m, c += L) {
         const int pr = p0 + m, gi = i0 + pr;
         const T f2 = sw[c + 2 * L], u2 = sr[c + 2 * L];
-        const T yf = face_flux(fm1, f0, f1, f2, um1, u0, u1, u2);
+        T yf;
+        if constexpr (sizeof(T) == 4) {
+          const T g2 = f2 * u2;
+          yf = face_flux_g(gm1, g0, g1, g2, u0, u1);
+          gm1 = g0;
+          g0 = g1;
+          g1 = g2;
+        } else {
+          yf = face_flux(fm1, f0, f1, f2, um1, u0, u1, u2);
+        }
         T val = T(0);
         if (jin && gi >= 0 && gi < nr) {
           T flux = T(0);
