@@ -538,11 +538,16 @@ __device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* 
       __syncwarp();
       // Z[k] and Z[N-k] both depend on X[k] and X[N-k] only: each lane
       // rewrites its own pairs in place
+      // (unrolled by 4 so the rotation-table loads of several k are in flight
+      // together)
+      const float2* __restrict__ rot = job.rot;
+#pragma unroll 4
       for (int k = lane; k <= N / 2; k += 32) {
+        const float2 rk = __ldg(rot + k), rn = __ldg(rot + (N - k) % N);
         const float2 xk = buf[k];
         const float2 xn = k == 0 ? make_float2(0.0f, 0.0f) : buf[N - k];
-        const float2 zk = inverse_pre(job.rot[k], xk, xn);
-        if (k != 0 && k != N / 2) buf[N - k] = inverse_pre(job.rot[N - k], xn, xk);
+        const float2 zk = inverse_pre(rk, xk, xn);
+        if (k != 0 && k != N / 2) buf[N - k] = inverse_pre(rn, xn, xk);
         buf[k] = zk;
       }
       __syncwarp();
@@ -555,6 +560,7 @@ __device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* 
   // of an item and the output offsets are multiples of 4)
   constexpr int G = RR / 4;
   if (forward) {
+#pragma unroll 4
     for (int t = threadIdx.x; t < G * N; t += blockDim.x) {
       const int k = t / G, g = t - k * G;
       const int r0 = 4 * g;
@@ -576,6 +582,7 @@ __device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* 
     }
   } else {
     const float inv_n = 1.0f / (float)N;
+#pragma unroll 4
     for (int t = threadIdx.x; t < G * N; t += blockDim.x) {
       const int j = t / G, g = t - j * G;
       const int r0 = 4 * g;
