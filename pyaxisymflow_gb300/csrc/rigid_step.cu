@@ -519,7 +519,7 @@ constexpr int penalise_smem() {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 2) penalise_kernel(const axi_case* __restrict__ cases,
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 2) penalise_kernel(const axi_case* __restrict__ cases,
                                                       const int4* __restrict__ tiles, int n_tiles,
                                                       const CUtensorMap* __restrict__ maps,
                                                       int* __restrict__ err, int ahead) {
