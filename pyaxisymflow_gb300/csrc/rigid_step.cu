@@ -352,7 +352,7 @@ __device__ __forceinline__ int ring_prologue(const Ring& ring, const CUtensorMap
 
 // ---------------------------------------------------------------------------
 // vel_max: max over the case of |u_z| + |u_r| (flow_past_sphere.py:150-153),
-// one atomic maximum per tile; the last block to finish (a grid-wide arrival
+// atomic maxima per warp; the last block to finish (a grid-wide arrival
 // count, reset by kill_reset each step) turns every case's maximum into dt,
 // so no tile waits on another.
 // ---------------------------------------------------------------------------
@@ -411,7 +411,6 @@ __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict_
                                                      unsigned int* __restrict__ done) {
   extern __shared__ unsigned char vm_raw[];
   __shared__ __align__(8) uint64_t bars[VM_NBUF];
-  __shared__ unsigned long long wm[2][NT / 32];
   VmRing<T> ring{reinterpret_cast<T*>(align_smem(vm_raw)), axi_tma::smem_u32(bars)};
   constexpr int which[1] = {MAP_PSI};
   int issued = 0;
@@ -425,13 +424,6 @@ __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict_
   int it = 0;
   bool ok = true;
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
-    if (threadIdx.x == 0) {
-      const int tn = t + (VM_NBUF - 1) * gridDim.x;
-      if (tn < n_tiles) {
-        ring.issue(maps, tiles[tn], which, -2, (it + VM_NBUF - 1) % VM_NBUF);
-        ++issued;
-      }
-    }
     const int4 tr = tiles[t];
     const axi_case& k = cases[tr.x];
     const int nr = k.nr, nz = k.nz;
@@ -440,6 +432,15 @@ __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict_
     if (!ring.wait_all(it, err)) {
       ok = false;
       break;
+    }
+    // past the ring's block barrier every warp has finished tile it - 1, so
+    // its slot can take the tile VM_NBUF - 1 ahead
+    if (threadIdx.x == 0) {
+      const int tn = t + (VM_NBUF - 1) * gridDim.x;
+      if (tn < n_tiles) {
+        ring.issue(maps, tiles[tn], which, -2, (it + VM_NBUF - 1) % VM_NBUF);
+        ++issued;
+      }
     }
     const T* bx = ring.box(it % VM_NBUF, 0);
     const int i0 = tr.y, j0 = tr.z;
@@ -469,14 +470,11 @@ __global__ void __launch_bounds__(NT) vel_max_kernel(const axi_case* __restrict_
       const unsigned long long other = __shfl_down_sync(0xffffffffu, bits, o);
       bits = other > bits ? other : bits;
     }
-    if ((threadIdx.x & 31) == 0) wm[it & 1][threadIdx.x >> 5] = bits;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      unsigned long long m = 0;
-      for (int q = 0; q < NT / 32; ++q) m = wm[it & 1][q] > m ? wm[it & 1][q] : m;
-      // fire-and-forget: the maximum is read after this kernel has finished
-      atomicMax(reinterpret_cast<unsigned long long*>(&k.state[AXI_ST_UMAX]), m);
-    }
+    // one fire-and-forget atomic maximum per warp (no block barrier: the ring
+    // wait at the top of the next tile orders the box reuse); the maximum is
+    // read once every block has arrived
+    if ((threadIdx.x & 31) == 0 && bits != 0)
+      atomicMax(reinterpret_cast<unsigned long long*>(&k.state[AXI_ST_UMAX]), bits);
   }
   if (!ok && threadIdx.x == 0) ring.drain(it, issued, err);
   // every block arrives (a failed one too); the last one sees every tile's
