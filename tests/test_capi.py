@@ -39,3 +39,39 @@ def test_no_cpu_fallback_for_cpu_tensors():
     t = torch.zeros((4, 4), dtype=torch.float64)
     with pytest.raises(ValueError, match="CUDA"):
         brinkmann_penalize(1.0, 1.0, t, 0.0, 0.0, t, t, t, t)
+
+
+def test_new_entry_points_reject_bad_arguments_before_any_launch():
+    """Argument checks of the particle, mesh-to-particle and level-set entry
+    points run on the host before anything touches the GPU: null pointers,
+    bad sizes and aliasing come back as AXI_ERR_INVALID with a message naming
+    the call (fake non-null pointers are never dereferenced)."""
+    import ctypes as c
+
+    from pyaxisymflow_gb300 import _native as N
+    lib = N.lib()
+    P = c.c_void_p
+    fake = P(4096)  # never dereferenced: every call below fails its checks first
+    null = P(None)
+
+    st = lib.axi_level_set_distance_f64(null, fake, 8, 8, 0.1, 0.5, null, fake, null)
+    assert st == N.AXI_ERR_INVALID and b"level_set_distance" in lib.axi_last_error()
+    st = lib.axi_level_set_distance_f64(fake, fake, 8, 8, 0.1, 0.5, null, fake, null)
+    assert st == N.AXI_ERR_INVALID and b"alias" in lib.axi_last_error()
+    st = lib.axi_level_set_distance_f64(P(8192), fake, 8, 8, 0.0, 0.5, null, fake, null)
+    assert st == N.AXI_ERR_INVALID
+    st = lib.axi_level_set_distance_f64(P(8192), fake, 1, 8, 0.1, 0.5, null, fake, null)
+    assert st == N.AXI_ERR_INVALID
+    assert lib.axi_level_set_work_bytes(1, 8) == 0 and lib.axi_level_set_work_bytes(8, 8) > 0
+
+    st = lib.axi_mesh_to_particles_2d_mp4_f64(fake, fake, 0, 8, fake, fake, fake, fake, 4, 4,
+                                              0.1, 0.1, 1, null)
+    assert st == N.AXI_ERR_INVALID and b"mesh_to_particles" in lib.axi_last_error()
+    st = lib.axi_mesh_to_particles_2d_mp4_f64(fake, null, 8, 8, fake, fake, fake, fake, 4, 4,
+                                              0.1, 0.1, 1, null)
+    assert st == N.AXI_ERR_INVALID
+
+    st = lib.axi_particles_to_mesh_2d_mp4_f64(fake, fake, fake, fake, 4, 8, 0.1, 0.1, 0, fake,
+                                              null)
+    assert st == N.AXI_ERR_INVALID and b"particles_to_mesh" in lib.axi_last_error()
+    assert lib.axi_p2m_mp4_work_bytes(0, 8) == 0
