@@ -6,13 +6,13 @@
 * oracle/_ref/libref_p2m.so: the reference's particle-to-mesh and
   mesh-to-particle interpolation (core/src/particles_to_mesh.hpp,
   core/src/mesh_to_particles.hpp) through oracle/ref_p2m_shim.cpp.
-Built only where the reference sources exist; never shipped.
+Built only where the reference sources exist (their root is given by the
+caller or by the PYAXISYMFLOW_REF environment variable); never shipped.
 """
 import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("PYAXISYMFLOW_REF", "/root/reference")
 REF_DIR = os.path.join(HERE, "_ref")
 
 
@@ -24,8 +24,14 @@ def ref_p2m_path():
     return os.path.join(REF_DIR, "libref_p2m.so")
 
 
-def _build_shim(shim_name, out):
-    src_dir = os.path.join(REF_ROOT, "pyaxisymflow", "core", "src")
+def _ref_root(ref_root):
+    return ref_root if ref_root else os.environ.get("PYAXISYMFLOW_REF")
+
+
+def _build_shim(shim_name, out, ref_root):
+    if not ref_root:
+        return None
+    src_dir = os.path.join(ref_root, "pyaxisymflow", "core", "src")
     if not os.path.isdir(src_dir):
         return None
     os.makedirs(REF_DIR, exist_ok=True)
@@ -39,17 +45,20 @@ def _build_shim(shim_name, out):
     return out
 
 
-def build_ref():
-    return _build_shim("ref_shim.cpp", ref_lsq_path())
+def build_ref(ref_root=None):
+    return _build_shim("ref_shim.cpp", ref_lsq_path(), _ref_root(ref_root))
 
 
-def build_ref_p2m():
-    return _build_shim("ref_p2m_shim.cpp", ref_p2m_path())
+def build_ref_p2m(ref_root=None):
+    return _build_shim("ref_p2m_shim.cpp", ref_p2m_path(), _ref_root(ref_root))
 
 
-def build_all():
-    return {"ref_lsq": build_ref(), "ref_p2m": build_ref_p2m()}
+def build_all(ref_root=None):
+    """Builds what the given reference root (or PYAXISYMFLOW_REF) allows;
+    nothing without one."""
+    return {"ref_lsq": build_ref(ref_root), "ref_p2m": build_ref_p2m(ref_root)}
 
 
 if __name__ == "__main__":
-    print(build_all())
+    import sys
+    print(build_all(sys.argv[1] if len(sys.argv) > 1 else None))

@@ -19,9 +19,21 @@ What runs unmodified from the reference:
     (``oracle/_ref/libref_lsq.so``, ``oracle/_ref/libref_p2m.so``), and
     ``kernels/advect_particle.py`` over the latter.
 
-What cannot run: the pystencils ENO3 kernels (pystencils is not installed).
-Full-step vectors therefore use the oracle's ENO3 restatement for the
-advection call only; everything else in those loops is the reference's code.
+  * the pystencils ENO3 advection kernels (``pyst_kernels/advection_flux.py``,
+    ``advection_timestep.py``, ``elementwise_ops.py``) and the closures that
+    call them (``kernels/advect_vorticity_via_eno3.py``,
+    ``elasto_kernels/advect_refmap_via_eno3.py``): pystencils is not
+    installed, so ``tests/golden/pystencils_standin`` (a test-only restatement
+    of the pystencils subset they use) takes its place. The kernels' own
+    symbolic expressions are built, ordered and printed by sympy and evaluated
+    literally in IEEE double (what pystencils' compiler flags may reorder is
+    not modelled).
+
+The full-step vectors (rigid, sedimenting and soft loops) therefore run the
+reference's code for every kernel of the step, ENO3 included.
+
+Run with the path of the reference sources as the first argument; nothing is
+written into that tree (bytecode writing is switched off).
 """
 import ctypes
 import os
@@ -40,6 +52,9 @@ from oracle import simulation as sim  # noqa: E402
 
 
 def _install_reference(ref_root):
+    # the reference tree is read-only source: no __pycache__ written into it
+    sys.dont_write_bytecode = True
+    sys.path.insert(0, os.path.join(HERE, "pystencils_standin"))
     stub = tempfile.mkdtemp(prefix="numba_stub_")
     os.makedirs(os.path.join(stub, "numba"))
     with open(os.path.join(stub, "numba", "__init__.py"), "w") as f:
@@ -77,6 +92,8 @@ def _ref_kernels():
     from pyaxisymflow.kernels import FastDiagonalisationStokesSolver as fs
     from pyaxisymflow.kernels import FastDiagonalisationPotentialSolver as fpo
     from pyaxisymflow.kernels import implicit_diffusion_solver as ids
+    from pyaxisymflow.kernels import advect_vorticity_via_eno3 as aw
+    from pyaxisymflow.elasto_kernels import advect_refmap_via_eno3 as ae
 
     ns = types.SimpleNamespace(
         brinkmann_penalize=bp.brinkmann_penalize,
@@ -98,6 +115,10 @@ def _ref_kernels():
         FastDiagonalisationStokesSolver=fs.FastDiagonalisationStokesSolver,
         FastDiagonalisationPotentialSolver=fpo.FastDiagonalisationPotentialSolver,
         ImplicitEulerDiffusionStepper=ids.ImplicitEulerDiffusionStepper,
+        gen_advect_vorticity_via_eno3=aw.gen_advect_vorticity_via_eno3,
+        gen_advect_vorticity_via_eno3_periodic=aw.gen_advect_vorticity_via_eno3_periodic,
+        gen_advect_refmap_via_eno3=ae.gen_advect_refmap_via_eno3,
+        gen_advect_refmap_via_eno3_periodic=ae.gen_advect_refmap_via_eno3_periodic,
         extrapolate_eta_with_least_squares=None,
     )
     return ns
@@ -325,7 +346,7 @@ def lsq_vectors(extrap_first_order):
 
 
 def step_vectors(ref):
-    """Full-step loops on small grids, reference kernels + oracle ENO3."""
+    """Full-step loops on small grids, every kernel the reference's own."""
     out = {}
     # rigid sphere (flow past sphere), config-1 geometry scaled to 64 x 32
     case = sim.RigidSphereCase(nz=64, nr=32, dx=2.0 / 64, r_sphere=0.125, z_cm=0.5)
@@ -333,7 +354,7 @@ def step_vectors(ref):
     out["rigid/omega0"] = st.vorticity.copy()
     out["rigid/chi"] = st.char_func.copy()
     solver = ref.FastDiagonalisationStokesSolver(case.nr, case.nz, case.dx)
-    adv = OK.gen_advect_vorticity_via_eno3(case.dx, case.nr, case.nz)
+    adv = ref.gen_advect_vorticity_via_eno3(case.dx, case.nr, case.nz)
     dts, cds = [], []
     for n in range(40):
         sim.rigid_sphere_step(case, st, coords, solver, adv, ref)
@@ -354,7 +375,7 @@ def step_vectors(ref):
     sst, scoords = sim.sedimenting_init(scase, ref, vorticity=w0)
     out["sediment/omega0"] = w0
     ssolver = ref.FastDiagonalisationStokesSolver(scase.nr, scase.nz, scase.dx)
-    sadv = OK.gen_advect_vorticity_via_eno3(scase.dx, scase.nr, scase.nz)
+    sadv = ref.gen_advect_vorticity_via_eno3(scase.dx, scase.nr, scase.nz)
     hist = []
     for n in range(30):
         sim.sedimenting_step(scase, sst, scoords, ssolver, sadv, ref)
@@ -370,8 +391,8 @@ def soft_vectors(ref):
     case = sim.SoftSphereCase(nz=64, nr=32, dx=1.0 / 64, r_ball=0.15, lam=1e6)
     st, coords = sim.soft_sphere_init(case, ref)
     solver = ref.FastDiagonalisationStokesSolver(case.nr, case.nz, case.dx)
-    adv_w = OK.gen_advect_vorticity_via_eno3(case.dx, case.nr, case.nz)
-    adv_e = OK.gen_advect_refmap_via_eno3(case.dx, case.nr, case.nz)
+    adv_w = ref.gen_advect_vorticity_via_eno3(case.dx, case.nr, case.nz)
+    adv_e = ref.gen_advect_refmap_via_eno3(case.dx, case.nr, case.nz)
     for n in range(12):
         sim.soft_sphere_step(case, st, coords, solver, adv_w, adv_e, ref)
     out["soft/omega_12"] = st.vorticity.copy()
@@ -380,6 +401,56 @@ def soft_vectors(ref):
     out["soft/phi_12"] = st.ball_phi.copy()
     out["soft/chi_12"] = st.ball_char_func.copy()
     out["soft/t_12"] = np.array(st.t)
+    return out
+
+
+def eno3_vectors(ref):
+    """The reference's own ENO3 advection closures (vorticity: conservative,
+    reference map: non-conservative; unbounded and periodic) on seeded
+    fields, through the pystencils stand-in. Case "tie" draws velocities from
+    a few multiples of 1/4, so many faces have u0 == -u1 exactly (the
+    upwind test is strict)."""
+    out = {}
+    rng = np.random.default_rng(31)
+    for tag, (nr, nz, tie) in {"a": (24, 40, False), "b": (37, 29, False),
+                               "tie": (20, 32, True)}.items():
+        dx = 1.0 / nz
+        dt = 0.37 * dx
+        z, r, Z, R = _coords(nr, nz, dx)
+        if tie:
+            uz = 0.25 * rng.integers(-3, 4, (nr, nz)).astype(np.float64)
+            ur = 0.25 * rng.integers(-3, 4, (nr, nz)).astype(np.float64)
+        else:
+            uz = rng.standard_normal((nr, nz))
+            ur = rng.standard_normal((nr, nz))
+        w0 = rng.standard_normal((nr, nz))
+        e10 = Z + 0.05 * rng.standard_normal((nr, nz))
+        e20 = R + 0.05 * rng.standard_normal((nr, nz))
+        out[f"{tag}/dx"], out[f"{tag}/dt"] = np.array(dx), np.array(dt)
+        out[f"{tag}/u_z"], out[f"{tag}/u_r"] = uz, ur
+        out[f"{tag}/w0"], out[f"{tag}/eta1_0"], out[f"{tag}/eta2_0"] = w0, e10, e20
+        # two successive calls of one closure (its buffers carry over)
+        adv = ref.gen_advect_vorticity_via_eno3(dx, nr, nz)
+        w = w0.copy()
+        adv(w, uz, ur, dt)
+        out[f"{tag}/w_1"] = w.copy()
+        adv(w, uz, ur, dt)
+        out[f"{tag}/w_2"] = w.copy()
+        adve = ref.gen_advect_refmap_via_eno3(dx, nr, nz)
+        e1, e2 = e10.copy(), e20.copy()
+        adve(e1, e2, uz, ur, dt)
+        out[f"{tag}/eta1_1"], out[f"{tag}/eta2_1"] = e1.copy(), e2.copy()
+        # periodic along z (2 ghost columns each side)
+        comm = ref.gen_periodic_boundary_ghost_comm(2)
+        comm_eta = ref.gen_periodic_boundary_ghost_comm_eta(2, nz * dx, dx)
+        advp = ref.gen_advect_vorticity_via_eno3_periodic(dx, nr, nz, comm)
+        uzp, urp, wp = uz.copy(), ur.copy(), w0.copy()
+        advp(wp, uzp, urp, dt)
+        out[f"{tag}/w_periodic"] = wp
+        advpe = ref.gen_advect_refmap_via_eno3_periodic(dx, nr, nz, comm, comm_eta)
+        uzp, urp, e1, e2 = uz.copy(), ur.copy(), e10.copy(), e20.copy()
+        advpe(e1, e2, uzp, urp, dt)
+        out[f"{tag}/eta1_periodic"], out[f"{tag}/eta2_periodic"] = e1, e2
     return out
 
 
@@ -497,15 +568,23 @@ def main(ref_root):
     np.savez_compressed(os.path.join(HERE, "m2p.npz"), **m2p_vectors())
     np.savez_compressed(os.path.join(HERE, "steps.npz"), **step_vectors(ref))
     np.savez_compressed(os.path.join(HERE, "soft.npz"), **soft_vectors(ref))
+    np.savez_compressed(os.path.join(HERE, "eno3.npz"), **eno3_vectors(ref))
     print("golden vectors written to", HERE)
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT [m2p|p2m|eno3]")
+    root = sys.argv[1]
     if len(sys.argv) > 2 and sys.argv[2] == "m2p":
         # only the mesh-to-particle vectors (needs oracle/_ref/libref_p2m.so)
         np.savez_compressed(os.path.join(HERE, "m2p.npz"), **m2p_vectors())
         print("m2p vectors written to", HERE)
+    elif len(sys.argv) > 2 and sys.argv[2] == "eno3":
+        # only the ENO3 vectors (reference kernels through the stand-in)
+        _install_reference(root)
+        np.savez_compressed(os.path.join(HERE, "eno3.npz"), **eno3_vectors(_ref_kernels()))
+        print("eno3 vectors written to", HERE)
     elif len(sys.argv) > 2 and sys.argv[2] == "p2m":
         # only the particle remeshing vectors
         _install_reference(root)

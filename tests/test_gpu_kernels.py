@@ -221,6 +221,51 @@ def test_eno3_periodic_variants():
     np.testing.assert_array_equal(host(t2), r2)
 
 
+@pytest.mark.parametrize("tag", ["a", "b", "tie"])
+def test_eno3_matches_reference_expressions(golden, tag):
+    """The CUDA ENO3 steps (FP64, through the drop-in closures) against the
+    reference's own pystencils kernels evaluated in sympy's term order
+    (tests/golden/eno3.npz): a few units in the last place of the field
+    magnitude, exact upwind ties included; unbounded and periodic,
+    conservative (vorticity) and non-conservative (reference map)."""
+    from pyaxisymflow_gb300.elasto_kernels.advect_refmap_via_eno3 import (
+        gen_advect_refmap_via_eno3, gen_advect_refmap_via_eno3_periodic)
+    from pyaxisymflow_gb300.kernels.advect_vorticity_via_eno3 import (
+        gen_advect_vorticity_via_eno3, gen_advect_vorticity_via_eno3_periodic)
+    from pyaxisymflow_gb300.kernels.periodic_boundary_ghost_comm import (
+        gen_periodic_boundary_ghost_comm, gen_periodic_boundary_ghost_comm_eta)
+    g = golden("eno3")
+    dx, dt = float(g[f"{tag}/dx"]), float(g[f"{tag}/dt"])
+    uz, ur, w0 = g[f"{tag}/u_z"], g[f"{tag}/u_r"], g[f"{tag}/w0"]
+    nr, nz = w0.shape
+
+    def close(t, ref):
+        scale = max(float(np.abs(ref).max()), 1.0)
+        err = float(np.abs(host(t) - ref).max())
+        assert err <= 1e-14 * scale, err
+
+    adv = gen_advect_vorticity_via_eno3(dx, nr, nz)
+    tw = dev(w0)
+    adv(tw, dev(uz), dev(ur), dt)
+    close(tw, g[f"{tag}/w_1"])
+    adv(tw, dev(uz), dev(ur), dt)
+    close(tw, g[f"{tag}/w_2"])
+    t1, t2 = dev(g[f"{tag}/eta1_0"]), dev(g[f"{tag}/eta2_0"])
+    gen_advect_refmap_via_eno3(dx, nr, nz)(t1, t2, dev(uz), dev(ur), dt)
+    close(t1, g[f"{tag}/eta1_1"])
+    close(t2, g[f"{tag}/eta2_1"])
+    comm = gen_periodic_boundary_ghost_comm(2)
+    tw = dev(w0)
+    gen_advect_vorticity_via_eno3_periodic(dx, nr, nz, comm)(tw, dev(uz), dev(ur), dt)
+    close(tw, g[f"{tag}/w_periodic"])
+    t1, t2 = dev(g[f"{tag}/eta1_0"]), dev(g[f"{tag}/eta2_0"])
+    gen_advect_refmap_via_eno3_periodic(
+        dx, nr, nz, comm, gen_periodic_boundary_ghost_comm_eta(2, nz * dx, dx))(
+        t1, t2, dev(uz), dev(ur), dt)
+    close(t1, g[f"{tag}/eta1_periodic"])
+    close(t2, g[f"{tag}/eta2_periodic"])
+
+
 def test_spectral_solvers_against_reference_golden(golden):
     from pyaxisymflow_gb300.kernels.FastDiagonalisationPotentialSolver import \
         FastDiagonalisationPotentialSolver

@@ -293,3 +293,101 @@ def test_m2p_oracle_matches_reference_golden(golden):
             fn(fx, fy, px, py, ox, oy, dx, dx)
             assert np.array_equal(ox, g[f"{tag}/{name}_x"]), (tag, name)
             assert np.array_equal(oy, g[f"{tag}/{name}_y"]), (tag, name)
+
+
+# The reference's ENO3 kernels are pystencils expressions; sympy orders the
+# terms of each three-term face sum by symbol name, so some faces round in a
+# different order from the kernel source text the oracle follows. The two
+# agree to a few units in the last place of the field magnitude.
+ENO3_ATOL_REL = 1e-14
+
+
+def _assert_eno3_close(mine, ref, what):
+    scale = max(float(np.abs(ref).max()), 1.0)
+    err = float(np.abs(mine - ref).max())
+    assert err <= ENO3_ATOL_REL * scale, (what, err)
+
+
+@pytest.mark.parametrize("tag", ["a", "b", "tie"])
+def test_eno3_matches_reference_expressions(golden, tag):
+    """The oracle's ENO3 restatement against the reference's own kernels
+    (pyst_kernels/advection_flux.py:9-332, advection_timestep.py:14-104,
+    kernels/advect_vorticity_via_eno3.py:8-91,
+    elasto_kernels/advect_refmap_via_eno3.py:8-115) run through the
+    pystencils stand-in: conservative and non-conservative, unbounded and
+    periodic, two successive calls of one closure, and exact upwind ties
+    (case "tie": u0 == -u1 on many faces, where the strict test picks the
+    second branch). Cells the flux kernels do not reach (pystencils' ghost
+    layers) are unchanged in both, bit for bit."""
+    g = golden("eno3")
+    dx, dt = float(g[f"{tag}/dx"]), float(g[f"{tag}/dt"])
+    uz, ur, w0 = g[f"{tag}/u_z"], g[f"{tag}/u_r"], g[f"{tag}/w0"]
+    nr, nz = w0.shape
+    gl = K.ENO3_GHOST_LAYERS
+    adv = K.gen_advect_vorticity_via_eno3(dx, nr, nz)
+    w = w0.copy()
+    adv(w, uz, ur, dt)
+    _assert_eno3_close(w, g[f"{tag}/w_1"], "w_1")
+    for a in (w, g[f"{tag}/w_1"]):
+        np.testing.assert_array_equal(a[-gl:, :], w0[-gl:, :])
+        np.testing.assert_array_equal(a[:, :gl], w0[:, :gl])
+        np.testing.assert_array_equal(a[:, -gl:], w0[:, -gl:])
+    adv(w, uz, ur, dt)
+    _assert_eno3_close(w, g[f"{tag}/w_2"], "w_2")
+    e1, e2 = g[f"{tag}/eta1_0"].copy(), g[f"{tag}/eta2_0"].copy()
+    K.gen_advect_refmap_via_eno3(dx, nr, nz)(e1, e2, uz, ur, dt)
+    _assert_eno3_close(e1, g[f"{tag}/eta1_1"], "eta1_1")
+    _assert_eno3_close(e2, g[f"{tag}/eta2_1"], "eta2_1")
+    comm = K.gen_periodic_boundary_ghost_comm(2)
+    comm_eta = K.gen_periodic_boundary_ghost_comm_eta(2, nz * dx, dx)
+    uzp, urp, wp = uz.copy(), ur.copy(), w0.copy()
+    K.gen_advect_vorticity_via_eno3_periodic(dx, nr, nz, comm)(wp, uzp, urp, dt)
+    _assert_eno3_close(wp, g[f"{tag}/w_periodic"], "w_periodic")
+    uzp, urp = uz.copy(), ur.copy()
+    e1, e2 = g[f"{tag}/eta1_0"].copy(), g[f"{tag}/eta2_0"].copy()
+    K.gen_advect_refmap_via_eno3_periodic(dx, nr, nz, comm, comm_eta)(e1, e2, uzp, urp, dt)
+    _assert_eno3_close(e1, g[f"{tag}/eta1_periodic"], "eta1_periodic")
+    _assert_eno3_close(e2, g[f"{tag}/eta2_periodic"], "eta2_periodic")
+
+
+def test_pystencils_standin_semantics():
+    """The stand-in that runs the reference's pystencils kernels: `@=` and
+    conditional expressions become assignments and Piecewise, the update
+    covers the cells at least the largest offset away from every edge, and
+    sums are evaluated in sympy's printed term order."""
+    import importlib
+    import os
+    import sys
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                        "pystencils_standin")
+    sys.path.insert(0, path)
+    try:
+        ps = importlib.import_module("pystencils")
+    finally:
+        sys.path.remove(path)
+    import sympy as sp
+
+    assert ps.offset_to_direction_string((0, 2)) == "2N"
+    assert ps.offset_to_direction_string((-1, 0)) == "W"
+    assert ps.offset_to_direction_string((-3, 0, -2)) == "2B3W"
+    assert ps.offset_to_direction_string((0, 0)) == "C"
+
+    @ps.kernel
+    def _stencil():
+        out, a = ps.fields("out, a : float64[2D]")
+        c = sp.symbols("c")
+        out[0, 0] @= (a[0, 1] - a[0, -2]) * c if a[1, 0] > -a[0, 0] else a[-1, 0]
+
+    kern = ps.create_kernel(_stencil, config=ps.CreateKernelConfig()).compile()
+    assert kern.ghost == 2
+    rng = np.random.default_rng(1)
+    a = rng.standard_normal((9, 11))
+    out = np.full_like(a, 7.0)
+    kern(out=out, a=a, c=0.5)
+    exp = np.full_like(a, 7.0)
+    for i in range(2, 7):
+        for j in range(2, 9):
+            exp[i, j] = ((a[i, j + 1] - a[i, j - 2]) * 0.5 if a[i + 1, j] > -a[i, j]
+                         else a[i - 1, j])
+    np.testing.assert_array_equal(out, exp)
+    assert "_where(" in kern.printed[0]
