@@ -496,6 +496,11 @@ typedef struct axi_case {
    * c_k = sqrt(2 / nz)); inv_eig then holds 1 / (lambda_r_i + lambda_z_k) in
    * DCT order, lambda_z_k = (2 - 2 cos(pi k / nz)) / dx^2. */
   const void* dct_table;
+  /* AXI_PLAN_REFINE: the low part of psi, float (nr, nz): psi is carried as
+   * the pair psi + psi_lo (about 48 significant bits), so the velocity
+   * differences of neighbouring psi values keep the refined solve's
+   * accuracy instead of the float rounding of psi. Start at zero. */
+  void* psi_lo;
 } axi_case;
 
 /* Launch plan of a set of cases: tile tables in device memory. */
@@ -515,7 +520,15 @@ typedef struct axi_plan_info {
  * z operator), the radial ones on the tensor cores; every nz even with no
  * prime factor other than 2 and 3; omega_hi / omega_lo and the z entries of
  * tc_basis are then unused (may be NULL). */
-enum { AXI_PLAN_TENSOR_CORES = 1, AXI_PLAN_DCT_Z = 2 };
+/* AXI_PLAN_REFINE (with AXI_PLAN_DCT_Z): every solve is one step of
+ * iterative refinement started from the psi the case already holds (the
+ * previous step's; zero for a new case): the forward z transform reads the
+ * residual omega - (A psi) / r of the discrete operator instead of omega, and
+ * the last radial product adds its result to the pair (psi, psi_lo), which
+ * the velocity kernels read back as psi + psi_lo. The solve error then
+ * shrinks with the step-to-step change of psi instead of with psi itself; the
+ * first solve of a case is the plain solve. Needs psi_lo. */
+enum { AXI_PLAN_TENSOR_CORES = 1, AXI_PLAN_DCT_Z = 2, AXI_PLAN_REFINE = 4 };
 
 /* Host only: validates the cases, assigns each its first tile
  * (cases[k].stencil_tile0) and fills `info` (sizes of the plan). flags:

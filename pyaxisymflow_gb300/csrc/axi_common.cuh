@@ -80,3 +80,28 @@ template <> __device__ __forceinline__ float dev_sin(float x) { return sinf(x); 
 template <typename T> struct Pi;
 template <> struct Pi<double> { static constexpr double v = 3.141592653589793; };
 template <> struct Pi<float> { static constexpr float v = 3.14159265f; };
+
+// Error-free float transformations (Knuth's two-sum; the FMA form of the
+// exact product): a + b = s + e and a * b = p + e exactly. Used where float
+// values are carried as unevaluated pairs (hi + lo) to keep more than float
+// precision in float storage and arithmetic.
+namespace axi_eft {
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+  p = __fmul_rn(a, b);
+  e = fmaf(a, b, -p);
+}
+// (hi, lo) + v as a renormalised pair: hi' is the rounded sum, lo' the
+// remainder; hi' + lo' = hi + lo + v up to the rounding of the low part.
+__device__ __forceinline__ void pair_add(float& hi, float& lo, float v) {
+  float s, e, h2, l2;
+  two_sum(hi, v, s, e);
+  two_sum(s, __fadd_rn(lo, e), h2, l2);
+  hi = h2;
+  lo = l2;
+}
+}  // namespace axi_eft

@@ -109,6 +109,46 @@ __device__ __forceinline__ void store_split4(const DctJob& job, int k, int i, co
   *reinterpret_cast<float4*>(job.out_lo + o) = make_float4(lo[0], lo[1], lo[2], lo[3]);
 }
 
+// Residual of the refinement, x = in - (A psi) / r at (row i, column j):
+//   (A psi) / r = [(c - W) + (c - E) + (c - S) + (c - N)] / (r dx^2)
+//                 + (N - S) / (2 dx r^2)
+// with the operator's boundary rows: W := c at j = 0 and E := c at j = N - 1
+// (Neumann z ends), S := 0 below the axis row, N := c above the outer row
+// and no first-derivative term there (its row of the r operator is
+// (psi_{nr-1} - psi_{nr-2}) / dx^2 only). psi is the pair psi + psi_lo:
+// each neighbour difference is the difference of the high parts (exact for
+// close values) plus that of the low parts, so the residual sees psi to the
+// pair's precision, not to its float rounding.
+struct PsiPair {
+  float h, l;
+};
+__device__ __forceinline__ float pdiff(PsiPair a, PsiPair b) { return (a.h - b.h) + (a.l - b.l); }
+__device__ __forceinline__ float residual_value(float in, PsiPair c, PsiPair w, PsiPair e,
+                                                PsiPair s, PsiPair n, float k1, float k2) {
+  return in - ((pdiff(c, w) + pdiff(c, e)) + (pdiff(c, s) + pdiff(c, n))) * k1 +
+         pdiff(s, n) * k2;
+}
+
+__device__ __forceinline__ float residual_at(const DctJob& job, int i, int j) {
+  const int N = job.N, nr = job.rows;
+  const long long o = (long long)i * N + j;
+  const float* ph = job.psi + o;
+  const float* pl = job.psi_lo + o;
+  const PsiPair c{ph[0], pl[0]};
+  const PsiPair w = j > 0 ? PsiPair{ph[-1], pl[-1]} : c;
+  const PsiPair e = j + 1 < N ? PsiPair{ph[1], pl[1]} : c;
+  const PsiPair s = i > 0 ? PsiPair{ph[-N], pl[-N]} : PsiPair{0.0f, 0.0f};
+  const PsiPair n = i + 1 < nr ? PsiPair{ph[N], pl[N]} : c;
+  const float k1 = job.two_over_dx * job.rinv2dx[i];
+  const float k2 = i + 1 < nr ? job.inv_2dx * job.rinv2[i] : 0.0f;
+  return residual_value(job.in[o], c, w, e, s, n, k1, k2);
+}
+
+// Forward input element (row i, column j): the field, or the refinement residual.
+__device__ __forceinline__ float forward_input(const DctJob& job, int i, int j) {
+  return job.psi ? residual_at(job, i, j) : job.in[(long long)i * job.N + j];
+}
+
 // Bulk prefetch of `bytes` (a multiple of 16, 16-byte aligned) into L2.
 __device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
@@ -135,6 +175,10 @@ __global__ void __launch_bounds__(THREADS) dct_rows_kernel(const DctJob* __restr
     const long long off = (long long)nx.y * nj.N;
     prefetch_l2(nj.in + off, bytes);
     if (!forward && nj.row_scale) prefetch_l2(nj.row_scale + off, bytes);
+    if (forward && nj.psi) {
+      prefetch_l2(nj.psi + off, bytes);
+      prefetch_l2(nj.psi_lo + off, bytes);
+    }
   }
   __syncthreads();
   // the twiddle table of this row length, staged once per block at the end
@@ -167,7 +211,7 @@ __global__ void __launch_bounds__(THREADS) dct_rows_kernel(const DctJob* __restr
     // v[n] = x[2n], v[N-1-n] = x[2n+1]
     for (int t = threadIdx.x; t < nrows * N; t += blockDim.x) {
       const int r = t / N, p = t - r * N;
-      const float x = job.in[(long long)(row0 + r) * N + p];
+      const float x = forward_input(job, row0 + r, p);
       const int d = (p & 1) ? N - 1 - (p >> 1) : (p >> 1);
       a[r * N + d] = make_float2(x, 0.0f);
     }
@@ -291,7 +335,7 @@ __device__ void dct_item_fixed(const DctJob& job, int row0, bool forward, float2
     float* af = reinterpret_cast<float*>(a);
     for (int t = threadIdx.x; t < ncrows * 2 * N; t += blockDim.x) {
       const int r = t / N, p = t - r * N;
-      const float x = r < nrows ? job.in[(long long)(row0 + r) * N + p] : 0.0f;
+      const float x = r < nrows ? forward_input(job, row0 + r, p) : 0.0f;
       const int d = (p & 1) ? N - 1 - (p >> 1) : (p >> 1);
       af[2 * ((r >> 1) * N + d) + (r & 1)] = x;
     }
@@ -466,6 +510,75 @@ __device__ __forceinline__ float2 inverse_pre(float2 cs, float2 x, float2 y) {
   return make_float2(va.x - vb.y, va.y + vb.x);
 }
 
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+
+// Four consecutive columns (float4 group at column p) of one row of the psi pair.
+struct Pair4 {
+  float4 h, l;
+};
+__device__ __forceinline__ Pair4 ld_pair4(const DctJob& job, long long o) {
+  return Pair4{ld4(job.psi + o), ld4(job.psi_lo + o)};
+}
+__device__ __forceinline__ PsiPair ld_pair(const DctJob& job, long long o) {
+  return PsiPair{job.psi[o], job.psi_lo[o]};
+}
+__device__ __forceinline__ PsiPair pick(const Pair4& a, int q) {
+  return q == 0 ? PsiPair{a.h.x, a.l.x}
+                : q == 1 ? PsiPair{a.h.y, a.l.y} : q == 2 ? PsiPair{a.h.z, a.l.z}
+                                                            : PsiPair{a.h.w, a.l.w};
+}
+
+// residual_value on four consecutive columns of one row: c the row's psi,
+// w / e the values left of column 0 / right of column 3 of the group, s / n
+// the rows below / above.
+__device__ __forceinline__ float4 residual4(float4 in, const Pair4& c, PsiPair w, PsiPair e,
+                                            const Pair4& s, const Pair4& n, float k1, float k2) {
+  return make_float4(
+      residual_value(in.x, pick(c, 0), w, pick(c, 1), pick(s, 0), pick(n, 0), k1, k2),
+      residual_value(in.y, pick(c, 1), pick(c, 0), pick(c, 2), pick(s, 1), pick(n, 1), k1, k2),
+      residual_value(in.z, pick(c, 2), pick(c, 1), pick(c, 3), pick(s, 2), pick(n, 2), k1, k2),
+      residual_value(in.w, pick(c, 3), pick(c, 2), e, pick(s, 3), pick(n, 3), k1, k2));
+}
+
+// Residual rows ga, ga + 1 (global) of the refinement into one warp buffer
+// as z[n] = x_a[n] + i x_b[n] in Makhoul order, as the plain forward path
+// stores the field rows. Rows missing from the item are zero.
+template <int N>
+__device__ __forceinline__ void residual_pair_to_buf(const DctJob& job, int ga, bool has_a,
+                                                     bool has_b, int lane, float2* buf) {
+  constexpr int NV = N / 128;  // float4 groups per lane and row
+  const int nr = job.rows, gb = ga + 1;
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  const long long oa = (long long)ga * N, ob = oa + N;
+  const float k1a = has_a ? job.two_over_dx * job.rinv2dx[ga] : 0.0f;
+  const float k2a = has_a ? job.inv_2dx * job.rinv2[ga] : 0.0f;
+  const float k1b = has_b ? job.two_over_dx * job.rinv2dx[gb] : 0.0f;
+  const float k2b = (has_b && gb + 1 < nr) ? job.inv_2dx * job.rinv2[gb] : 0.0f;
+#pragma unroll 1
+  for (int m = 0; m < NV; ++m) {
+    const int p = 4 * (lane + 32 * m);
+    float4 xa = zero, xb = zero;
+    if (has_a) {
+      const Pair4 ca = ld_pair4(job, oa + p);
+      const Pair4 sa = ga > 0 ? ld_pair4(job, oa - N + p) : Pair4{zero, zero};
+      // row a is never the outer row (rows come in even-aligned pairs)
+      const Pair4 cb = has_b ? ld_pair4(job, ob + p) : ca;
+      const PsiPair wa = p > 0 ? ld_pair(job, oa + p - 1) : pick(ca, 0);
+      const PsiPair ea = p + 4 < N ? ld_pair(job, oa + p + 4) : pick(ca, 3);
+      xa = residual4(ld4(job.in + oa + p), ca, wa, ea, sa, cb, k1a, k2a);
+      if (has_b) {
+        const Pair4 nb = gb + 1 < nr ? ld_pair4(job, ob + N + p) : cb;
+        const PsiPair wb = p > 0 ? ld_pair(job, ob + p - 1) : pick(cb, 0);
+        const PsiPair eb = p + 4 < N ? ld_pair(job, ob + p + 4) : pick(cb, 3);
+        xb = residual4(ld4(job.in + ob + p), cb, wb, eb, ca, nb, k1b, k2b);
+      }
+    }
+    const int h = p >> 1;
+    *reinterpret_cast<float4*>(buf + h) = make_float4(xa.x, xb.x, xa.z, xb.z);
+    *reinterpret_cast<float4*>(buf + N - 2 - h) = make_float4(xa.w, xb.w, xa.y, xb.y);
+  }
+}
+
 // Work item of the register path: warp w transforms real rows 2w, 2w + 1 of
 // the item as one complex row in its own buffer; the block then stores the
 // results transposed (rows fastest).
@@ -481,7 +594,14 @@ __device__ void dct_item_reg(const DctJob& job, int row0, bool forward, float2* 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nrows = min(2 * W, job.rows - row0);  // real rows of this item
   const int ra = 2 * warp, rb = ra + 1;
-  if (warp < W) {
+  if (warp < W && forward && job.psi) {
+    // refinement: the residual rows of the pair, four columns per lane and
+    // float4 group at a time, straight into the warp buffer (Makhoul order)
+    float2* buf = dsm + warp * BUF;
+    residual_pair_to_buf<N>(job, row0 + ra, ra < nrows, rb < nrows, lane, buf);
+    __syncwarp();
+    warp_fft<N, N1, true>(buf, tw, lane);
+  } else if (warp < W) {
     float2* buf = dsm + warp * BUF;
     const bool has_a = ra < nrows, has_b = rb < nrows;
     const float* ia = job.in + (long long)(row0 + ra) * N;

@@ -42,6 +42,17 @@ struct DctJob {
   const float* row_scale;      // inverse: (rows, N) elementwise factor applied to
                                // the input before 1 / c_k (the spectral
                                // inverse), or nullptr
+  // Forward with psi (iterative refinement of the Poisson solve): the rows
+  // transformed are the residual x = in - (A psi) / r of the discrete
+  // operator A = A_r (x) I + I (x) A_z of the solve (Neumann z ends, axis
+  // row 0, Neumann outer row), so the solve of x is the correction to add to
+  // psi. rinv2dx = 1 / (2 dx r_i), rinv2 = 1 / r_i^2 per row.
+  const float* psi;
+  const float* psi_lo;         // psi is the pair psi + psi_lo
+  const float* rinv2dx;
+  const float* rinv2;
+  float two_over_dx;           // 2 / dx
+  float inv_2dx;               // 1 / (2 dx)
 };
 
 // Rows one work item of the generic path transforms for a row length N.

@@ -27,6 +27,8 @@
 // per-step scalars are computed once per case. FP64 remains in the time
 // step, the simulated time, the drag sums across warps and tiles and the
 // body ODE.
+#include <type_traits>
+
 #include "axi_common.cuh"
 #include "dct.cuh"
 #include "tc_gemm.cuh"
@@ -51,15 +53,20 @@ constexpr double kPi = 3.141592653589793;
 // copies that kill_reset and vel_max write once per case and step, so no
 // thread converts from double (GB300 issues FP64 conversions at the FP64
 // rate).
+// The float engine's body geometry is kept in cell units, split into float
+// hi / lo pairs: S = z_cm / dx, R = radius / dx (and W = blend width / dx), so
+// the moving mask sees the double position, not its float rounding.
 enum {
-  SF_UFREE, SF_LAMDT, SF_ADV, SF_C1, SF_C2, SF_UBODY, SF_ZCM, SF_INV2DX, SF_INVDX2, SF_RBODY,
-  SF_BLENDW, SF_COUNT
+  SF_UFREE, SF_LAMDT, SF_ADV, SF_C1, SF_C2, SF_UBODY, SF_INV2DX, SF_INVDX2,
+  SF_S_HI, SF_S_LO, SF_R_HI, SF_R_LO, SF_W, SF_UBODY_LO, SF_FLOAT_END,
+  // read by the double engine only (from the state block and the case)
+  SF_ZCM = SF_FLOAT_END, SF_RBODY, SF_BLENDW
 };
-static_assert(SF_COUNT <= 2 * (AXI_ST_WORDS - AXI_ST_F32), "float scalar slots");
+static_assert(SF_FLOAT_END <= 2 * (AXI_ST_WORDS - AXI_ST_F32), "float scalar slots");
 
 // Tensor maps of a case's fields (the stencil kernels' TMA boxes) and the
 // error codes of their bounded waits (plan error word).
-enum { MAP_PSI = 0, MAP_CHI = 1, MAP_W = 2, MAP_UZ = 3, MAP_UR = 4, MAP_COUNT = 5 };
+enum { MAP_PSI = 0, MAP_CHI = 1, MAP_W = 2, MAP_UZ = 3, MAP_UR = 4, MAP_PSI_LO = 5, MAP_COUNT = 6 };
 enum { ERR_STENCIL_WAIT = 5, ERR_STENCIL_DRAIN = 6 };
 
 __device__ __forceinline__ float* fslots(const axi_case& k) {
@@ -70,7 +77,7 @@ template <typename T>
 __device__ __forceinline__ T scalar(const axi_case& k, int f);
 template <>
 __device__ __forceinline__ float scalar<float>(const axi_case& k, int f) {
-  return fslots(k)[f];
+  return fslots(k)[f];  // f < SF_FLOAT_END
 }
 template <>
 __device__ __forceinline__ double scalar<double>(const axi_case& k, int f) {
@@ -161,25 +168,32 @@ __global__ void __launch_bounds__(256) kill_reset_kernel(const axi_case* __restr
     k.state[AXI_ST_UFREE] = k.U0 * prefac;
     float* f = fslots(k);
     f[SF_UFREE] = (float)(k.U0 * prefac);
-    f[SF_UBODY] =
-        (float)((k.flags & AXI_CASE_SEDIMENTING) ? k.state[AXI_ST_UBODY] : k.U_body);
-    f[SF_ZCM] = (float)k.state[AXI_ST_ZCM];
+    const double ub = (k.flags & AXI_CASE_SEDIMENTING) ? k.state[AXI_ST_UBODY] : k.U_body;
+    f[SF_UBODY] = (float)ub;
+    f[SF_UBODY_LO] = (float)(ub - (double)(float)ub);  // the body velocity as a float pair
     f[SF_INV2DX] = (float)k.inv_2dx;
     f[SF_INVDX2] = (float)k.inv_dx2;
-    f[SF_RBODY] = (float)k.r_body;
-    f[SF_BLENDW] = (float)k.blend_w;
+    const double sc = k.state[AXI_ST_ZCM] / k.dx, rc = k.r_body / k.dx;
+    f[SF_S_HI] = (float)sc;
+    f[SF_S_LO] = (float)(sc - (double)(float)sc);
+    f[SF_R_HI] = (float)rc;
+    f[SF_R_LO] = (float)(rc - (double)(float)rc);
+    f[SF_W] = (float)(k.blend_w / k.dx);
   }
   const int band = (nr - wd) * nz;  // first outer row
   // output pointers in registers (a store through a pointer read from the
   // case record would force the record to be re-read after it)
   float* const whi = static_cast<float*>(k.omega_hi);
   float* const wlo = static_cast<float*>(k.omega_lo);
-  auto put = [&](int c, T v) {
-    w[c] = v;
+  auto wval = [&](int c) -> double { return (double)w[c]; };
+  // stores the tapered value v (double), rounded to T
+  auto put = [&](int c, double v) {
+    const T h = (T)v;
+    w[c] = h;
     if constexpr (sizeof(T) == 4) {
       if (whi) {
         float hi, lo;
-        axi_tc::tf32_split((float)v, hi, lo);
+        axi_tc::tf32_split((float)h, hi, lo);
         whi[c] = hi;
         wlo[c] = lo;
       }
@@ -192,26 +206,25 @@ __global__ void __launch_bounds__(256) kill_reset_kernel(const axi_case* __restr
   const int je = t < wd ? t : nz - 2 * wd + t;
   double esrc = 0.0;
   if (edge)
-    esrc = t < wd ? (double)(T)(cz0[t] * (double)w[band + wd - 1])
-                  : (double)(T)(cz1[t - wd] * (double)w[band + nz - wd]);
+    esrc = (double)(T)(t < wd ? cz0[t] * wval(band + wd - 1) : cz1[t - wd] * wval(band + nz - wd));
   __syncthreads();
   if (edge) {
-    for (int q = 0; q < wd; ++q) put(band + q * nz + je, (T)(cr[q] * esrc));
-    put(je, T(0));
+    for (int q = 0; q < wd; ++q) put(band + q * nz + je, cr[q] * esrc);
+    put(je, 0.0);
   }
   const int n_units = nz + (nr - wd - 1 > 0 ? nr - wd - 1 : 0);
   for (int u = 2 * wd + blockIdx.x * blockDim.x + t; u < n_units; u += gridDim.x * blockDim.x) {
     if (u < nz) {
       const int j = u - wd;  // inner column w .. nz - w - 1
-      const double src = (double)w[band + j];
-      for (int q = 0; q < wd; ++q) put(band + q * nz + j, (T)(cr[q] * src));
-      put(j, T(0));
+      const double src = wval(band + j);
+      for (int q = 0; q < wd; ++q) put(band + q * nz + j, cr[q] * src);
+      put(j, 0.0);
     } else {
       const int row = (1 + u - nz) * nz;  // rows 1 .. nr - w - 1
-      const double left = (double)w[row + wd - 1];
-      const double right = (double)w[row + nz - wd];
-      for (int q = 0; q < wd; ++q) put(row + q, (T)(cz0[q] * left));
-      for (int q = 0; q < wd; ++q) put(row + nz - wd + q, (T)(cz1[q] * right));
+      const double left = wval(row + wd - 1);
+      const double right = wval(row + nz - wd);
+      for (int q = 0; q < wd; ++q) put(row + q, cz0[q] * left);
+      for (int q = 0; q < wd; ++q) put(row + nz - wd + q, cz1[q] * right);
     }
   }
 }
@@ -219,12 +232,40 @@ __global__ void __launch_bounds__(256) kill_reset_kernel(const axi_case* __restr
 // ---------------------------------------------------------------------------
 // velocity from psi (kernels/compute_velocity_from_psi.py:9-17) plus the free
 // stream. psi(a, b) is an accessor; rinv = 1 / (2 dx r_i). The one-sided rows
-// and columns at the grid edges run in double in the double engine (the
-// reference's expression) and in float in the float engine.
+// and columns at the grid edges (the r = 0 axis closure, the outer r row and
+// the z ends): in the double engine the reference's expression in double; in
+// the float engine the three-point difference of the float psi values is
+// formed with one rounding (edge_diff_exact: what double arithmetic gives for
+// these inputs), since it cancels most of its terms at the axis, where
+// psi ~ r^2.
 // ---------------------------------------------------------------------------
-template <typename T, typename Acc>
+using axi_eft::pair_add;
+using axi_eft::two_prod;
+using axi_eft::two_sum;
+
+// -p2 + 4 p1 - 3 p0 of float values with a single final rounding (the value
+// FP64 arithmetic gives for these float inputs, rounded to float): the
+// one-sided difference of the axis closure and the other grid edges cancels
+// most of its terms where psi ~ r^2.
+__device__ __forceinline__ float edge_diff_exact(float p2, float p1, float p0) {
+  float b, be, s1, e1, s2, e2;
+  two_prod(3.0f, p0, b, be);
+  two_sum(4.0f * p1, -b, s1, e1);
+  two_sum(s1, -p2, s2, e2);
+  return __fadd_rn(s2, __fsub_rn(__fadd_rn(e1, e2), be));
+}
+
+// With a low-part accessor `lo` (float engine, psi carried as psi + psi_lo)
+// every difference is the difference of the high parts plus that of the low
+// parts.
+struct NoLow {
+  __device__ float operator()(int, int) const { return 0.0f; }
+};
+
+template <typename T, typename Acc, typename Lo = NoLow>
 __device__ __forceinline__ void velocity_at(const axi_case& k, Acc psi, int i, int j, T rinv,
-                                            T ufree, T& uz, T& ur) {
+                                            T ufree, T& uz, T& ur, Lo lo = Lo()) {
+  constexpr bool PAIR = !std::is_same<Lo, NoLow>::value;
   const int nr = k.nr, nz = k.nz;
   if (i == 0 || i == nr - 1) {
     if constexpr (sizeof(T) == 8) {
@@ -235,12 +276,17 @@ __device__ __forceinline__ void velocity_at(const axi_case& k, Acc psi, int i, i
         d = (double)psi(nr - 3, j) - 4.0 * (double)psi(nr - 2, j) + 3.0 * (double)psi(nr - 1, j);
       uz = (T)(d * (0.5 / k.dx) / k.r[i]) + ufree;
     } else {
-      const T d = (i == 0) ? -psi(2, j) + T(4) * psi(1, j) - T(3) * psi(0, j)
-                           : psi(nr - 3, j) - T(4) * psi(nr - 2, j) + T(3) * psi(nr - 1, j);
+      T d = i == 0 ? edge_diff_exact(psi(2, j), psi(1, j), psi(0, j))
+                   : -edge_diff_exact(psi(nr - 3, j), psi(nr - 2, j), psi(nr - 1, j));
+      if constexpr (PAIR)
+        d += i == 0 ? -lo(2, j) + T(4) * lo(1, j) - T(3) * lo(0, j)
+                    : lo(nr - 3, j) - T(4) * lo(nr - 2, j) + T(3) * lo(nr - 1, j);
       uz = d * rinv + ufree;
     }
   } else {
-    uz = (psi(i + 1, j) - psi(i - 1, j)) * rinv + ufree;
+    T d = psi(i + 1, j) - psi(i - 1, j);
+    if constexpr (PAIR) d += lo(i + 1, j) - lo(i - 1, j);
+    uz = d * rinv + ufree;
   }
   if (j == 0 || j == nz - 1) {
     if constexpr (sizeof(T) == 8) {
@@ -251,12 +297,17 @@ __device__ __forceinline__ void velocity_at(const axi_case& k, Acc psi, int i, i
         d = (double)psi(i, nz - 3) - 4.0 * (double)psi(i, nz - 2) + 3.0 * (double)psi(i, nz - 1);
       ur = (T)(-d) * rinv;
     } else {
-      const T d = (j == 0) ? -psi(i, 2) + T(4) * psi(i, 1) - T(3) * psi(i, 0)
-                           : psi(i, nz - 3) - T(4) * psi(i, nz - 2) + T(3) * psi(i, nz - 1);
+      T d = j == 0 ? edge_diff_exact(psi(i, 2), psi(i, 1), psi(i, 0))
+                   : -edge_diff_exact(psi(i, nz - 3), psi(i, nz - 2), psi(i, nz - 1));
+      if constexpr (PAIR)
+        d += j == 0 ? -lo(i, 2) + T(4) * lo(i, 1) - T(3) * lo(i, 0)
+                    : lo(i, nz - 3) - T(4) * lo(i, nz - 2) + T(3) * lo(i, nz - 1);
       ur = -d * rinv;
     }
   } else {
-    ur = -(psi(i, j + 1) - psi(i, j - 1)) * rinv;
+    T d = psi(i, j + 1) - psi(i, j - 1);
+    if constexpr (PAIR) d += lo(i, j + 1) - lo(i, j - 1);
+    ur = -d * rinv;
   }
 }
 
@@ -396,6 +447,10 @@ __device__ __forceinline__ void finish_step_dt(const axi_case& k) {
   f[SF_C2] = (float)(k.nu * dt);
 }
 
+// dt comes from the velocities of psi alone, also in the refined float
+// engine (the float rounding of psi moves the maximum, and dt, by about 1e-7;
+// on the 2000-step FP32-vs-FP64 comparison reading psi_lo here made no
+// measurable difference)
 template <typename T>
 using VmRing = BoxRing<T, VM_NBUF, 1, PSI_ROWS>;
 template <typename T>
@@ -514,30 +569,38 @@ __device__ __forceinline__ void penalise_point(T uz, T ur, T lc, T ubody, T& pz,
 
 constexpr int PN_SW = TX + 2, PN_SH = TY + 2;  // u_pen - u, halo 1
 constexpr int PN_RB = (TY + 2 + RG - 1) / RG;  // rows per group of the halo-1 march
-template <typename T>
-using PnRing = BoxRing<T, PN_NBUF, 2, PSI_ROWS>;
-template <typename T>
+// boxes: psi, chi and, with PAIR (refined float engine), psi_lo
+template <typename T, bool PAIR>
+using PnRing = BoxRing<T, PN_NBUF, PAIR ? 3 : 2, PSI_ROWS>;
+template <typename T, bool PAIR>
 constexpr int penalise_smem() {
-  return PnRing<T>::BYTES + 2 * PN_SH * PN_SW * (int)sizeof(T) + 128;
+  return PnRing<T, PAIR>::BYTES + 2 * PN_SH * PN_SW * (int)sizeof(T) + 128;
+}
+template <typename T, bool PAIR>
+constexpr int penalise_min_blocks() {
+  return sizeof(T) == 8 ? 2 : (PAIR ? 4 : 5);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 2) penalise_kernel(const axi_case* __restrict__ cases,
-                                                      const int4* __restrict__ tiles, int n_tiles,
-                                                      const CUtensorMap* __restrict__ maps,
-                                                      int* __restrict__ err, int ahead) {
+template <typename T, bool PAIR>
+__global__ void __launch_bounds__(NT, penalise_min_blocks<T, PAIR>()) penalise_kernel(
+    const axi_case* __restrict__ cases, const int4* __restrict__ tiles, int n_tiles,
+    const CUtensorMap* __restrict__ maps, int* __restrict__ err, int ahead) {
+  static_assert(!PAIR || sizeof(T) == 4, "psi pairs belong to the float engine");
+  constexpr int NB = PAIR ? 3 : 2;
+  using Ring = PnRing<T, PAIR>;
   extern __shared__ unsigned char pn_raw[];
   __shared__ __align__(8) uint64_t bars[PN_NBUF];
   __shared__ double red[2][NT / 32];
-  __shared__ T rowf[2][PN_SH];
-  PnRing<T> ring{reinterpret_cast<T*>(align_smem(pn_raw)), axi_tma::smem_u32(bars)};
-  T* duz = ring.base + PnRing<T>::BYTES / sizeof(T);
+  __shared__ T rowf[2][PN_SH];  // 1 / (2 dx r), r
+  Ring ring{reinterpret_cast<T*>(align_smem(pn_raw)), axi_tma::smem_u32(bars)};
+  T* duz = ring.base + Ring::BYTES / sizeof(T);
   T* dur = duz + PN_SH * PN_SW;
-  constexpr int which[2] = {MAP_PSI, MAP_CHI};
+  constexpr int which3[3] = {MAP_PSI, MAP_CHI, MAP_PSI_LO};
+  const int(&which)[NB] = *reinterpret_cast<const int(*)[NB]>(&which3);
   int issued = 0;
   if (threadIdx.x == 0) {
     ring.init();
-    issued = ring_prologue<PnRing<T>, PN_NBUF, 2>(ring, maps, tiles, n_tiles, which, -2);
+    issued = ring_prologue<Ring, PN_NBUF, NB>(ring, maps, tiles, n_tiles, which, -2);
   }
   __syncthreads();
   int it = 0;
@@ -560,6 +623,9 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 2) penalise_kernel(co
     const T* __restrict__ rw = CF<T>(k.rw);
     const T ufree = scalar<T>(k, SF_UFREE);
     const T ubody = scalar<T>(k, SF_UBODY);
+    // low part of the body velocity (float engine: U = ubody + ubody_lo)
+    T ubody_lo = T(0);
+    if constexpr (sizeof(T) == 4) ubody_lo = scalar<T>(k, SF_UBODY_LO);
     const T inv2dx = scalar<T>(k, SF_INV2DX);
     T* w = F<T>(k.omega);
     const T lamdt = scalar<T>(k, SF_LAMDT);
@@ -575,10 +641,17 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 2) penalise_kernel(co
     }
     const T* ps = ring.box(it % PN_NBUF, 0);
     const T* sc = ring.box(it % PN_NBUF, 1);
+    // low part of psi (PAIR); the psi box itself otherwise (never read)
+    const T* pl = ring.box(it % PN_NBUF, NB - 1);
     // every one-sided stencil of an edge cell stays inside the box
     auto sp = [&](int gi, int gj) { return ps[(gi - i0 + 2) * BOXW + (gj - j0 + 4)]; };
+    auto spl = [&](int gi, int gj) { return pl[(gi - i0 + 2) * BOXW + (gj - j0 + 4)]; };
     T* uzp = F<T>(k.u_z);
     T* urp = F<T>(k.u_r);
+    // drag integrand sum of this thread (the float engine forms u_pen - U as
+    // (u_z - U) / (1 + lam dt chi), the same value without its cancellation;
+    // the sum over the body is well conditioned, sum |t| / |sum t| below 5
+    // on the sedimenting cases, so float partial sums suffice)
     T cd_part = T(0);
     // Column march (as in advect_diffuse): warp w owns tile columns
     // 32 (w % 2) .. + 31 and a run of consecutive rows from (w / 2) x rows
@@ -590,18 +663,37 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 2) penalise_kernel(co
     const int gjm = j0 + qm;
     // u_pen - u at one point of the tile + halo 1 (p in [-1, TY], q in [-1, TX])
     auto point = [&](int p, int q, T uz, T ur, T ch, int gi, int gj) {
-      T pz, pr;
-      penalise_point<T>(uz, ur, lamdt * ch, ubody, pz, pr);
+      T pz, pr, dz, dr;
+      if constexpr (sizeof(T) == 8) {
+        penalise_point<T>(uz, ur, lamdt * ch, ubody, pz, pr);
+        dz = pz - uz;
+        dr = pr - ur;
+      } else {
+        // u_pen - u = lam dt chi (U - u) / (1 + lam dt chi), formed directly:
+        // inside the body u is close to U, and the difference of the rounded
+        // u_pen and u would keep only the rounding of u_pen (its curl, / dx,
+        // is vorticity noise of ulp(U) / dx per step); U = ubody + ubody_lo
+        const T lc = lamdt * ch;
+        const T inv = T(1) / (T(1) + lc);
+        const T du = (ubody - uz) + ubody_lo;
+        dz = (lc * inv) * du;
+        dr = -(lc * inv) * ur;
+        pz = uz + dz;
+        pr = ur + dr;
+        if (p >= 0 && p < TY && q >= 0 && q < TX)
+          cd_part -= rowf[1][p + 1] * ch * (du * inv);
+      }
       const int d = (p + 1) * PN_SW + (q + 1);
-      duz[d] = pz - uz;
-      dur[d] = pr - ur;
+      duz[d] = dz;
+      dur[d] = dr;
       if (p >= 0 && p < TY && q >= 0 && q < TX) {
         const int c = gi * nz + gj;
         uzp[c] = pz;
         urp[c] = pr;
         // drag / penalisation force integrand r chi (u_z - U_body)
-        // (flow_past_sphere.py:173, compute_forces.py:14)
-        cd_part += rowf[1][p + 1] * ch * (pz - ubody);
+        // (flow_past_sphere.py:173, compute_forces.py:14); the float engine
+        // adds it above as -r chi (U - u) / (1 + lam dt chi)
+        if constexpr (sizeof(T) == 8) cd_part += rowf[1][p + 1] * ch * (pz - ubody);
       }
     };
     {
@@ -609,22 +701,36 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 2) penalise_kernel(co
       const int p0 = -1 + PN_RB * grp;
       int cb = (p0 + 2) * BOXW + (qm + 4);
       T pm = ps[cb - BOXW], pc = ps[cb];
+      T lm = T(0), lc = T(0);
+      if constexpr (PAIR) {
+        lm = pl[cb - BOXW];
+        lc = pl[cb];
+      }
 #pragma unroll
       for (int m = 0; m < PN_RB; ++m, cb += BOXW) {
         const int pr_ = p0 + m;
         if (pr_ > TY) break;
         const T pn = ps[cb + BOXW];
+        T ln = T(0);
+        if constexpr (PAIR) ln = pl[cb + BOXW];
         const int gi = i0 + pr_;
         if (jin && gi >= 0 && gi < nr) {
           const T rv = rowf[0][pr_ + 1];
+          const T ch = sc[cb];
           T uz, ur;
           if (gi == 0 || gi == nr - 1 || !jint) {
-            velocity_at<T>(k, sp, gi, gjm, rv, ufree, uz, ur);
+            if constexpr (PAIR)
+              velocity_at<T>(k, sp, gi, gjm, rv, ufree, uz, ur, spl);
+            else
+              velocity_at<T>(k, sp, gi, gjm, rv, ufree, uz, ur);
+          } else if constexpr (PAIR) {
+            uz = ((pn - pm) + (ln - lm)) * rv + ufree;
+            ur = -((ps[cb + 1] - ps[cb - 1]) + (pl[cb + 1] - pl[cb - 1])) * rv;
           } else {
             uz = (pn - pm) * rv + ufree;
             ur = -(ps[cb + 1] - ps[cb - 1]) * rv;
           }
-          point(pr_, qm, uz, ur, sc[cb], gi, gjm);
+          point(pr_, qm, uz, ur, ch, gi, gjm);
         } else {
           const int d = (pr_ + 1) * PN_SW + (qm + 1);
           duz[d] = T(0);
@@ -632,6 +738,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 2) penalise_kernel(co
         }
         pm = pc;
         pc = pn;
+        lm = lc;
+        lc = ln;
       }
       // halo columns -1 and TX
       if (threadIdx.x < 2 * PN_SH) {
@@ -639,7 +747,10 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 2) penalise_kernel(co
         const int gi = i0 + pe, gj = j0 + qe;
         if (gi >= 0 && gi < nr && gj >= 0 && gj < nz) {
           T uz, ur;
-          velocity_at<T>(k, sp, gi, gj, rowf[0][pe + 1], ufree, uz, ur);
+          if constexpr (PAIR)
+            velocity_at<T>(k, sp, gi, gj, rowf[0][pe + 1], ufree, uz, ur, spl);
+          else
+            velocity_at<T>(k, sp, gi, gj, rowf[0][pe + 1], ufree, uz, ur);
           point(pe, qe, uz, ur, sc[(pe + 2) * BOXW + (qe + 4)], gi, gj);
         } else {
           const int d = (pe + 1) * PN_SW + (qe + 1);
@@ -675,8 +786,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 2) penalise_kernel(co
         zc = zn;
       }
     }
-    // drag: thread and warp sums in T, then warps and tiles in double, fixed order
-    T x = cd_part;
+    // drag: thread sums in T, then warps, tiles and cases in double, fixed order
+    double x = cd_part;
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if ((threadIdx.x & 31) == 0) red[it & 1][threadIdx.x >> 5] = (double)x;
     __syncthreads();
@@ -748,6 +859,37 @@ __device__ __forceinline__ T sphere_mask(T z, T r, T zc, T radius, T w) {
   const T phi = -sqrt(dz * dz + r * r) + radius;
   T h = phi >= w ? T(1) : T(0);
   if (fabs(phi) < w) h += T(0.5) * (T(1) + phi / w + dev_sin(Pi<T>::v * phi / w) / Pi<T>::v);
+  return h;
+}
+
+// The float engine's moving-body mask, in cell units: t = j + 1/2 - z_cm / dx,
+// q = i + 1/2, level set phi = R - sqrt(t^2 + q^2) with R = radius / dx. A
+// float estimate decides the cells well inside (1) and outside (0) the blend
+// band |phi| < W; within the band (and the estimate's error of it) phi is
+// formed as (R^2 - t^2 - q^2) / (R + sqrt(t^2 + q^2)) with the squares and
+// the difference carried as exact float pairs, from the hi / lo splits of
+// z_cm / dx and R, so the mask follows the double body position (a float
+// z_cm alone is off by up to 6e-8 absolute, i.e. 5e-5 of the blend width at
+// dx = 1/512, and shifts every band cell the same way).
+__device__ __forceinline__ float sphere_mask_cells(int i, int j, float s_hi, float s_lo,
+                                                   float r_hi, float r_lo, float w) {
+  const float t = __fsub_rn((float)j + 0.5f, s_hi);  // exact near the body
+  const float q = (float)i + 0.5f;
+  const float q2 = q * q;                            // exact (q <= 2^11)
+  const float est = r_hi - sqrtf(fmaf(t, t, q2));
+  if (fabsf(est) >= w + 1e-3f) return est >= w ? 1.0f : 0.0f;
+  // D = t_true^2 + q^2 with t_true = t - s_lo; R^2 = r_hi^2 + 2 r_hi r_lo
+  float a, ae, d_hi, d_e, c, ce, n_hi, n_e;
+  two_prod(t, t, a, ae);
+  two_sum(a, q2, d_hi, d_e);
+  const float d_lo = __fadd_rn(__fadd_rn(d_e, ae), -2.0f * t * s_lo);
+  two_prod(r_hi, r_hi, c, ce);
+  const float c_lo = __fadd_rn(ce, 2.0f * r_hi * r_lo);
+  two_sum(c, -d_hi, n_hi, n_e);
+  const float num = __fadd_rn(n_hi, __fsub_rn(__fadd_rn(n_e, c_lo), d_lo));
+  const float phi = num / (r_hi + sqrtf(d_hi));
+  float h = phi >= w ? 1.0f : 0.0f;
+  if (fabsf(phi) < w) h += 0.5f * (1.0f + phi / w + sinf(3.14159265f * phi / w) / 3.14159265f);
   return h;
 }
 
@@ -1011,20 +1153,31 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) advect_diffuse_ker
       float* const whi = static_cast<float*>(k.omega_hi);
       float* const wlo = static_cast<float*>(k.omega_lo);
       T* const chi = F<T>(k.chi);
-      const T zc = scalar<T>(k, SF_ZCM);
-      const T rbody = scalar<T>(k, SF_RBODY);
-      const T blendw = scalar<T>(k, SF_BLENDW);
-      const T zcol = (sediment && gjm < nz) ? CF<T>(k.zw)[gjm] : T(0);
       // a tile farther than radius + 2 w from the body centre (z_cm, 0) has
       // mask 0 at every cell (phi < -w) and adds nothing to the drag: the
       // per-cell mask is skipped there (the same values)
       bool near = sediment;
-      if (sediment) {
-        const T* zw = CF<T>(k.zw);
-        const T zlo = zw[j0], zhi = zw[min(j0 + TX, nz) - 1];
-        const T rlo = rowf[2][1];  // r of row i0
-        const T dz = zc < zlo ? zlo - zc : (zc > zhi ? zc - zhi : T(0));
-        const T reach = rbody + T(2) * blendw;
+      T zc = T(0), rbody = T(0), blendw = T(0), zcol = T(0);
+      if constexpr (sizeof(T) == 8) {
+        zc = scalar<T>(k, SF_ZCM);
+        rbody = scalar<T>(k, SF_RBODY);
+        blendw = scalar<T>(k, SF_BLENDW);
+        zcol = (sediment && gjm < nz) ? CF<T>(k.zw)[gjm] : T(0);
+        if (sediment) {
+          const T* zw = CF<T>(k.zw);
+          const T zlo = zw[j0], zhi = zw[min(j0 + TX, nz) - 1];
+          const T rlo = rowf[2][1];  // r of row i0
+          const T dz = zc < zlo ? zlo - zc : (zc > zhi ? zc - zhi : T(0));
+          const T reach = rbody + T(2) * blendw;
+          near = dz * dz + rlo * rlo <= reach * reach;
+        }
+      } else if (sediment) {
+        // in cells: centre column S, radius R, blend W
+        const float sc = scalar<T>(k, SF_S_HI);
+        const float zlo = (float)j0 + 0.5f, zhi = (float)(min(j0 + TX, nz) - 1) + 0.5f;
+        const float dz = sc < zlo ? zlo - sc : (sc > zhi ? sc - zhi : 0.0f);
+        const float rlo = (float)i0 + 0.5f;
+        const float reach = scalar<T>(k, SF_R_HI) + 2.0f * scalar<T>(k, SF_W) + 1.0f;
         near = dz * dz + rlo * rlo <= reach * reach;
       }
       const bool jin = gjm < nz, jint = gjm >= 1 && gjm < nz - 1;
@@ -1058,9 +1211,17 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) advect_diffuse_ker
             // then the drag integrand with the new mask (:164-173)
             if (near) {
               const T rr = rowf[2][pr + 1];
-              const T ch = sphere_mask<T>(zcol, rr, zc, rbody, blendw);
+              T ch;
+              if constexpr (sizeof(T) == 8) {
+                ch = sphere_mask<T>(zcol, rr, zc, rbody, blendw);
+                cd_part += rr * ch * sz[ad_box(pr, qm)];
+              } else {
+                ch = sphere_mask_cells(gi, gjm, scalar<T>(k, SF_S_HI), scalar<T>(k, SF_S_LO),
+                                       scalar<T>(k, SF_R_HI), scalar<T>(k, SF_R_LO),
+                                       scalar<T>(k, SF_W));
+                cd_part += rr * ch * sz[ad_box(pr, qm)];
+              }
               chi[c] = ch;
-              cd_part += rr * ch * sz[ad_box(pr, qm)];
             } else {
               chi[c] = T(0);
             }
@@ -1071,7 +1232,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) advect_diffuse_ker
       }
     }
     if (sediment) {
-      T x = cd_part;
+      double x = cd_part;
       for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
       if ((threadIdx.x & 31) == 0) red[it & 1][threadIdx.x >> 5] = (double)x;
     }
@@ -1322,7 +1483,7 @@ inline PlanView plan_view(const void* plan_dev, const axi_plan_info* info) {
 // kernels/FastDiagonalisationStokesSolver.py:137-156.
 // With `dct`, stages 0 and 2 run as z transforms (build_dct_jobs) and stage 1
 // writes its scaled result plain for the inverse transform.
-int build_tc_jobs(const axi_case& k, axi_tc::TcJob job[4], bool dct) {
+int build_tc_jobs(const axi_case& k, axi_tc::TcJob job[4], bool dct, bool refine) {
   const int nr = k.nr, nz = k.nz;
   const float* const* b = reinterpret_cast<const float* const*>(k.tc_basis);
   float* const* w = reinterpret_cast<float* const*>(k.tc_work);
@@ -1343,8 +1504,15 @@ int build_tc_jobs(const axi_case& k, axi_tc::TcJob job[4], bool dct) {
     AXI_TRY(axi_tc::encode_operand(&job[3].b_lo, w[1], nz, nr, nr));
     job[3].c = static_cast<float*>(k.psi); job[3].M = nr; job[3].N = nz;
     job[3].K = nr; job[3].ldc = nz; job[3].mode = axi_tc::MODE_PLAIN;
-    // both products store their tiles by TMA (outputs 16-byte aligned, nz % 4 == 0)
-    if (!axi_tc::encode_output(&job[1]) || !axi_tc::encode_output(&job[3])) {
+    if (refine) {
+      // the solve of the residual is the correction, added to the pair
+      // (psi, psi_lo) with its rounding kept in psi_lo
+      job[3].c_lo = static_cast<float*>(k.psi_lo);
+      job[3].mode = axi_tc::MODE_PAIR_ADD;
+    }
+    // products store their tiles by TMA where they overwrite (outputs 16-byte
+    // aligned, nz % 4 == 0)
+    if (!axi_tc::encode_output(&job[1]) || (!refine && !axi_tc::encode_output(&job[3]))) {
       axi::set_error("plan: tensor-core output map rejected (nz %d)", nz);
       return AXI_ERR_INVALID;
     }
@@ -1389,7 +1557,7 @@ int build_tc_jobs(const axi_case& k, axi_tc::TcJob job[4], bool dct) {
 // z transforms of one case: forward (DCT-II of the rows of omega into the
 // X operand pair) and inverse (DCT-III of the rows of the plain stage-1
 // result Y into the X operand pair of stage 3).
-int build_dct_jobs(const axi_case& k, axi_dct::DctJob* fwd, axi_dct::DctJob* inv) {
+int build_dct_jobs(const axi_case& k, axi_dct::DctJob* fwd, axi_dct::DctJob* inv, bool refine) {
   axi_dct::DctJob j;
   memset(&j, 0, sizeof(j));
   j.N = k.nz;
@@ -1408,6 +1576,15 @@ int build_dct_jobs(const axi_case& k, axi_dct::DctJob* fwd, axi_dct::DctJob* inv
   *fwd = j;
   fwd->in = static_cast<const float*>(k.omega);
   fwd->scale = reinterpret_cast<const float*>(t + (size_t)16 * k.nz);
+  if (refine) {
+    // the residual omega - (A psi) / r of the psi the case holds
+    fwd->psi = static_cast<const float*>(k.psi);
+    fwd->psi_lo = static_cast<const float*>(k.psi_lo);
+    fwd->rinv2dx = static_cast<const float*>(k.rinv2dx);
+    fwd->rinv2 = static_cast<const float*>(k.rinv2);
+    fwd->two_over_dx = (float)(2.0 / k.dx);
+    fwd->inv_2dx = (float)(0.5 / k.dx);
+  }
   *inv = j;
   inv->in = w[2];
   inv->scale = reinterpret_cast<const float*>(t + (size_t)20 * k.nz);
@@ -1439,11 +1616,17 @@ template <typename T>
 int stencil_attrs() {
   static int status = -1;
   if (status < 0) {
-    status = (cudaFuncSetAttribute(vel_max_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    bool pair_ok = true;
+    if constexpr (sizeof(T) == 4)
+      pair_ok = cudaFuncSetAttribute(penalise_kernel<T, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     penalise_smem<T, true>()) == cudaSuccess;
+    status = (pair_ok &&
+              cudaFuncSetAttribute(vel_max_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    vel_max_smem<T>()) == cudaSuccess &&
-              cudaFuncSetAttribute(penalise_kernel<T>,
+              cudaFuncSetAttribute(penalise_kernel<T, false>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   penalise_smem<T>()) == cudaSuccess &&
+                                   penalise_smem<T, false>()) == cudaSuccess &&
               cudaFuncSetAttribute(advect_diffuse_kernel<T>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    advect_diffuse_smem<T>()) == cudaSuccess)
@@ -1456,32 +1639,39 @@ int stencil_attrs() {
 
 template <typename T>
 struct StencilGrid {
-  // blocks per SM of each stencil phase, measured once
-  static int per_sm(int phase) {
-    static int n[PH_COUNT] = {0};
-    if (n[phase] == 0) {
+  // blocks per SM of each stencil phase, measured once (slot PH_COUNT: the
+  // penalise variant that reads psi as a pair)
+  static int per_sm(int phase, bool pair = false) {
+    static int n[PH_COUNT + 1] = {0};
+    const int slot = (phase == PH_PENALISE && pair) ? PH_COUNT : phase;
+    if (n[slot] == 0) {
       int b = 0;
       cudaError_t e = cudaErrorInvalidValue;
       if (phase == PH_VEL_MAX)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, vel_max_kernel<T>, NT,
                                                           vel_max_smem<T>());
+      else if (phase == PH_PENALISE && pair && sizeof(T) == 4)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, penalise_kernel<T, sizeof(T) == 4>,
+                                                          NT, penalise_smem<T, sizeof(T) == 4>());
       else if (phase == PH_PENALISE)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, penalise_kernel<T>, NT,
-                                                          penalise_smem<T>());
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, penalise_kernel<T, false>, NT,
+                                                          penalise_smem<T, false>());
       else if (phase == PH_ADVECT_DIFFUSE)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, advect_diffuse_kernel<T>, NT,
                                                           advect_diffuse_smem<T>());
-      n[phase] = (e == cudaSuccess && b > 0) ? b : 1;
+      n[slot] = (e == cudaSuccess && b > 0) ? b : 1;
     }
-    return n[phase];
+    return n[slot];
   }
   // blocks of the phase resident on the GPU at once
-  static int resident(int phase) { return per_sm(phase) * axi::sm_count(); }
-  static int get(int phase, int n_tiles) {
+  static int resident(int phase, bool pair = false) {
+    return per_sm(phase, pair) * axi::sm_count();
+  }
+  static int get(int phase, int n_tiles, bool pair = false) {
     // ring depth 1: one block per tile
     if ((phase == PH_PENALISE && PN_NBUF == 1) || (phase == PH_ADVECT_DIFFUSE && AD_NBUF == 1))
       return n_tiles;
-    const int g = per_sm(phase) * axi::sm_count();
+    const int g = per_sm(phase, pair) * axi::sm_count();
     return n_tiles < g ? n_tiles : g;
   }
 };
@@ -1522,8 +1712,19 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
       break;
     case PH_PENALISE:
       AXI_TRY(stencil_attrs<T>());
-      penalise_kernel<T><<<StencilGrid<T>::get(PH_PENALISE, nt), NT, penalise_smem<T>(), s>>>(
-          v.cases, v.stencil, nt, v.maps, v.err, StencilGrid<T>::resident(PH_PENALISE));
+      if constexpr (sizeof(T) == 4) {
+        if (info->flags & AXI_PLAN_REFINE) {
+          // psi read as psi + psi_lo
+          penalise_kernel<T, true>
+              <<<StencilGrid<T>::get(PH_PENALISE, nt), NT, penalise_smem<T, true>(), s>>>(
+                  v.cases, v.stencil, nt, v.maps, v.err,
+                  StencilGrid<T>::resident(PH_PENALISE, true));
+          break;
+        }
+      }
+      penalise_kernel<T, false>
+          <<<StencilGrid<T>::get(PH_PENALISE, nt), NT, penalise_smem<T, false>(), s>>>(
+              v.cases, v.stencil, nt, v.maps, v.err, StencilGrid<T>::resident(PH_PENALISE));
       break;
     case PH_ADVECT_DIFFUSE:
       AXI_TRY(stencil_attrs<T>());
@@ -1635,6 +1836,17 @@ extern "C" int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, int f
   AXI_TRY(gemm_tile_dims(elem_bytes, &bm, &bn));
   const bool tc = (flags & AXI_PLAN_TENSOR_CORES) != 0;
   const bool dct = (flags & AXI_PLAN_DCT_Z) != 0;
+  const bool refine = (flags & AXI_PLAN_REFINE) != 0;
+  if (refine && !dct) {
+    axi::set_error("plan_init: refinement runs on the DCT z transform (AXI_PLAN_DCT_Z)");
+    return AXI_ERR_INVALID;
+  }
+  for (int c = 0; refine && c < n_cases; ++c) {
+    if (!cases[c].psi_lo) {
+      axi::set_error("plan_init: case %d: refinement needs psi_lo", c);
+      return AXI_ERR_INVALID;
+    }
+  }
   if (tc && elem_bytes != 4) {
     axi::set_error("plan_init: tensor-core products need float32 fields");
     return AXI_ERR_INVALID;
@@ -1678,7 +1890,8 @@ extern "C" int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, int f
   info->n_stencil_tiles = nt;
   info->n_gemm_tiles = ng;
   info->elem_bytes = elem_bytes;
-  info->flags = (tc ? AXI_PLAN_TENSOR_CORES : 0) | (dct ? AXI_PLAN_DCT_Z : 0);
+  info->flags = (tc ? AXI_PLAN_TENSOR_CORES : 0) | (dct ? AXI_PLAN_DCT_Z : 0) |
+                (refine ? AXI_PLAN_REFINE : 0);
   info->n_dct_items = nd;
   info->bytes = (int64_t)plan_offsets(info).total;
   return AXI_OK;
@@ -1728,19 +1941,22 @@ extern "C" int axi_plan_upload(const axi_case* cases, const axi_plan_info* info,
     AXI_TRY(axi_tma::encode_box(m + MAP_W, k.omega, eb, k.nr, k.nz, ADV_ROWS, BOXW));
     AXI_TRY(axi_tma::encode_box(m + MAP_UZ, k.u_z, eb, k.nr, k.nz, ADV_ROWS, BOXW));
     AXI_TRY(axi_tma::encode_box(m + MAP_UR, k.u_r, eb, k.nr, k.nz, ADV_ROWS, BOXW));
+    if (info->flags & AXI_PLAN_REFINE)
+      AXI_TRY(axi_tma::encode_box(m + MAP_PSI_LO, k.psi_lo, eb, k.nr, k.nz, PSI_ROWS, BOXW));
   }
   if (info->flags & AXI_PLAN_TENSOR_CORES) {
     const PlanOffsets& o = po;
     axi_tc::TcJob* jobs = reinterpret_cast<axi_tc::TcJob*>(&buf[o.jobs]);
     const bool dct = (info->flags & AXI_PLAN_DCT_Z) != 0;
-    for (int c = 0; c < n; ++c) AXI_TRY(build_tc_jobs(cases[c], jobs + 4 * c, dct));
+    const bool refine = (info->flags & AXI_PLAN_REFINE) != 0;
+    for (int c = 0; c < n; ++c) AXI_TRY(build_tc_jobs(cases[c], jobs + 4 * c, dct, refine));
     if (dct) {
       axi_dct::DctJob* dj = reinterpret_cast<axi_dct::DctJob*>(&buf[o.dct_jobs]);
       int4* di = reinterpret_cast<int4*>(&buf[o.dct_items]);
       int q = 0;
       int nz_min = 1 << 30;
       for (int c = 0; c < n; ++c) {
-        AXI_TRY(build_dct_jobs(cases[c], dj + c, dj + n + c));
+        AXI_TRY(build_dct_jobs(cases[c], dj + c, dj + n + c, refine));
         nz_min = cases[c].nz < nz_min ? cases[c].nz : nz_min;
       }
       // items in case order, the shortest rows' items last: the last wave of

@@ -259,6 +259,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int row0 = tr.y + 32 * q;
       const bool scaled = mode == MODE_SCALE_SPLIT || mode == MODE_SCALE;
       const bool split = mode == MODE_SPLIT || mode == MODE_SCALE_SPLIT;
+      const bool pair = mode == MODE_PAIR_ADD;
 #pragma unroll 1
       for (int cc = half * CHUNKS; cc < (half + 1) * CHUNKS; ++cc) {
         const int col = tr.z + cc * 32 + lane;
@@ -271,6 +272,18 @@ __global__ void __launch_bounds__(THREADS, 1)
           for (int rr = 0; rr < 32; ++rr) {
             const int row = row0 + rr;
             sv[rr] = (col < Nc && row < M) ? __ldg(scl + (long long)row * Nc + col) : 0.0f;
+          }
+        }
+        // the pair the product is added to, likewise in flight before the read
+        float ph[32], pl[32];
+        if (pair) {
+#pragma unroll
+          for (int rr = 0; rr < 32; ++rr) {
+            const int row = row0 + rr;
+            const bool in = col < Nc && row < M;
+            const long long idx = (long long)row * ldc + col;
+            ph[rr] = in ? c[idx] : 0.0f;
+            pl[rr] = in ? c_lo[idx] : 0.0f;
           }
         }
         uint32_t r[32];
@@ -305,7 +318,12 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (scaled) v *= sv[rr];
             if (row < M) {
               const long long idx = (long long)row * ldc + col;
-              if (split) {
+              if (pair) {
+                float hi = ph[rr], lo = pl[rr];
+                axi_eft::pair_add(hi, lo, v);
+                c[idx] = hi;
+                c_lo[idx] = lo;
+              } else if (split) {
                 float hi, lo;
                 tf32_split(v, hi, lo);
                 c[idx] = hi;

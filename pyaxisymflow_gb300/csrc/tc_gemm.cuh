@@ -58,7 +58,10 @@ constexpr int EPI_STAGE_BYTES = EPI_WARPS * 32 * 33 * 4;
 static_assert(EPI_WARPS * 4096 <= EPI_STAGE_BYTES, "TMA store boxes fit the staging region");
 constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 + EPI_STAGE_BYTES + 256;
 
-enum { MODE_PLAIN = 0, MODE_SPLIT = 1, MODE_SCALE_SPLIT = 2, MODE_SCALE = 3 };
+// MODE_PAIR_ADD: the output is the float pair (c, c_lo) holding c + c_lo;
+// the product is added to it and the pair renormalised (c the rounded sum,
+// c_lo the exact remainder), so repeated additions keep about 48 bits.
+enum { MODE_PLAIN = 0, MODE_SPLIT = 1, MODE_SCALE_SPLIT = 2, MODE_SCALE = 3, MODE_PAIR_ADD = 4 };
 enum { ERR_PRODUCER = 1, ERR_MMA = 2, ERR_EPILOGUE = 3, ERR_DRAIN = 4 };
 
 // One GEMM problem. Tensor maps are encoded on the host (cuTensorMapEncodeTiled)
@@ -67,7 +70,7 @@ struct TcJob {
   CUtensorMap a_hi, a_lo, b_hi, b_lo;
   CUtensorMap c_map;   // MODE_PLAIN with c_tma: the output in 32 x 32 boxes for TMA stores
   float* c;            // output (MODE_PLAIN) or its hi part
-  float* c_lo;         // lo part (split modes)
+  float* c_lo;         // lo part (split modes; MODE_PAIR_ADD: low part of the pair)
   const float* scale;  // elementwise factor, row-major (M, N) (MODE_SCALE*)
   int M, N, K, ldc;
   int mode;

@@ -54,6 +54,7 @@ class AxiCase(ctypes.Structure):
         ("omega_hi", ctypes.c_void_p), ("omega_lo", ctypes.c_void_p),
         ("tc_basis", ctypes.c_void_p * 8), ("tc_work", ctypes.c_void_p * 4),
         ("dct_table", ctypes.c_void_p),
+        ("psi_lo", ctypes.c_void_p),
     ]
 
 
@@ -142,6 +143,7 @@ class AxiPlanInfo(ctypes.Structure):
 
 PLAN_TENSOR_CORES = 1
 PLAN_DCT_Z = 2
+PLAN_REFINE = 4
 
 
 def dct_ok(nz):
@@ -248,6 +250,9 @@ class CaseState:
         if ens.tensor_cores:
             t["tc_work"] = [torch.zeros(c.nr * c.nz, dtype=torch.float32, device=dev)
                             for _ in range(4)]
+        if ens.refine:
+            # low part of psi: the refined solve keeps psi as psi + psi_lo
+            t["psi_lo"] = torch.zeros((c.nr, c.nz), dtype=torch.float32, device=dev)
         self.fields = t
         self.history = (torch.zeros((history_steps, 2), **f64) if history_steps else None)
         st = ens.state_arena[slot]
@@ -290,6 +295,8 @@ class CaseState:
                 s.tc_work[q] = t["tc_work"][q].data_ptr()
         if ens.dct:
             s.dct_table = b.dct_table.data_ptr()
+        if ens.refine:
+            s.psi_lo = t["psi_lo"].data_ptr()
         s.state = st.data_ptr()
         if self.history is not None:
             s.history = self.history.data_ptr()
@@ -309,7 +316,8 @@ class RigidEnsemble:
     step. Cases may join (add_case) and leave (remove_case) between steps."""
 
     def __init__(self, cases, precision="f64", device="cuda", history_steps=0,
-                 initial_vorticity=None, tensor_cores=None, capacity=None, dct=None):
+                 initial_vorticity=None, tensor_cores=None, capacity=None, dct=None,
+                 refine=None):
         if precision not in ("f64", "f32"):
             raise ValueError("precision must be 'f64' or 'f32'")
         if tensor_cores is None:
@@ -323,8 +331,14 @@ class RigidEnsemble:
             dct = tensor_cores and all(dct_ok(c.nz) for c in cases)
         if dct and not tensor_cores:
             raise ValueError("the DCT z transform goes with the tensor-core products")
+        if refine is None:
+            # each solve one refinement step from the psi of the previous step
+            refine = dct
+        if refine and not dct:
+            raise ValueError("refinement of the solve runs with the DCT z transform")
         self.tensor_cores = tensor_cores
         self.dct = dct
+        self.refine = refine
         self.precision = precision
         self.dtype = torch.float64 if precision == "f64" else torch.float32
         self.device = torch.device(device)
@@ -390,7 +404,8 @@ class RigidEnsemble:
             return
         lib = N.lib()
         esize = 8 if self.precision == "f64" else 4
-        flags = (PLAN_TENSOR_CORES if self.tensor_cores else 0) | (PLAN_DCT_Z if self.dct else 0)
+        flags = ((PLAN_TENSOR_CORES if self.tensor_cores else 0) | (PLAN_DCT_Z if self.dct else 0)
+                 | (PLAN_REFINE if self.refine else 0))
         N.check(lib.axi_plan_init(ctypes.addressof(self.structs), n, esize, flags,
                                   ctypes.byref(self.info)), "plan_init")
         self.n_tiles = self.info.n_stencil_tiles

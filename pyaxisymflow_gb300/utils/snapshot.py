@@ -7,8 +7,9 @@ ensemble continues bit-identically: per case its parameters (the
 RigidBodyCase fields as JSON), omega, the body mask chi (rebuilt each step for
 a sedimenting sphere), the state block (time, dt, drag, body position and
 velocity, step count, ...) and the (dt, Cd) history, plus the engine options
-(precision, tensor cores, z transform). psi, u_z and u_r are saved as well
-for post-processing; the next step recomputes them from omega.
+(precision, tensor cores, z transform, refinement). psi is saved, and with
+refinement its low part psi_lo too: the refined solve starts from the pair.
+u_z and u_r are saved for post-processing; the next step recomputes them.
 """
 import dataclasses
 import json
@@ -17,6 +18,11 @@ import numpy as np
 
 FORMAT = "pyaxisymflow-gb300 rigid ensemble snapshot 1"
 FIELDS = ("omega", "psi", "u_z", "u_r", "chi")
+REFINE_FIELDS = ("psi_lo",)
+
+
+def _fields(refine):
+    return FIELDS + (REFINE_FIELDS if refine else ())
 
 
 def ensemble_snapshot(ens):
@@ -28,9 +34,11 @@ def ensemble_snapshot(ens):
         "precision": ens.precision,
         "tensor_cores": bool(ens.tensor_cores),
         "dct": bool(ens.dct),
+        "refine": bool(ens.refine),
         "cases": [dataclasses.asdict(c) for c in ens.cases],
         "state": ens.state.cpu().numpy().copy(),
-        "fields": [{n: m.fields[n].cpu().numpy().copy() for n in FIELDS} for m in ens.members],
+        "fields": [{n: m.fields[n].cpu().numpy().copy() for n in _fields(ens.refine)}
+                   for m in ens.members],
         "history": [None if m.history is None else m.history.cpu().numpy().copy()
                     for m in ens.members],
     }
@@ -40,10 +48,11 @@ def ensemble_snapshot(ens):
 def write_snapshot(path, snap):
     """Writes a snapshot dict as .npz (arrays stored as they are)."""
     meta = {k: snap[k] for k in ("format", "precision", "tensor_cores", "dct", "cases")}
+    meta["refine"] = bool(snap.get("refine", False))
     meta["history_steps"] = [0 if h is None else int(h.shape[0]) for h in snap["history"]]
     arrays = {"meta": np.array(json.dumps(meta)), "state": snap["state"]}
     for k, f in enumerate(snap["fields"]):
-        for n in FIELDS:
+        for n in _fields(meta["refine"]):
             arrays[f"{n}_{k}"] = f[n]
     for k, h in enumerate(snap["history"]):
         if h is not None:
@@ -59,8 +68,10 @@ def read_snapshot(path):
             raise ValueError(f"{path}: not a rigid ensemble snapshot")
         n = len(meta["cases"])
         snap = {k: meta[k] for k in ("format", "precision", "tensor_cores", "dct", "cases")}
+        snap["refine"] = bool(meta.get("refine", False))
         snap["state"] = z["state"].copy()
-        snap["fields"] = [{f: z[f"{f}_{k}"].copy() for f in FIELDS} for k in range(n)]
+        snap["fields"] = [{f: z[f"{f}_{k}"].copy() for f in _fields(snap["refine"])}
+                          for k in range(n)]
         snap["history"] = [z[f"history_{k}"].copy() if meta["history_steps"][k] else None
                            for k in range(n)]
     return snap
@@ -78,12 +89,13 @@ def restore_ensemble(snap, device="cuda"):
     ens = RigidEnsemble(cases, precision=snap["precision"], device=device,
                         history_steps=steps.pop() if steps else 0,
                         initial_vorticity=[f["omega"] for f in snap["fields"]],
-                        tensor_cores=snap["tensor_cores"], dct=snap["dct"])
+                        tensor_cores=snap["tensor_cores"], dct=snap["dct"],
+                        refine=bool(snap.get("refine", False)))
     state = np.asarray(snap["state"], dtype=np.float64)
     if state.shape != (len(cases), ST_WORDS):
         raise ValueError("state block shape does not match the cases")
     for k, m in enumerate(ens.members):
-        for n in FIELDS:
+        for n in _fields(ens.refine):
             m.fields[n].copy_(torch.as_tensor(snap["fields"][k][n]).to(m.fields[n].dtype))
         if m.history is not None:
             m.history.copy_(torch.as_tensor(snap["history"][k]))

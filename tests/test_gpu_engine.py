@@ -275,3 +275,40 @@ def test_engine_sedimenting_sphere_matches_oracle(precision, tol):
     assert err < tol * 10, err
     chi_err = np.abs(e.fields[0]["chi"].double().cpu().numpy() - st.char_func).max()
     assert chi_err < (1e-12 if precision == "f64" else 1e-5), chi_err
+
+
+def test_engine_refined_solve_matches_fp64_solve():
+    """The FP32 engine's solve with one refinement step per solve, started
+    from the previous step's psi (AXI_PLAN_REFINE, the default with the DCT z
+    transform) and kept as the pair psi + psi_lo: after a few steps, psi of
+    the kill + transform phases equals the FP64 solve of the same (float)
+    vorticity to better than float resolution, closer than the plain FP32
+    solve."""
+    from pyaxisymflow_gb300.engine import RigidBodyCase, RigidEnsemble
+    from pyaxisymflow_gb300.kernels.FastDiagonalisationStokesSolver import \
+        FastDiagonalisationStokesSolver
+    cases = [RigidBodyCase(nz=256, nr=128, dx=2.0 / 256, r_sphere=0.08, Re=300.0, seed=3),
+             RigidBodyCase(nz=768, nr=384, dx=2.0 / 768, r_sphere=0.06, z_cm=1.4, U0=0.0,
+                           ramp=False, sediment=True, rho_s=2.0, Re=500.0, seed=4)]
+    errs = {}
+    for refine in (True, False):
+        e = RigidEnsemble(cases, precision="f32", dct=True, refine=refine)
+        assert e.refine == refine
+        e.step(30)
+        e.phase(0)      # kill
+        e.phase(1)      # transform: psi of the current vorticity
+        torch.cuda.synchronize()
+        assert not e.status().any()
+        worst = 0.0
+        for k, c in enumerate(cases):
+            s64 = FastDiagonalisationStokesSolver(c.nr, c.nz, c.dx, device="cuda")
+            psi = torch.zeros((c.nr, c.nz), dtype=torch.float64, device="cuda")
+            s64.solve(psi, e.fields[k]["omega"].double())
+            mine = e.fields[k]["psi"].double()
+            if refine:
+                mine = mine + e.fields[k]["psi_lo"].double()
+            worst = max(worst, rel_l2(mine.cpu().numpy(), psi.cpu().numpy()))
+        errs[refine] = worst
+    print("psi rel L2 vs the FP64 solve of the same vorticity:", errs)
+    assert errs[True] < 1e-7, errs
+    assert errs[True] < errs[False], errs
