@@ -45,6 +45,8 @@ PHASES = ("kill", "transform", "vel_max", "penalise", "advect_diffuse")
 # u_z u_r -> omega (+ omega's TF32 hi / lo operand copy on the tensor-core
 # path, + the rebuilt mask of sedimenting bodies).
 PHASE_FIELDS = {"vel_max": 1, "penalise": 6, "advect_diffuse": 4}
+# the same in the FP64 engine (sedimenting bodies: + the rebuilt mask)
+PHASE_FIELDS_F64 = {"vel_max": 1, "penalise": 6, "advect_diffuse": 5}
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of a phase, from the
@@ -213,6 +215,105 @@ def cpu_oracle_rate(cases, steps, min_seconds=0.0):
     return runs.cells * rounds / secs, secs, rounds
 
 
+def phase_times(ens, stream, n):
+    """Mean device time (ms) of each phase of a step, CUDA events on `stream`."""
+    import torch
+    out = {p: 0.0 for p in PHASES}
+    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            for _ in PHASES] for _ in range(n)]
+    for s in range(n):
+        for k, _ in enumerate(PHASES):
+            evs[s][k][0].record(stream)
+            ens.phase(k)
+            evs[s][k][1].record(stream)
+    torch.cuda.synchronize()
+    for s in range(n):
+        for k, p in enumerate(PHASES):
+            out[p] += evs[s][k][0].elapsed_time(evs[s][k][1]) / n
+    return out
+
+
+def accuracy_cases(cases):
+    """Indices of the hardest cases of the seeded ensemble per grid size: the
+    highest Reynolds number and the smallest sphere."""
+    idx = []
+    for nz in sorted({c.nz for c in cases}):
+        group = [k for k, c in enumerate(cases) if c.nz == nz]
+        for k in (max(group, key=lambda q: cases[q].Re),
+                  min(group, key=lambda q: cases[q].r_sphere)):
+            if k not in idx:
+                idx.append(k)
+    return idx
+
+
+def fp32_accuracy(cases, dev, steps):
+    """Relative L2 error of the FP32 engine against the FP64 engine (within
+    1e-12 of the FP64 oracle) on the hardest cases, at checkpoints up to
+    `steps`, with two FP64 controls run the same way: the initial vorticity
+    moved by one double ulp (does the flow amplify round-off?) and the sphere
+    radius moved by one float ulp at the same viscosity (how far does a
+    float-sized change of the problem itself move the fields?)."""
+    import dataclasses
+
+    import torch
+
+    from pyaxisymflow_gb300.engine import ST_UBODY, ST_ZCM, RigidEnsemble
+    idx = accuracy_cases(cases)
+    sel = [cases[k] for k in idx]
+    w0 = [c.noise * np.random.default_rng(c.seed).standard_normal((c.nr, c.nz)) for c in sel]
+    ulp = 2.0 ** -24
+    wider = [dataclasses.replace(c, r_sphere=c.r_sphere * (1 + ulp), Re=c.Re * (1 + ulp))
+             for c in sel]
+    checkpoints = sorted({steps // 4, steps // 2, steps})
+    fields = ("omega", "psi", "u_z", "u_r")
+
+    def snaps(ens):
+        out = {}
+        for s in range(1, steps + 1):
+            ens.step(1)
+            if s in checkpoints:
+                rows = []
+                for m in ens.members:
+                    f = {n: m.fields[n].double().clone() for n in fields}
+                    if "psi_lo" in m.fields:
+                        f["psi"] += m.fields["psi_lo"].double()
+                    rows.append(f)
+                out[s] = (rows, ens.state.cpu().numpy().copy())
+        torch.cuda.synchronize(dev)
+        return out
+
+    ref = snaps(RigidEnsemble(sel, precision="f64", device=dev, initial_vorticity=w0))
+    runs = {
+        "fp32": snaps(RigidEnsemble(sel, precision="f32", device=dev, initial_vorticity=w0)),
+        "fp64_double_ulp_noise": snaps(RigidEnsemble(
+            sel, precision="f64", device=dev,
+            initial_vorticity=[np.nextafter(w, np.inf) for w in w0])),
+        "fp64_radius_float_ulp": snaps(RigidEnsemble(wider, precision="f64", device=dev,
+                                                     initial_vorticity=w0)),
+    }
+    per_case = []
+    for q, c in enumerate(sel):
+        row = {"case": idx[q], "grid": f"{c.nz}x{c.nr}", "Re": c.Re, "radius": c.r_sphere,
+               "density_ratio": c.rho_s}
+        for name, sn in runs.items():
+            row[name] = {}
+            for s in checkpoints:
+                a, sa = sn[s]
+                b, sb = ref[s]
+                e = {n: float(torch.linalg.norm(a[q][n] - b[q][n]) / torch.linalg.norm(b[q][n]))
+                     for n in fields}
+                e["z_body"] = float(abs(sa[q, ST_ZCM] - sb[q, ST_ZCM]) / abs(sb[q, ST_ZCM]))
+                e["U_body"] = float(abs(sa[q, ST_UBODY] - sb[q, ST_UBODY])
+                                    / max(abs(sb[q, ST_UBODY]), 1e-300))
+                row[name][str(s)] = e
+        per_case.append(row)
+    last = str(steps)
+    summary = {name: {n: max(r[name][last][n] for r in per_case) for n in fields}
+               for name in runs}
+    return {"steps": steps, "checkpoints": checkpoints, "cases": idx,
+            "max_rel_l2_at_end": summary, "per_case": per_case}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -343,38 +444,36 @@ def run_gb300(args, world, rank, local):
     if args.precision == "f32" and not args.no_fp64_compare:
         del ens
         torch.cuda.empty_cache()
-        e64 = RigidEnsemble(cases, precision="f64", device=dev)
-        e64.step(1)
-        torch.cuda.synchronize(dev)
-        f0 = torch.cuda.Event(enable_timing=True)
-        f1 = torch.cuda.Event(enable_timing=True)
-        nf = 3
-        f0.record(stream)
-        e64.step(nf)
-        f1.record(stream)
-        torch.cuda.synchronize(dev)
-        fp64_ms = f0.elapsed_time(f1) / nf
-        del e64
-        torch.cuda.empty_cache()
-        # accuracy of the FP32 engine against the FP64 engine (itself within
-        # 1e-12 of the FP64 oracle) after many steps on one case of each size
-        errs = {}
-        nsteps = 300
-        for nz in sorted({c.nz for c in cases}):
-            c = next(c for c in cases if c.nz == nz)
-            a = RigidEnsemble([c], precision="f64", device=dev)
-            b = RigidEnsemble([c], precision="f32", device=dev)
-            a.step(nsteps)
-            b.step(nsteps)
+        fp64 = {}
+        for variant, dct in (("dct", True), ("dense", False)):
+            e64 = RigidEnsemble(cases, precision="f64", device=dev, dct=dct)
+            e64.step(1)
             torch.cuda.synchronize(dev)
-            for f in ("omega", "psi", "u_z", "u_r"):
-                x = b.fields[0][f].double()
-                y = a.fields[0][f]
-                e = float(torch.linalg.norm(x - y) / torch.linalg.norm(y))
-                errs[f] = max(errs.get(f, 0.0), e)
-        fp64 = {"value": cells * world / (fp64_ms / 1000.0), "ms_per_step": fp64_ms,
-                "speedup_fp32_over_fp64": fp64_ms / ms_per_step,
-                "rel_l2_fp32_vs_fp64_max_over_sizes": errs, "accuracy_steps": nsteps}
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            nf = 3
+            f0.record(stream)
+            e64.step(nf)
+            f1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms64 = f0.elapsed_time(f1) / nf
+            entry = {"value": cells * world / (ms64 / 1000.0), "ms_per_step": ms64,
+                     "speedup_fp32_over_fp64": ms64 / ms_per_step,
+                     "z_transform": "FP64 DCT" if dct else "dense FP64 products"}
+            if dct:
+                # per-phase device times of the FP64 step, and its stencil passes'
+                # algorithmic bytes (FP64 fields) over their time
+                p64 = phase_times(e64, stream, 3)
+                entry["phase_ms"] = p64
+                b64 = sum(sum(PHASE_FIELDS_F64.values()) * 8 * c.nr * c.nz for c in cases)
+                entry["stencil_hbm_gbs"] = b64 / (sum(p64[p] for p in PHASE_FIELDS_F64)
+                                                   / 1000.0) / 1e9
+            fp64[variant] = entry
+            del e64
+            torch.cuda.empty_cache()
+        fp64["speedup_fp32_over_fp64"] = fp64["dct"]["speedup_fp32_over_fp64"]
+        if not args.no_accuracy:
+            fp64["accuracy"] = fp32_accuracy(cases, dev, args.accuracy_steps)
     # ---- roofline of the dominant kernel ---------------------------------------
     hbm, bf16, src = peaks()
     esize = 8 if args.precision == "f64" else 4
@@ -740,6 +839,9 @@ def main():
     ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the FP32-vs-FP64 comparison over --accuracy-steps steps")
+    ap.add_argument("--accuracy-steps", type=int, default=2000)
     ap.add_argument("--z-transform", default="default", choices=["default", "dense", "dct"],
                     help="FP32 engine: z products as dense tensor-core GEMMs or as DCTs")
     args = ap.parse_args()

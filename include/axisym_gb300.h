@@ -490,8 +490,9 @@ typedef struct axi_case {
   const void* tc_basis[8]; /* E_z^-1 hi, lo (nz, nz); E_r^-1 diag(r) hi, lo (nr, nr);
                               E_z hi, lo (nz, nz); E_r hi, lo (nr, nr) */
   void* tc_work[4];        /* X hi, lo (nz, nr); Y hi, lo (nr, nz) */
-  /* AXI_PLAN_DCT_Z: float tables of the z transform for this nz (shared by
-   * cases of equal nz): exp(-2 pi i m / nz) as (cos, sin) pairs, m < nz;
+  /* AXI_PLAN_DCT_Z: tables of the z transform for this nz (shared by cases of
+   * equal nz), float for the float engine and double for the double engine:
+   * exp(-2 pi i m / nz) as (cos, sin) pairs, m < nz;
    * (cos, sin)(pi k / 2 nz), k < nz; c_k; 1 / c_k (c_0 = sqrt(1 / nz),
    * c_k = sqrt(2 / nz)); inv_eig then holds 1 / (lambda_r_i + lambda_z_k) in
    * DCT order, lambda_z_k = (2 - 2 cos(pi k / nz)) / dx^2. */
@@ -515,11 +516,13 @@ typedef struct axi_plan_info {
   int32_t n_dct_items;     /* row groups of the z transforms (AXI_PLAN_DCT_Z) */
 } axi_plan_info;
 
-/* AXI_PLAN_DCT_Z (with AXI_PLAN_TENSOR_CORES): the z-direction products run
- * as orthonormal DCT-II / DCT-III transforms (the eigenbasis of the Neumann
- * z operator), the radial ones on the tensor cores; every nz even with no
- * prime factor other than 2 and 3; omega_hi / omega_lo and the z entries of
- * tc_basis are then unused (may be NULL). */
+/* AXI_PLAN_DCT_Z: the z-direction products run as orthonormal DCT-II /
+ * DCT-III transforms (the eigenbasis of the Neumann z operator); every nz
+ * even with no prime factor other than 2 and 3. Float fields (with
+ * AXI_PLAN_TENSOR_CORES): the radial products on the tensor cores,
+ * omega_hi / omega_lo and the z entries of tc_basis unused (may be NULL).
+ * Double fields (without it): the radial products on the SIMT FP64 GEMM,
+ * nz <= 2048, dct_table holding the tables in double. */
 /* AXI_PLAN_REFINE (with AXI_PLAN_DCT_Z): every solve is one step of
  * iterative refinement started from the psi the case already holds (the
  * previous step's; zero for a new case): the forward z transform reads the

@@ -31,6 +31,7 @@
 
 #include "axi_common.cuh"
 #include "dct.cuh"
+#include "dct64.cuh"
 #include "tc_gemm.cuh"
 #include "tma.cuh"
 
@@ -1410,6 +1411,7 @@ struct PlanView {
   const int4* tc_tiles[4];
   const axi_dct::DctJob* dct_jobs;  // forward jobs, then inverse jobs (n_cases each)
   const int4* dct_items;
+  const axi_dct64::Job* dct64_jobs;  // double engine: forward, then inverse jobs
   int* err;
 };
 
@@ -1442,7 +1444,9 @@ inline PlanOffsets plan_offsets(const axi_plan_info* info) {
   }
   if (info->flags & AXI_PLAN_DCT_Z) {
     o.dct_jobs = align128(end);
-    end = o.dct_jobs + (size_t)2 * info->n_cases * sizeof(axi_dct::DctJob);
+    const size_t job_bytes =
+        info->elem_bytes == 8 ? sizeof(axi_dct64::Job) : sizeof(axi_dct::DctJob);
+    end = o.dct_jobs + (size_t)2 * info->n_cases * job_bytes;
     o.dct_items = align16(end);
     end = o.dct_items + (size_t)info->n_dct_items * sizeof(int4);
   } else {
@@ -1467,7 +1471,11 @@ inline PlanView plan_view(const void* plan_dev, const axi_plan_info* info) {
   for (int st = 0; st < 4; ++st)
     v.tc_tiles[st] = tc ? reinterpret_cast<const int4*>(base + o.tc_tiles[st]) : nullptr;
   const bool dct = (info->flags & AXI_PLAN_DCT_Z) != 0;
-  v.dct_jobs = dct ? reinterpret_cast<const axi_dct::DctJob*>(base + o.dct_jobs) : nullptr;
+  const bool dbl = info->elem_bytes == 8;
+  v.dct_jobs =
+      (dct && !dbl) ? reinterpret_cast<const axi_dct::DctJob*>(base + o.dct_jobs) : nullptr;
+  v.dct64_jobs =
+      (dct && dbl) ? reinterpret_cast<const axi_dct64::Job*>(base + o.dct_jobs) : nullptr;
   v.dct_items = dct ? reinterpret_cast<const int4*>(base + o.dct_items) : nullptr;
   v.err = reinterpret_cast<int*>(const_cast<char*>(base) + o.err);
   return v;
@@ -1597,6 +1605,42 @@ inline int dct_items_of(const axi_case& k) {
   return (k.nr + r - 1) / r;
 }
 
+// Double engine: z transforms of one case on the SIMT product buffers
+// (gemm_work = w1 | w2, each (nr, nz)): forward omega -> w1 (in place of the
+// E_z^-T product), inverse w2 -> w1 (in place of the E_z^T product). The
+// table k.dct_table holds doubles: exp(-2 pi i m / nz) as (cos, sin),
+// (cos, sin)(pi k / 2 nz), c_k, 1 / c_k.
+int build_dct64_jobs(const axi_case& k, axi_dct64::Job* fwd, axi_dct64::Job* inv) {
+  axi_dct64::Job j;
+  memset(&j, 0, sizeof(j));
+  j.N = k.nz;
+  j.rows = k.nr;
+  if (!axi_dct64::plan_radices(k.nz, j.radix, &j.nstages)) {
+    axi::set_error("plan: nz %d has no double DCT plan (even, factors 2 and 3 only, <= %d)",
+                   k.nz, axi_dct64::ELEMS);
+    return AXI_ERR_INVALID;
+  }
+  const double* t = static_cast<const double*>(k.dct_table);
+  j.twiddle = reinterpret_cast<const double2*>(t);
+  j.rot = reinterpret_cast<const double2*>(t + (size_t)2 * k.nz);
+  double* w1 = static_cast<double*>(k.gemm_work);
+  double* w2 = w1 + (size_t)k.nr * k.nz;
+  *fwd = j;
+  fwd->in = static_cast<const double*>(k.omega);
+  fwd->out = w1;
+  fwd->scale = t + (size_t)4 * k.nz;
+  *inv = j;
+  inv->in = w2;
+  inv->out = w1;
+  inv->scale = t + (size_t)5 * k.nz;
+  return AXI_OK;
+}
+
+inline int dct64_items_of(const axi_case& k) {
+  const int r = axi_dct64::rows_per_item(k.nz);
+  return (k.nr + r - 1) / r;
+}
+
 inline int tc_tiles_of(const axi_case& k, int stage) {
   const int M = (stage % 2 == 0) ? k.nz : k.nr;
   const int N = (stage % 2 == 0) ? k.nr : k.nz;
@@ -1699,6 +1743,15 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
           AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[st], info->n_tc_tiles[st], v.err, s));
         break;
       }
+      if (v.dct64_jobs) {
+        // double: z transform, radial product, inverse z transform, radial product
+        AXI_TRY(axi_dct64::launch(v.dct64_jobs, v.dct_items, info->n_dct_items, true, s));
+        grouped_gemm_kernel<T, 1><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
+        AXI_TRY(axi_dct64::launch(v.dct64_jobs + info->n_cases, v.dct_items, info->n_dct_items,
+                                  false, s));
+        grouped_gemm_kernel<T, 3><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
+        break;
+      }
       grouped_gemm_kernel<T, 0><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
       grouped_gemm_kernel<T, 1><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
       grouped_gemm_kernel<T, 2><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
@@ -1740,6 +1793,9 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
       if (v.dct_jobs && (st == 0 || st == 2)) {
         AXI_TRY(axi_dct::launch(st == 0 ? v.dct_jobs : v.dct_jobs + info->n_cases, v.dct_items,
                                 info->n_dct_items, st == 0, s));
+      } else if (v.dct64_jobs && (st == 0 || st == 2)) {
+        AXI_TRY(axi_dct64::launch(st == 0 ? v.dct64_jobs : v.dct64_jobs + info->n_cases,
+                                  v.dct_items, info->n_dct_items, st == 0, s));
       } else if (v.jobs) {
         AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[st], info->n_tc_tiles[st], v.err, s));
       } else if (st == 0) {
@@ -1851,8 +1907,12 @@ extern "C" int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, int f
     axi::set_error("plan_init: tensor-core products need float32 fields");
     return AXI_ERR_INVALID;
   }
-  if (dct && !tc) {
-    axi::set_error("plan_init: the DCT z transform goes with the tensor-core products");
+  if (dct && !tc && elem_bytes != 8) {
+    axi::set_error("plan_init: the float DCT z transform goes with the tensor-core products");
+    return AXI_ERR_INVALID;
+  }
+  if (refine && elem_bytes != 4) {
+    axi::set_error("plan_init: refinement belongs to the float engine");
     return AXI_ERR_INVALID;
   }
   memset(info, 0, sizeof(*info));
@@ -1884,6 +1944,15 @@ extern "C" int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, int f
       for (int st = 0; st < 4; ++st)
         if (!(dct && (st == 0 || st == 2))) info->n_tc_tiles[st] += tc_tiles_of(k, st);
       if (dct) nd += dct_items_of(k);
+    } else if (dct) {
+      // double engine: DCT z transforms around the SIMT radial products
+      int radix[axi_dct64::MAX_STAGES], ns;
+      if (!k.dct_table || !axi_dct64::plan_radices(k.nz, radix, &ns)) {
+        axi::set_error("plan_init: case %d: no DCT table or nz %d not even with factors 2, 3 "
+                       "(<= %d)", c, k.nz, axi_dct64::ELEMS);
+        return AXI_ERR_INVALID;
+      }
+      nd += dct64_items_of(k);
     }
   }
   info->n_cases = n_cases;
@@ -1990,6 +2059,21 @@ extern "C" int axi_plan_upload(const axi_case* cases, const axi_plan_info* info,
         return AXI_ERR_INVALID;
       }
       axi_tc::order_tiles_by_k(tt, qq, jobs);
+    }
+  }
+  if (!(info->flags & AXI_PLAN_TENSOR_CORES) && (info->flags & AXI_PLAN_DCT_Z)) {
+    // double engine: z transforms as DCTs, items in case order
+    axi_dct64::Job* dj = reinterpret_cast<axi_dct64::Job*>(&buf[po.dct_jobs]);
+    int4* di = reinterpret_cast<int4*>(&buf[po.dct_items]);
+    int q = 0;
+    for (int c = 0; c < n; ++c) {
+      AXI_TRY(build_dct64_jobs(cases[c], dj + c, dj + n + c));
+      const int rows = axi_dct64::rows_per_item(cases[c].nz);
+      for (int r0 = 0; r0 < cases[c].nr; r0 += rows) di[q++] = make_int4(c, r0, 0, 0);
+    }
+    if (q != info->n_dct_items) {
+      axi::set_error("plan_upload: cases changed since plan_init");
+      return AXI_ERR_INVALID;
     }
   }
   cudaStream_t s = axi::as_stream(stream);

@@ -146,10 +146,11 @@ PLAN_DCT_Z = 2
 PLAN_REFINE = 4
 
 
-def dct_ok(nz):
-    """nz the z transform handles as a DCT: even, factors 2 and 3 only, <= 4096."""
+def dct_ok(nz, precision="f32"):
+    """nz the z transform handles as a DCT: even, factors 2 and 3 only, at most
+    4096 (float engine) or 2048 (double engine)."""
     n = int(nz)
-    if n < 2 or n % 2 or n > 4096:
+    if n < 2 or n % 2 or n > (4096 if precision == "f32" else 2048):
         return False
     for f in (2, 3):
         while n % f == 0:
@@ -157,15 +158,16 @@ def dct_ok(nz):
     return n == 1
 
 
-def dct_table(nz):
-    """Float tables of the z transform (layout of axi_case.dct_table):
-    exp(-2 pi i m / nz) as (cos, sin), (cos, sin)(pi k / 2 nz), c_k, 1 / c_k."""
+def dct_table(nz, dtype=np.float32):
+    """Tables of the z transform (layout of axi_case.dct_table), float for the
+    float engine, double for the double engine: exp(-2 pi i m / nz) as
+    (cos, sin), (cos, sin)(pi k / 2 nz), c_k, 1 / c_k."""
     m = np.arange(nz, dtype=np.float64)
     tw = np.stack([np.cos(2 * np.pi * m / nz), -np.sin(2 * np.pi * m / nz)], axis=1)
     rot = np.stack([np.cos(np.pi * m / (2 * nz)), np.sin(np.pi * m / (2 * nz))], axis=1)
     c = np.full(nz, np.sqrt(2.0 / nz))
     c[0] = np.sqrt(1.0 / nz)
-    return np.concatenate([tw.ravel(), rot.ravel(), c, 1.0 / c]).astype(np.float32)
+    return np.concatenate([tw.ravel(), rot.ravel(), c, 1.0 / c]).astype(dtype)
 
 
 class _Bases:
@@ -187,7 +189,8 @@ class _Bases:
             lam_z = (2.0 - 2.0 * np.cos(np.pi * np.arange(nz) / nz)) / (dx * dx)
             inv = 1.0 / (solver.engine.eig_vals_r.reshape(nr, 1) + lam_z.reshape(1, nz))
             self.t["inv_eig"] = torch.tensor(inv, dtype=dtype, device=device)
-            self.dct_table = torch.tensor(dct_table(nz), device=device)
+            self.dct_table = torch.tensor(
+                dct_table(nz, np.float64 if dtype == torch.float64 else np.float32), device=device)
         if tensor_cores:
             h = solver.engine.host
             # operands of the K-major tensor-core form (C = A B^T per stage):
@@ -327,15 +330,19 @@ class RigidEnsemble:
         cases = list(cases)
         if dct is None:
             # z products as DCTs when every case's nz allows it (faster than
-            # the dense tensor-core z products on the 64-case ensemble)
-            dct = tensor_cores and all(dct_ok(c.nz) for c in cases)
-        if dct and not tensor_cores:
-            raise ValueError("the DCT z transform goes with the tensor-core products")
+            # the dense z products: tensor-core ones in the float engine, SIMT
+            # FP64 ones in the double engine); the float engine's DCT feeds
+            # the tensor-core radial products only
+            dct = ((tensor_cores or precision == "f64")
+                   and all(dct_ok(c.nz, precision) for c in cases))
+        if dct and precision == "f32" and not tensor_cores:
+            raise ValueError("the float DCT z transform goes with the tensor-core products")
         if refine is None:
             # each solve one refinement step from the psi of the previous step
-            refine = dct
-        if refine and not dct:
-            raise ValueError("refinement of the solve runs with the DCT z transform")
+            refine = dct and precision == "f32"
+        if refine and (not dct or precision != "f32"):
+            raise ValueError("refinement of the solve runs in the float engine with the DCT "
+                             "z transform")
         self.tensor_cores = tensor_cores
         self.dct = dct
         self.refine = refine
@@ -367,7 +374,7 @@ class RigidEnsemble:
     def _admit(self, case, history_steps=0, initial_vorticity=None):
         if not self._free:
             raise RuntimeError("ensemble is at capacity")
-        if self.dct and not dct_ok(case.nz):
+        if self.dct and not dct_ok(case.nz, self.precision):
             raise ValueError(f"nz = {case.nz} has no DCT plan (even, factors 2 and 3 only); "
                              "build the ensemble with dct=False for such grids")
         m = CaseState(self, case, self._free.pop(), history_steps, initial_vorticity)

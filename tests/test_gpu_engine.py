@@ -31,12 +31,22 @@ def run_oracle(c, steps):
     return st, np.array(hist)
 
 
+@pytest.mark.parametrize("dct", [False, True])
 @pytest.mark.parametrize("nz,nr,steps", [(64, 32, 40), (512, 256, 25)])
-def test_engine_f64_matches_oracle(nz, nr, steps):
+def test_engine_f64_matches_oracle(nz, nr, steps, dct):
+    """The plain FP64 engine against the oracle, with the z products dense (the
+    reference's own form, 1e-12) and as FP64 DCTs. The DCT uses the exact
+    eigenvectors and eigenvalues of the z operator; the reference uses the
+    ones LAPACK computes, whose low modes carry errors of about
+    eps ||A|| / gap (1e-12 relative on one 512 x 256 solve against an exact
+    DCT-basis solve in numpy, both with discrete-operator residuals of 2e-11):
+    over the steps the two differ by up to a few 1e-12, so the DCT variant is
+    held to 2e-11."""
     from pyaxisymflow_gb300.engine import RigidBodyCase, RigidEnsemble
     c = RigidBodyCase(nz=nz, nr=nr, dx=2.0 / nz, r_sphere=max(0.0625, 4 * 2.0 / nz))
     ref, hist = run_oracle(c, steps)
-    e = RigidEnsemble([c], precision="f64", history_steps=steps)
+    e = RigidEnsemble([c], precision="f64", history_steps=steps, dct=dct)
+    assert e.dct == dct
     e.step(steps)
     torch.cuda.synchronize()
     assert e.status()[0] == 0
@@ -45,7 +55,7 @@ def test_engine_f64_matches_oracle(nz, nr, steps):
                                ("u_z", e.fields[0]["u_z"], ref.u_z),
                                ("u_r", e.fields[0]["u_r"], ref.u_r)):
         err = rel_l2(mine.cpu().numpy(), theirs)
-        assert err < 1e-12, (name, err)
+        assert err < (2e-11 if dct else 1e-12), (name, err)
     h = e.history[0].cpu().numpy()
     np.testing.assert_allclose(h[:, 0], hist[:, 0], rtol=1e-12)
     np.testing.assert_allclose(h[:, 1], hist[:, 1], rtol=1e-10, atol=1e-12)
