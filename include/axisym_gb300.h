@@ -504,6 +504,32 @@ typedef struct axi_case {
   void* psi_lo;
 } axi_case;
 
+/* Launch choices of a plan that change the scheduling of the work, never its
+ * results: every choice gives bit-identical fields (the work units, their
+ * arithmetic and every reduction order are fixed; only which block takes which
+ * unit, and when, changes). 0 selects the built-in default. Set them in
+ * axi_plan_info.tune after axi_plan_init and before axi_plan_upload (the
+ * orders are laid out by the upload); the launch choices apply to every
+ * later step. No counterpart in the reference (its kernels are pystencils /
+ * numpy calls); pyaxisymflow_gb300.autotune picks them per grid-size mix by
+ * measurement. */
+typedef struct axi_tuning {
+  /* resident blocks per SM of vel_max, penalise and advect_diffuse (0: all
+   * that fit; penalise and advect_diffuse then take one tile per block) */
+  int32_t stencil_blocks_per_sm[3];
+  /* L2 prefetch distance of the stencil tiles and the DCT items, in resident
+   * waves (0: one wave; -1: no prefetch) */
+  int32_t prefetch_waves;
+  /* persistent CTAs of the tensor-core products, percent of the SMs (0: 100) */
+  int32_t tc_ctas_percent;
+  /* tensor-core tile order: 0 longest main loop (K) first, 1 case order */
+  int32_t tc_tile_order;
+  /* DCT item order: 0 case order with the shortest rows last, 1 case order,
+   * 2 longest rows first */
+  int32_t dct_item_order;
+  int32_t reserved;
+} axi_tuning;
+
 /* Launch plan of a set of cases: tile tables in device memory. */
 typedef struct axi_plan_info {
   int32_t n_cases;
@@ -514,6 +540,7 @@ typedef struct axi_plan_info {
   int32_t flags;           /* AXI_PLAN_* */
   int32_t n_tc_tiles[4];   /* tensor-core tiles per spectral stage */
   int32_t n_dct_items;     /* row groups of the z transforms (AXI_PLAN_DCT_Z) */
+  axi_tuning tune;         /* launch choices (zero: defaults) */
 } axi_plan_info;
 
 /* AXI_PLAN_DCT_Z: the z-direction products run as orthonormal DCT-II /

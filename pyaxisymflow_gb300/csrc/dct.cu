@@ -729,7 +729,7 @@ bool plan_radices(int N, int* radix, int* nstages) {
 }
 
 int launch(const DctJob* jobs_dev, const int4* items_dev, int n_items, bool forward,
-           cudaStream_t s) {
+           cudaStream_t s, int prefetch_waves) {
   static std::once_flag once;
   static cudaError_t attr = cudaSuccess;
   std::call_once(once, [] {
@@ -749,8 +749,11 @@ int launch(const DctJob* jobs_dev, const int4* items_dev, int n_items, bool forw
                  ? b
                  : 1;
   }
-  dct_rows_kernel<<<n_items, THREADS, SMEM_BYTES, s>>>(jobs_dev, items_dev, n_items,
-                                                       per_sm * axi::sm_count(), forward ? 1 : 0);
+  // prefetch distance: `prefetch_waves` resident waves ahead (n_items: none)
+  const int wave = per_sm * axi::sm_count();
+  const int ahead = prefetch_waves < 0 ? n_items : wave * (prefetch_waves > 0 ? prefetch_waves : 1);
+  dct_rows_kernel<<<n_items, THREADS, SMEM_BYTES, s>>>(jobs_dev, items_dev, n_items, ahead,
+                                                       forward ? 1 : 0);
   return axi::launch_status("dct_rows");
 }
 

@@ -98,7 +98,8 @@ bool plan_radices(int N, int* radix, int* nstages);
 
 // Host: launch over `n_items` work items (job, row0, -, -); forward = DCT-II
 // (E_z^T x), else DCT-III (E_z y).
+// `prefetch_waves`: L2 prefetch distance in resident waves (0: one, -1: none).
 int launch(const DctJob* jobs_dev, const int4* items_dev, int n_items, bool forward,
-           cudaStream_t s);
+           cudaStream_t s, int prefetch_waves = 0);
 
 }  // namespace axi_dct

@@ -20,6 +20,8 @@ extern "C" int axi_fd_transform_f64(double* out, int ld_out, const double* in, i
   axi::clear_error();
   const char* what = "fd_transform";
   AXI_TRY(axi::check_grid(what, nr, nz, 1, 1));
+  AXI_TRY(axi::check_ptr(what, out, "out"));
+  AXI_TRY(axi::check_ptr(what, in, "in"));
   AXI_TRY(axi::check_ptr(what, work, "work"));
   AXI_TRY(axi::check_ptr(what, Er_inv_w, "Er_inv_w"));
   AXI_TRY(axi::check_ptr(what, EzinvT, "EzinvT"));
@@ -49,18 +51,42 @@ namespace {
 constexpr long long kFdStaticCells = 1LL << 19;  // per product: 512 x 1024 cells
 static __device__ __align__(256) double g_fd_static_scratch[2 * kFdStaticCells];
 
-// Device address of the array on each device, looked up once per device with
-// that device current (the host-side symbol is only a stand-in).
+// The driver's cuCtxGetCurrent, taken through the runtime (no -lcuda link).
+using CtxGetCurrentFn = int (*)(void**);
+CtxGetCurrentFn ctx_get_current_fn() {
+  static CtxGetCurrentFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrentFn>(p);
+  });
+  return fn;
+}
+
+// Device address of the array on each device, looked up with that device
+// current (the host-side symbol is only a stand-in). It is cached per device
+// together with the context it was looked up in: after a device reset the
+// primary context is a new one, and the address is looked up again.
 double* fd_static_scratch(const char* what) {
   static std::mutex mu;
   static double* addr[128] = {nullptr};
+  static void* ctx_of[128] = {nullptr};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) {
     axi::set_error("%s: no current CUDA device", what);
     return nullptr;
   }
+  const CtxGetCurrentFn get = ctx_get_current_fn();
+  auto current = [get]() -> void* {
+    void* c = nullptr;
+    return (get && get(&c) == 0) ? c : nullptr;
+  };
   std::lock_guard<std::mutex> lock(mu);
-  if (!addr[dev]) {
+  if (!addr[dev] || ctx_of[dev] != current()) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_fd_static_scratch);
     if (e != cudaSuccess || !p) {
@@ -68,6 +94,7 @@ double* fd_static_scratch(const char* what) {
       return nullptr;
     }
     addr[dev] = static_cast<double*>(p);
+    ctx_of[dev] = current();  // the context the lookup made current
   }
   return addr[dev];
 }
@@ -88,6 +115,8 @@ extern "C" int axi_fd_transform_static_f64(double* out, int ld_out, const double
                    what, nr, nz, (long long)nr * nz, kFdStaticCells);
     return AXI_ERR_INVALID;
   }
+  AXI_TRY(axi::check_ptr(what, out, "out"));
+  AXI_TRY(axi::check_ptr(what, in, "in"));
   AXI_TRY(axi::check_ptr(what, Er_inv_w, "Er_inv_w"));
   AXI_TRY(axi::check_ptr(what, EzinvT, "EzinvT"));
   AXI_TRY(axi::check_ptr(what, inv_eig, "inv_eig"));

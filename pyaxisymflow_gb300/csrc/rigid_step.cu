@@ -27,7 +27,9 @@
 // per-step scalars are computed once per case. FP64 remains in the time
 // step, the simulated time, the drag sums across warps and tiles and the
 // body ODE.
+#include <algorithm>
 #include <type_traits>
+#include <vector>
 
 #include "axi_common.cuh"
 #include "dct.cuh"
@@ -1707,16 +1709,31 @@ struct StencilGrid {
     }
     return n[slot];
   }
-  // blocks of the phase resident on the GPU at once
-  static int resident(int phase, bool pair = false) {
-    return per_sm(phase, pair) * axi::sm_count();
+  // cap on resident blocks per SM chosen by the plan's tuning (0: none)
+  static int cap(const axi_plan_info* info, int phase) {
+    const int q = phase == PH_VEL_MAX ? 0 : phase == PH_PENALISE ? 1 : 2;
+    return info->tune.stencil_blocks_per_sm[q];
   }
-  static int get(int phase, int n_tiles, bool pair = false) {
-    // ring depth 1: one block per tile
-    if ((phase == PH_PENALISE && PN_NBUF == 1) || (phase == PH_ADVECT_DIFFUSE && AD_NBUF == 1))
+  // blocks of the phase resident on the GPU at once
+  static int resident(const axi_plan_info* info, int phase, bool pair = false) {
+    int b = per_sm(phase, pair);
+    const int c = cap(info, phase);
+    if (c > 0 && c < b) b = c;
+    return b * axi::sm_count();
+  }
+  static int get(const axi_plan_info* info, int phase, int n_tiles, bool pair = false) {
+    // ring depth 1 and no cap: one block per tile; otherwise persistent blocks
+    if (cap(info, phase) <= 0 &&
+        ((phase == PH_PENALISE && PN_NBUF == 1) || (phase == PH_ADVECT_DIFFUSE && AD_NBUF == 1)))
       return n_tiles;
-    const int g = per_sm(phase, pair) * axi::sm_count();
+    const int g = resident(info, phase, pair);
     return n_tiles < g ? n_tiles : g;
+  }
+  // L2 prefetch distance in tiles (the plan's waves of resident blocks)
+  static int ahead(const axi_plan_info* info, int phase, int n_tiles, bool pair = false) {
+    const int w = info->tune.prefetch_waves;
+    if (w < 0) return n_tiles;
+    return resident(info, phase, pair) * (w > 0 ? w : 1);
   }
 };
 
@@ -1731,16 +1748,20 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
     case PH_TRANSFORM:
       if (v.dct_jobs) {
         // z transform, radial product, inverse z transform, radial product
-        AXI_TRY(axi_dct::launch(v.dct_jobs, v.dct_items, info->n_dct_items, true, s));
-        AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[1], info->n_tc_tiles[1], v.err, s));
+        AXI_TRY(axi_dct::launch(v.dct_jobs, v.dct_items, info->n_dct_items, true, s,
+                                info->tune.prefetch_waves));
+        AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[1], info->n_tc_tiles[1], v.err, s,
+                               info->tune.tc_ctas_percent));
         AXI_TRY(axi_dct::launch(v.dct_jobs + info->n_cases, v.dct_items, info->n_dct_items,
-                                false, s));
-        AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[3], info->n_tc_tiles[3], v.err, s));
+                                false, s, info->tune.prefetch_waves));
+        AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[3], info->n_tc_tiles[3], v.err, s,
+                               info->tune.tc_ctas_percent));
         break;
       }
       if (v.jobs) {
         for (int st = 0; st < 4; ++st)
-          AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[st], info->n_tc_tiles[st], v.err, s));
+          AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[st], info->n_tc_tiles[st], v.err, s,
+                                 info->tune.tc_ctas_percent));
         break;
       }
       if (v.dct64_jobs) {
@@ -1759,7 +1780,7 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
       break;
     case PH_VEL_MAX:
       AXI_TRY(stencil_attrs<T>());
-      vel_max_kernel<T><<<StencilGrid<T>::get(PH_VEL_MAX, nt), NT, vel_max_smem<T>(), s>>>(
+      vel_max_kernel<T><<<StencilGrid<T>::get(info, PH_VEL_MAX, nt), NT, vel_max_smem<T>(), s>>>(
           v.cases, v.stencil, nt, v.maps, v.err, info->n_cases,
           reinterpret_cast<unsigned int*>(v.err + 1));
       break;
@@ -1769,21 +1790,23 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
         if (info->flags & AXI_PLAN_REFINE) {
           // psi read as psi + psi_lo
           penalise_kernel<T, true>
-              <<<StencilGrid<T>::get(PH_PENALISE, nt), NT, penalise_smem<T, true>(), s>>>(
-                  v.cases, v.stencil, nt, v.maps, v.err,
-                  StencilGrid<T>::resident(PH_PENALISE, true));
+              <<<StencilGrid<T>::get(info, PH_PENALISE, nt, true), NT, penalise_smem<T, true>(),
+                 s>>>(v.cases, v.stencil, nt, v.maps, v.err,
+                      StencilGrid<T>::ahead(info, PH_PENALISE, nt, true));
           break;
         }
       }
       penalise_kernel<T, false>
-          <<<StencilGrid<T>::get(PH_PENALISE, nt), NT, penalise_smem<T, false>(), s>>>(
-              v.cases, v.stencil, nt, v.maps, v.err, StencilGrid<T>::resident(PH_PENALISE));
+          <<<StencilGrid<T>::get(info, PH_PENALISE, nt), NT, penalise_smem<T, false>(), s>>>(
+              v.cases, v.stencil, nt, v.maps, v.err,
+              StencilGrid<T>::ahead(info, PH_PENALISE, nt));
       break;
     case PH_ADVECT_DIFFUSE:
       AXI_TRY(stencil_attrs<T>());
       advect_diffuse_kernel<T>
-          <<<StencilGrid<T>::get(PH_ADVECT_DIFFUSE, nt), NT, advect_diffuse_smem<T>(), s>>>(
-              v.cases, v.stencil, nt, v.maps, v.err, StencilGrid<T>::resident(PH_ADVECT_DIFFUSE));
+          <<<StencilGrid<T>::get(info, PH_ADVECT_DIFFUSE, nt), NT, advect_diffuse_smem<T>(), s>>>(
+              v.cases, v.stencil, nt, v.maps, v.err,
+              StencilGrid<T>::ahead(info, PH_ADVECT_DIFFUSE, nt));
       break;
     case PH_TRANSFORM_PART0:
     case PH_TRANSFORM_PART0 + 1:
@@ -1792,12 +1815,13 @@ int run_phase(int phase, const axi_plan_info* info, const PlanView& v, cudaStrea
       const int st = phase - PH_TRANSFORM_PART0;
       if (v.dct_jobs && (st == 0 || st == 2)) {
         AXI_TRY(axi_dct::launch(st == 0 ? v.dct_jobs : v.dct_jobs + info->n_cases, v.dct_items,
-                                info->n_dct_items, st == 0, s));
+                                info->n_dct_items, st == 0, s, info->tune.prefetch_waves));
       } else if (v.dct64_jobs && (st == 0 || st == 2)) {
         AXI_TRY(axi_dct64::launch(st == 0 ? v.dct64_jobs : v.dct64_jobs + info->n_cases,
                                   v.dct_items, info->n_dct_items, st == 0, s));
       } else if (v.jobs) {
-        AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[st], info->n_tc_tiles[st], v.err, s));
+        AXI_TRY(axi_tc::launch(v.jobs, v.tc_tiles[st], info->n_tc_tiles[st], v.err, s,
+                                 info->tune.tc_ctas_percent));
       } else if (st == 0) {
         grouped_gemm_kernel<T, 0><<<ng, gemm_threads<T>(), 0, s>>>(v.cases, v.gemm);
       } else if (st == 1) {
@@ -1915,7 +1939,9 @@ extern "C" int axi_plan_init(axi_case* cases, int n_cases, int elem_bytes, int f
     axi::set_error("plan_init: refinement belongs to the float engine");
     return AXI_ERR_INVALID;
   }
+  const axi_tuning tune = info->tune;  // the caller's launch choices survive re-planning
   memset(info, 0, sizeof(*info));
+  info->tune = tune;
   int nt = 0, ng = 0, nd = 0;
   for (int c = 0; c < n_cases; ++c) {
     const axi_case& k = cases[c];
@@ -2028,13 +2054,20 @@ extern "C" int axi_plan_upload(const axi_case* cases, const axi_plan_info* info,
         AXI_TRY(build_dct_jobs(cases[c], dj + c, dj + n + c, refine));
         nz_min = cases[c].nz < nz_min ? cases[c].nz : nz_min;
       }
-      // items in case order, the shortest rows' items last: the last wave of
-      // blocks then holds the quickest items (10 us less per pair of
-      // transforms on the 64-case ensemble; ordering every item by length was
-      // slower, the mix of lengths balancing the SMs)
+      // item order (tuning): 0 case order with the shortest rows' items
+      // last (the last wave of blocks then holds the quickest items: 10 us less
+      // per pair of transforms on the 64-case ensemble), 1 plain case order,
+      // 2 longest rows first
+      const int order = info->tune.dct_item_order;
+      std::vector<int> by_case(n);
+      for (int c = 0; c < n; ++c) by_case[c] = c;
+      if (order == 2)
+        std::stable_sort(by_case.begin(), by_case.end(),
+                         [cases](int a, int b) { return cases[a].nz > cases[b].nz; });
       for (int pass = 0; pass < 2; ++pass)
-        for (int c = 0; c < n; ++c) {
-          if ((cases[c].nz == nz_min) != (pass == 1)) continue;
+        for (int c : by_case) {
+          if (order == 0 && (cases[c].nz == nz_min) != (pass == 1)) continue;
+          if (order != 0 && pass == 1) continue;
           const int rows = axi_dct::rows_for(cases[c].nz);
           for (int r0 = 0; r0 < cases[c].nr; r0 += rows) di[q++] = make_int4(c, r0, 0, 0);
         }
@@ -2058,7 +2091,9 @@ extern "C" int axi_plan_upload(const axi_case* cases, const axi_plan_info* info,
         axi::set_error("plan_upload: cases changed since plan_init");
         return AXI_ERR_INVALID;
       }
-      axi_tc::order_tiles_by_k(tt, qq, jobs);
+      // tile order (tuning): 0 longest main loop first, 1 case order (the
+      // k-block counts are filled in either way)
+      axi_tc::order_tiles_by_k(tt, qq, jobs, info->tune.tc_tile_order == 0);
     }
   }
   if (!(info->flags & AXI_PLAN_TENSOR_CORES) && (info->flags & AXI_PLAN_DCT_Z)) {

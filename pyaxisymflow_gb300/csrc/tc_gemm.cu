@@ -407,14 +407,15 @@ bool encode_output(TcJob* job) {
   return true;
 }
 
-void order_tiles_by_k(int4* tiles, int n, const TcJob* jobs) {
+void order_tiles_by_k(int4* tiles, int n, const TcJob* jobs, bool sort) {
   for (int i = 0; i < n; ++i) tiles[i].w = (jobs[tiles[i].x].K + BKF - 1) / BKF;
+  if (!sort) return;
   std::stable_sort(tiles, tiles + n,
                    [jobs](const int4& a, const int4& b) { return jobs[a.x].K > jobs[b.x].K; });
 }
 
 int launch(const TcJob* jobs_dev, const int4* tiles_dev, int n_tiles, int* err_dev,
-           cudaStream_t s) {
+           cudaStream_t s, int ctas_percent) {
   static std::once_flag once;
   static cudaError_t attr_status = cudaSuccess;
   std::call_once(once, [] {
@@ -426,7 +427,9 @@ int launch(const TcJob* jobs_dev, const int4* tiles_dev, int n_tiles, int* err_d
     return AXI_ERR_CUDA;
   }
   if (n_tiles <= 0) return AXI_OK;
-  const int grid = n_tiles < axi::sm_count() ? n_tiles : axi::sm_count();
+  int ctas = axi::sm_count();
+  if (ctas_percent > 0 && ctas_percent < 100) ctas = ctas * ctas_percent / 100 > 0 ? ctas * ctas_percent / 100 : 1;
+  const int grid = n_tiles < ctas ? n_tiles : ctas;
   tf32x3_gemm_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(jobs_dev, tiles_dev, n_tiles, err_dev);
   return axi::launch_status("tf32x3_gemm");
 }

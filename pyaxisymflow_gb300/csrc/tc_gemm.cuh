@@ -106,13 +106,14 @@ bool encode_output(TcJob* job);
 
 // Host: complete a tile table (job, m0, n0, -) with each tile's k-block
 // count (w = ceil(K / BKF), which the kernel reads instead of the job) and
-// order it longest main loop (largest K) first, stable within equal K. The
-// persistent CTAs take tiles with a fixed stride, so the long tiles are
-// spread over all SMs before the short ones.
-void order_tiles_by_k(int4* tiles, int n, const TcJob* jobs);
+// (with `sort`) order it longest main loop (largest K) first, stable within
+// equal K. The persistent CTAs take tiles with a fixed stride, so the long
+// tiles are spread over all SMs before the short ones.
+void order_tiles_by_k(int4* tiles, int n, const TcJob* jobs, bool sort = true);
 
-// Host: launch the grouped kernel over `n_tiles` (job, m0, n0, k-blocks) tiles.
+// Host: launch the grouped kernel over `n_tiles` (job, m0, n0, k-blocks) tiles
+// with `ctas_percent` of the SMs as persistent CTAs (0: all of them).
 int launch(const TcJob* jobs_dev, const int4* tiles_dev, int n_tiles, int* err_dev,
-           cudaStream_t s);
+           cudaStream_t s, int ctas_percent = 0);
 
 }  // namespace axi_tc

@@ -133,12 +133,38 @@ def kill_coefficients(z, r, width, dx):
     return np.concatenate([zs, ze, rr])
 
 
+class AxiTuning(ctypes.Structure):
+    """Mirror of ``axi_tuning`` in include/axisym_gb300.h: launch choices that
+    change scheduling only (bit-identical results); 0 = default."""
+    _fields_ = [("stencil_blocks_per_sm", ctypes.c_int32 * 3),
+                ("prefetch_waves", ctypes.c_int32), ("tc_ctas_percent", ctypes.c_int32),
+                ("tc_tile_order", ctypes.c_int32), ("dct_item_order", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+# names of the launch choices (keys of RigidEnsemble.tuning)
+TUNING_KEYS = ("vel_max_blocks", "penalise_blocks", "advect_blocks", "prefetch_waves",
+               "tc_ctas_percent", "tc_tile_order", "dct_item_order")
+
+
+def fill_tuning(tune, choices):
+    """Writes a dict of launch choices (TUNING_KEYS) into an AxiTuning."""
+    unknown = set(choices) - set(TUNING_KEYS)
+    if unknown:
+        raise ValueError(f"unknown launch choices {sorted(unknown)}")
+    for q, k in enumerate(("vel_max_blocks", "penalise_blocks", "advect_blocks")):
+        tune.stencil_blocks_per_sm[q] = int(choices.get(k, 0))
+    for k in ("prefetch_waves", "tc_ctas_percent", "tc_tile_order", "dct_item_order"):
+        setattr(tune, k, int(choices.get(k, 0)))
+
+
 class AxiPlanInfo(ctypes.Structure):
     """Mirror of ``axi_plan_info`` in include/axisym_gb300.h."""
     _fields_ = [("n_cases", ctypes.c_int32), ("n_stencil_tiles", ctypes.c_int32),
                 ("n_gemm_tiles", ctypes.c_int32), ("elem_bytes", ctypes.c_int32),
                 ("bytes", ctypes.c_int64), ("flags", ctypes.c_int32),
-                ("n_tc_tiles", ctypes.c_int32 * 4), ("n_dct_items", ctypes.c_int32)]
+                ("n_tc_tiles", ctypes.c_int32 * 4), ("n_dct_items", ctypes.c_int32),
+                ("tune", AxiTuning)]
 
 
 PLAN_TENSOR_CORES = 1
@@ -356,6 +382,7 @@ class RigidEnsemble:
         self._bases = {}
         self.members = []
         self.graph = None
+        self.tuning = {}
         lib = N.lib()
         self._step_fn = getattr(lib, f"axi_rigid_step_{precision}")
         self._phase_fn = getattr(lib, f"axi_rigid_phase_{precision}")
@@ -405,6 +432,7 @@ class RigidEnsemble:
         for k, m in enumerate(self.members):
             self.structs[k] = m.struct
         self.info = AxiPlanInfo()
+        fill_tuning(self.info.tune, self.tuning)
         if n == 0:
             self.plan = None
             self.n_tiles = 0
@@ -421,6 +449,15 @@ class RigidEnsemble:
                                     ctypes.c_void_p(self.plan.data_ptr()),
                                     ctypes.c_void_p(torch.cuda.current_stream(
                                         self.device).cuda_stream)), "plan_upload")
+
+    def set_tuning(self, choices):
+        """Use the launch choices `choices` (a dict over TUNING_KEYS; missing
+        keys take the default) from the next step on. They change how the
+        work is scheduled, never the results. Re-plans (a captured graph must
+        be captured again)."""
+        fill_tuning(AxiTuning(), choices)  # validates the keys
+        self.tuning = dict(choices)
+        self._replan()
 
     def add_case(self, case, history_steps=0, initial_vorticity=None):
         """Admit a case between steps; returns its CaseState."""

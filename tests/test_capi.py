@@ -75,3 +75,21 @@ def test_new_entry_points_reject_bad_arguments_before_any_launch():
                                               null)
     assert st == N.AXI_ERR_INVALID and b"particles_to_mesh" in lib.axi_last_error()
     assert lib.axi_p2m_mp4_work_bytes(0, 8) == 0
+
+
+def test_spectral_transforms_reject_null_fields():
+    """Both FP64 spectral transform entry points (with caller scratch and with
+    the library's static scratch) reject null input and output pointers on the
+    host, before any launch."""
+    import ctypes as c
+
+    from pyaxisymflow_gb300 import _native as N
+    lib = N.lib()
+    fake, null = c.c_void_p(4096), c.c_void_p(None)
+    for out, inp in ((null, fake), (fake, null)):
+        st = lib.axi_fd_transform_f64(out, 8, inp, 8, fake, fake, fake, fake, fake, fake, 8, 8,
+                                      null)
+        assert st == N.AXI_ERR_INVALID and b"fd_transform" in lib.axi_last_error()
+        st = lib.axi_fd_transform_static_f64(out, 8, inp, 8, fake, fake, fake, fake, fake, 8, 8,
+                                             null)
+        assert st == N.AXI_ERR_INVALID and b"fd_transform_static" in lib.axi_last_error()
