@@ -477,7 +477,7 @@ typedef struct axi_case {
   const void* EzinvT;    /* (nz, nz) */
   const void* EzT;       /* (nz, nz) */
   const void* inv_eig;   /* (nr, nz) */
-  void* gemm_work;       /* 2 nr nz */
+  void* gemm_work;       /* 2 nr nz: spectral-solve scratch, then the penalised omega */
   double* state;         /* AXI_ST_WORDS doubles */
   double* partials;      /* one double per stencil tile of the case */
   double* history;       /* optional: 2 doubles (dt, Cd) per step, or NULL */
@@ -585,7 +585,9 @@ int axi_rigid_step_f32(const axi_plan_info* info, const void* plan_dev, int n_st
                        void* stream);
 /* One phase of a step (0 kill, 1 spectral transform, 2 velocity max and dt,
  * 3 penalisation and drag, 4 advection and both diffusion stages); running
- * phases 0..4 in order equals one step. Phases 5..8 are the four launches of
+ * phases 0..4 in order equals one step. Phase 3 leaves the penalised
+ * vorticity in the first nr x nz elements of gemm_work (omega unchanged);
+ * phase 4 advances it into omega. Phases 5..8 are the four launches of
  * phase 1 one at a time (z product or DCT, radial product, z product or
  * inverse DCT, radial product). Lets a caller time each kernel. */
 int axi_rigid_phase_f64(const axi_plan_info* info, const void* plan_dev, int phase,

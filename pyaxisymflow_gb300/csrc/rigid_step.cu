@@ -14,10 +14,12 @@
 //   transform    four grouped dense products (the spectral Poisson solve)
 //   vel_max      persistent, per tile: max(|u_z| + |u_r|) into the case
 //   step_dt      one thread per case: dt and the dt-dependent constants
-//   penalise     per tile: velocity + Brinkman + curl(u_pen - u) into omega,
-//                drag partials; the last tile of a case finalises the drag
+//   penalise     per tile: velocity + Brinkman + omega + curl(u_pen - u)
+//                into the staging half of the work buffer, drag partials;
+//                the last tile of a case finalises the drag
 //   advect_diffuse per tile: ENO3 advection (axis mirror) and both RK2
-//                stages in shared memory (halo 4); advances the time
+//                stages in shared memory (halo 4) from the staged omega
+//                into omega; advances the time
 //                (sedimenting cases: mask rebuild, drag, body ODE)
 // The stencil kernels receive their halo boxes by TMA.
 //
@@ -630,7 +632,12 @@ __global__ void __launch_bounds__(NT, penalise_min_blocks<T, PAIR>()) penalise_k
     T ubody_lo = T(0);
     if constexpr (sizeof(T) == 4) ubody_lo = scalar<T>(k, SF_UBODY_LO);
     const T inv2dx = scalar<T>(k, SF_INV2DX);
-    T* w = F<T>(k.omega);
+    const T* w = CF<T>(k.omega);
+    // the penalised vorticity goes to the first nr x nz elements of the work
+    // buffer (free between the spectral solve and the next step's solve):
+    // advect_diffuse reads its halo rows from there while it writes omega, so
+    // no tile reads a neighbour's already-advanced rows
+    T* const ws = F<T>(k.gemm_work);
     const T lamdt = scalar<T>(k, SF_LAMDT);
     // per-row factors of the tile + halo 1 (rows i0 - 1 .. i0 + TY)
     if (threadIdx.x < PN_SH) {
@@ -774,16 +781,20 @@ __global__ void __launch_bounds__(NT, penalise_min_blocks<T, PAIR>()) penalise_k
     }
     __syncthreads();
     {
-      const bool jint = gjm >= 1 && gjm < nz - 1;
+      const bool jin = gjm < nz, jint = gjm >= 1 && gjm < nz - 1;
       int d = (p0c + 1) * PN_SW + (qm + 1);
       T zs = duz[d - PN_SW], zc = duz[d];
 #pragma unroll
       for (int m = 0; m < RC; ++m, d += PN_SW) {
         const T zn = duz[d + PN_SW];
         const int gi = i0 + p0c + m;
-        if (jint && gi >= 1 && gi < nr - 1) {
-          const T pw = (dur[d + 1] - dur[d - 1]) * inv2dx - (zn - zs) * inv2dx;
-          w[gi * nz + gjm] = wown[m] + pw;
+        if (jin && gi < nr) {
+          T v = wown[m];
+          if (jint && gi >= 1 && gi < nr - 1) {
+            const T pw = (dur[d + 1] - dur[d - 1]) * inv2dx - (zn - zs) * inv2dx;
+            v = wown[m] + pw;
+          }
+          ws[gi * nz + gjm] = v;
         }
         zs = zc;
         zc = zn;
@@ -900,10 +911,13 @@ __device__ __forceinline__ float sphere_mask_cells(int i, int j, float s_hi, flo
 // advect_diffuse: ENO3 advection (kernels/advect_vorticity_via_eno3.py:28-42,
 // pyst_kernels/advection_flux.py:9-163, advection_timestep.py:37-54) followed
 // by both RK2 diffusion stages (kernels/diffusion_RK2.py:9-44), fused: the
-// boxes of omega, u_z, u_r (halo 4) arrive by TMA; the block advects the
-// tile plus a halo of 2, applies stage 1 on the tile plus a halo of 1 and
-// stage 2 on the tile, all in shared memory, so omega is read and written
-// once per step. Rows below the axis are the mirror images of rows 0..3
+// boxes of the penalised omega (staged in the work buffer by penalise), u_z
+// and u_r (halo 4) arrive by TMA; the block advects the tile plus a halo of
+// 2, applies stage 1 on the tile plus a halo of 1 and stage 2 on the tile,
+// all in shared memory, and writes omega: each value is read and written once
+// per step, and the halo rows a tile reads are never the ones another tile
+// has already advanced (blocks of a later wave start after earlier tiles
+// were written). Rows below the axis are the mirror images of rows 0..3
 // (omega and u_r odd, u_z even). Sedimenting cases also rebuild the body mask
 // here and close the step (falling_rigid_sphere.py:156-181).
 // ---------------------------------------------------------------------------
@@ -2033,7 +2047,8 @@ extern "C" int axi_plan_upload(const axi_case* cases, const axi_plan_info* info,
     CUtensorMap* m = maps + MAP_COUNT * c;
     AXI_TRY(axi_tma::encode_box(m + MAP_PSI, k.psi, eb, k.nr, k.nz, PSI_ROWS, BOXW));
     AXI_TRY(axi_tma::encode_box(m + MAP_CHI, k.chi, eb, k.nr, k.nz, PSI_ROWS, BOXW));
-    AXI_TRY(axi_tma::encode_box(m + MAP_W, k.omega, eb, k.nr, k.nz, ADV_ROWS, BOXW));
+    // penalised omega, staged by penalise in the first nr x nz elements of gemm_work
+    AXI_TRY(axi_tma::encode_box(m + MAP_W, k.gemm_work, eb, k.nr, k.nz, ADV_ROWS, BOXW));
     AXI_TRY(axi_tma::encode_box(m + MAP_UZ, k.u_z, eb, k.nr, k.nz, ADV_ROWS, BOXW));
     AXI_TRY(axi_tma::encode_box(m + MAP_UR, k.u_r, eb, k.nr, k.nz, ADV_ROWS, BOXW));
     if (info->flags & AXI_PLAN_REFINE)
