@@ -166,53 +166,85 @@ def max_over_ranks(world, x):
     return float(t.item())
 
 
-class OracleRuns:
-    """The oracle (numpy FP64, the reference's CPU algorithm) set up for
-    `cases`; one round advances every case one timestep on the host."""
-
-    def __init__(self, cases):
-        from oracle import kernels as K
-        from oracle import simulation as sim
-        self.K = K
-        self.runs = []
-        for c in cases:
-            if c.sediment:
-                oc = sim.SedimentingCase(nz=c.nz, nr=c.nr, dx=c.dx, z_cm=c.z_cm,
-                                         r_sphere=c.r_sphere, rho_f=c.rho_f, rho_s=c.rho_s,
-                                         nu=c.nu, lam=c.lam, cfl=c.cfl,
-                                         kill_width=c.kill_width, gravity=c.gravity)
-                w0 = c.noise * np.random.default_rng(c.seed).standard_normal((c.nr, c.nz))
-                st, coords = sim.sedimenting_init(oc, K, vorticity=w0)
-                step = sim.sedimenting_step
-            else:
-                oc = sim.RigidSphereCase(nz=c.nz, nr=c.nr, dx=c.dx, z_cm=c.z_cm,
-                                         r_sphere=c.r_sphere, U0=c.U0, Re=c.Re, lam=c.lam,
-                                         cfl=c.cfl, kill_width=c.kill_width, ramp=c.ramp,
-                                         noise=c.noise, seed=c.seed)
-                st, coords = sim.rigid_sphere_init(oc, K)
-                step = sim.rigid_sphere_step
-            solver = K.FastDiagonalisationStokesSolver(oc.nr, oc.nz, oc.dx)
-            adv = K.gen_advect_vorticity_via_eno3(oc.dx, oc.nr, oc.nz)
-            self.runs.append((oc, st, coords, solver, adv, step))
-        self.cells = sum(r[0].nr * r[0].nz for r in self.runs)
-
-    def round(self):
-        """One timestep of every case; returns the wall time in seconds."""
-        t0 = time.perf_counter()
-        for oc, st, coords, solver, adv, step in self.runs:
-            step(oc, st, coords, solver, adv, self.K)
-        return time.perf_counter() - t0
+def case_params(cases):
+    """The fields of each case that the oracle needs, as plain values."""
+    return [dict(nz=c.nz, nr=c.nr, dx=c.dx, z_cm=c.z_cm, r_sphere=c.r_sphere, U0=c.U0, Re=c.Re,
+                 nu=c.nu, lam=c.lam, cfl=c.cfl, kill_width=c.kill_width, ramp=c.ramp,
+                 noise=c.noise, seed=c.seed, sediment=c.sediment, rho_f=c.rho_f,
+                 rho_s=c.rho_s, gravity=c.gravity) for c in cases]
 
 
-def cpu_oracle_rate(cases, steps, min_seconds=0.0):
-    """Oracle cell-updates/s on the host for `cases`: `steps` rounds, continued
-    until at least `min_seconds` of stepping have passed."""
-    runs = OracleRuns(cases)
-    secs, rounds = 0.0, 0
-    while rounds < steps or secs < min_seconds:
-        secs += runs.round()
-        rounds += 1
-    return runs.cells * rounds / secs, secs, rounds
+def host_cores():
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+
+
+def cpu_run(cases, threads, seconds, warmup=1, max_rounds=1000, kind="cport", dump=None):
+    """The oracle timed on the host (oracle/cpu_baseline.py) in a child
+    process, so that its BLAS and OpenMP thread counts are set before numpy
+    loads; one round advances every case one timestep. Returns the child's
+    JSON record."""
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "cases.json")
+        with open(path, "w") as f:
+            json.dump(case_params(cases), f)
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads),
+                   OPENBLAS_NUM_THREADS=str(threads), OPENBLAS_THREAD_TIMEOUT="4",
+                   PYTHONDONTWRITEBYTECODE="1")
+        cmd = [sys.executable, "-m", "oracle.cpu_baseline", path, "--kind", kind,
+               "--seconds", str(seconds), "--warmup", str(warmup),
+               "--max-rounds", str(max_rounds)]
+        if dump:
+            cmd += ["--dump", dump]
+        r = subprocess.run(cmd, cwd=HERE, env=env, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"CPU baseline run failed: {r.stderr[-2000:]}")
+        return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def cpu_baseline_record(cases):
+    """The GPU line's cpu_baseline: the C + OpenMP oracle on every host core
+    over the whole workload (about 20 s of rounds), one core on a sample of
+    two cases per grid size, and the oracle's reproducibility across BLAS
+    thread counts (the 512 x 256 rigid sphere, 100 steps, 1 thread vs all)."""
+    cores = host_cores()
+    full = cpu_run(cases, cores, seconds=20.0)
+    by_size = {}
+    for c in cases:
+        by_size.setdefault(c.nz, [])
+        if len(by_size[c.nz]) < 2:
+            by_size[c.nz].append(c)
+    sample = [c for nz in sorted(by_size) for c in by_size[nz]]
+    one = cpu_run(sample, 1, seconds=8.0, warmup=0)
+    import tempfile
+
+    from pyaxisymflow_gb300.engine import RigidBodyCase
+    with tempfile.TemporaryDirectory() as d:
+        dumps = []
+        for th in (1, cores):
+            path = os.path.join(d, f"w{th}.npz")
+            cpu_run([RigidBodyCase()], th, seconds=1e9, warmup=0, max_rounds=100, dump=path)
+            dumps.append(path)
+        a = np.load(dumps[0])["arr_0"]
+        b = np.load(dumps[1])["arr_0"]
+        floor = float(np.linalg.norm(a - b) / np.linalg.norm(a))
+    return {
+        "value": full["value"], "unit": UNIT, "cores": cores, "kind": "port",
+        "sample": (f"all {full['cases']} cases of the workload, {full['rounds']} timesteps each "
+                   f"({full['seconds']:.1f} s): the oracle with its grid kernels in C + OpenMP "
+                   f"({full['omp_threads']} threads; ENO3 as the reference's pystencils C with "
+                   f"OpenMP, the rest as its numba loops), spectral solve by numpy / OpenBLAS "
+                   f"({full['blas_threads']} threads), FP64"),
+        "cpu_model": full["cpu_model"], "machine": full["machine"],
+        "omp_threads": full["omp_threads"], "blas_threads": full["blas_threads"],
+        "one_core": {"value": one["value"], "unit": UNIT,
+                     "sample": f"{one['cases']} cases (two per grid size), {one['rounds']} "
+                               f"timestep(s) each, 1 OpenMP + 1 BLAS thread"},
+        "per_core_scaling": full["value"] / one["value"],
+        "blas_thread_floor": {"rel_l2_omega": floor,
+                              "case": "512 x 256 rigid sphere, 100 steps, OpenBLAS 1 thread vs "
+                                      f"{cores}"},
+    }
 
 
 def phase_times(ens, stream, n):
@@ -315,35 +347,32 @@ def fp32_accuracy(cases, dev, steps):
 
 
 def run_reference(args, world, rank):
+    """The reference's CPU implementation of the path on the host cores: the
+    oracle with its grid kernels in C + OpenMP on every core and the
+    spectral solve on OpenBLAS; a step advances every case of the workload
+    one timestep (the GPU arm's step); the steps stop after about two minutes
+    of stepping."""
     if rank != 0:
         return
     cases = ensemble_cases(args.workload)
-    sample = cases[:4] if len(cases) > 4 else cases
-    runs = OracleRuns(sample)
-    for _ in range(args.warmup):
-        runs.round()
-    # each step: one timestep of every sampled case; at most ~2 minutes of
-    # stepping in total (the remaining steps are not run)
-    times = []
-    budget = 120.0
-    for _ in range(args.steps):
-        times.append(runs.round())
-        if sum(times) > budget:
-            break
-    value = runs.cells * len(times) / sum(times)
-    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    desc = (f"{len(sample)} of the {len(cases)} cases "
-            f"({', '.join(f'{c.nz}x{c.nr}' for c in sample)}), 1 timestep each per step, "
-            f"{len(times)} steps timed, numpy FP64 oracle (BLAS threads = all cores, "
-            "elementwise single-threaded)")
+    cores = host_cores()
+    rec = cpu_run(cases, cores, seconds=120.0, warmup=min(args.warmup, 1),
+                  max_rounds=args.steps)
+    value = rec["value"]
+    desc = (f"all {len(cases)} cases, 1 timestep each per step, {rec['rounds']} of "
+            f"{args.steps} steps timed ({rec['seconds']:.1f} s), oracle with C + OpenMP grid "
+            f"kernels ({rec['omp_threads']} threads) and OpenBLAS solve "
+            f"({rec['blas_threads']} threads), FP64, {rec['cpu_model']}")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": len(times), "warmup": args.warmup,
-        "ms_per_step": float(1000.0 * sum(times) / len(times)),
+        "steps": rec["rounds"], "warmup": args.warmup,
+        "ms_per_step": float(1000.0 * rec["seconds"] / rec["rounds"]),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": args.workload, "sample": desc},
+        "data": "synthetic",
+        "config": {"workload": args.workload, "cases": len(cases),
+                   "cells_per_step": rec["cells_per_round"], "sample": desc},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": desc},
+                         "sample": desc, "cpu_model": rec["cpu_model"]},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -564,13 +593,7 @@ def run_gb300(args, world, rank, local):
     n_launch = 1 + 4 + 3
     line["gpu_launches"] = n_launch * args.steps
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        sample = cases[:4]
-        rate, secs, rounds = cpu_oracle_rate(sample, 2, min_seconds=10.0)
-        cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else 1
-        line["cpu_baseline"] = {
-            "value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"cases {', '.join(f'{c.nz}x{c.nr}' for c in sample)}, {rounds} timesteps "
-                      f"each, numpy FP64 oracle (BLAS on all cores), {secs:.1f} s"}
+        line["cpu_baseline"] = cpu_baseline_record(cases)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

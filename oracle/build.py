@@ -8,12 +8,16 @@
   core/src/mesh_to_particles.hpp) through oracle/ref_p2m_shim.cpp.
 Built only where the reference sources exist (their root is given by the
 caller or by the PYAXISYMFLOW_REF environment variable); never shipped.
+* oracle/_build/libora_step.so: the oracle's own C restatement of the
+  per-step grid kernels (oracle/cstep.c, OpenMP), the timed CPU baseline;
+  built everywhere.
 """
 import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
+BUILD_DIR = os.path.join(HERE, "_build")
 
 
 def ref_lsq_path():
@@ -53,10 +57,30 @@ def build_ref_p2m(ref_root=None):
     return _build_shim("ref_p2m_shim.cpp", ref_p2m_path(), _ref_root(ref_root))
 
 
+def cstep_path():
+    return os.path.join(BUILD_DIR, "libora_step.so")
+
+
+def build_cstep():
+    """Compiles oracle/cstep.c (portable flags: no -march, no FMA contraction,
+    so it gives the numpy oracle's bits on x86 and Arm alike)."""
+    src = os.path.join(HERE, "cstep.c")
+    out = cstep_path()
+    if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
+        return out
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    tmp = out + ".tmp"
+    subprocess.run(["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+                    "-o", tmp, src, "-lm"], check=True)
+    os.replace(tmp, out)
+    return out
+
+
 def build_all(ref_root=None):
-    """Builds what the given reference root (or PYAXISYMFLOW_REF) allows;
-    nothing without one."""
-    return {"ref_lsq": build_ref(ref_root), "ref_p2m": build_ref_p2m(ref_root)}
+    """Builds the oracle's C restatement and what the given reference root (or
+    PYAXISYMFLOW_REF) allows of the reference's own sources."""
+    return {"cstep": build_cstep(), "ref_lsq": build_ref(ref_root),
+            "ref_p2m": build_ref_p2m(ref_root)}
 
 
 if __name__ == "__main__":
