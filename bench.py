@@ -41,9 +41,11 @@ METRIC = "cell-updates/s on 1 GB300, batched FP32 vs plain FP64 at <=1e-5 L2; p5
 UNIT = "cell-updates/s"
 PHASES = ("kill", "transform", "vel_max", "penalise", "advect_diffuse")
 # Algorithmic fields moved per cell by each stencil phase (reads + writes):
-# vel_max psi; penalise psi chi omega -> u_z u_r omega; advect_diffuse omega
-# u_z u_r -> omega (+ omega's TF32 hi / lo operand copy on the tensor-core
-# path, + the rebuilt mask of sedimenting bodies).
+# vel_max psi; penalise psi chi omega -> u_z u_r and the penalised omega
+# (staged in the work buffer; + psi_lo with the refinement step);
+# advect_diffuse staged omega, u_z, u_r -> omega (+ omega's TF32 hi / lo
+# operand copy on the dense tensor-core path, + the rebuilt mask of
+# sedimenting bodies).
 PHASE_FIELDS = {"vel_max": 1, "penalise": 6, "advect_diffuse": 4}
 # the same in the FP64 engine (sedimenting bodies: + the rebuilt mask)
 PHASE_FIELDS_F64 = {"vel_max": 1, "penalise": 6, "advect_diffuse": 5}
@@ -449,6 +451,7 @@ def run_gb300(args, world, rank, local):
         for q in range(4):
             part_ms[q] += pev[s][q][0].elapsed_time(pev[s][q][1]) / nph
     uses_dct = ens.dct
+    uses_refine = ens.refine
     # ---- end to end through the public API with host buffers ------------------
     # every case's vorticity in pinned host memory; each step copies it in,
     # advances every case and copies it and the state blocks (dt, Cd) back,
@@ -521,6 +524,8 @@ def run_gb300(args, world, rank, local):
         PHASE_FIELDS["advect_diffuse"] += 2   # omega's TF32 operand pair
     if any(c.sediment for c in cases):
         PHASE_FIELDS["advect_diffuse"] += 1   # the rebuilt mask
+    if uses_refine:
+        PHASE_FIELDS["penalise"] += 1         # psi_lo
     zname = "z_transforms" if uses_dct else "z_products"
     kern_ms = {"kill": ph_ms["kill"], zname: part_ms[0] + part_ms[2],
                "r_products": part_ms[1] + part_ms[3], "vel_max": ph_ms["vel_max"],
@@ -544,9 +549,12 @@ def run_gb300(args, world, rank, local):
                     "unit": "TFLOP/s", "useful_tflops": achieved,
                     "peak_source": f"{src} bf16 / 2 (TF32 dense rate)"}
     elif dom == "z_transforms":
-        # forward: read the rows (4 B), write the TF32 pair (8 B); inverse: read
-        # the rows and the spectral factor (4 + 4 B), write the pair (8 B)
-        nbytes = sum(28.0 * c.nr * c.nz for c in cases)
+        # forward: read the rows (4 B; with the refinement step also psi and
+        # psi_lo, 8 B more, for the residual), write the TF32 pair (8 B);
+        # inverse: read the rows and the spectral factor (4 + 4 B), write the
+        # pair (8 B)
+        per_cell = 36.0 if uses_refine else 28.0
+        nbytes = sum(per_cell * c.nr * c.nz for c in cases)
         achieved = nbytes / (kern_ms[dom] / 1000.0) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "peak_source": f"{src} hbm"}
@@ -592,6 +600,9 @@ def run_gb300(args, world, rank, local):
     # path), vel_max (which also computes dt), penalise, advect_diffuse
     n_launch = 1 + 4 + 3
     line["gpu_launches"] = n_launch * args.steps
+    # ---- continuous-batching serving leg (config 5) ----------------------------
+    if not args.no_serve:
+        line["serving"] = serve_leg(args, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_record(cases)
     if rank == 0:
@@ -652,9 +663,21 @@ def run_poisson(args, world, rank, local):
         t32 = timed(lambda: s32.solve(psi32, tw), args.steps)
     t64 = timed(lambda: s64.solve(psi64, tw), max(3, args.steps // 4))
     tc_ms = timed(lambda: s32.engine._tc_run(ctypes_stream(stream)), args.steps)
-    uz64, ur64, uz32, ur32 = (torch.zeros_like(tw) for _ in range(4))
+    uz64, ur64 = (torch.zeros_like(tw) for _ in range(2))
     compute_velocity_from_psi_unb(uz64, ur64, psi64, tR, dx)
-    compute_velocity_from_psi_unb(uz32, ur32, psi32, tR, dx)
+    # velocity by the FP32 stencil from psi as a float pair hi + lo (the
+    # fused engine's representation), summed in float
+    f32 = dict(dtype=torch.float32, device=dev)
+    hi = psi32.float()
+    lo = (psi32 - hi.double()).float()
+    tRf = tR.float()
+    parts = []
+    for part in (hi, lo):
+        u = [torch.zeros((nr, nz), **f32) for _ in range(2)]
+        compute_velocity_from_psi_unb(u[0], u[1], part, tRf, dx)
+        parts.append(u)
+    uz32 = (parts[0][0] + parts[1][0]).double()
+    ur32 = (parts[0][1] + parts[1][1]).double()
 
     def rel(a, b):
         return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
@@ -712,23 +735,23 @@ def ctypes_stream(stream):
     return ctypes.c_void_p(stream.cuda_stream)
 
 
-def run_serve(args, world, rank, local):
-    """Continuous-batching server on a Poisson stream of requests (mean 20/s):
-    grids 256 x 128 .. 2048 x 1024, sphere / torus / spheroid, 500-5000 steps,
-    Re log-uniform in [10, 500], 80% HBM budget."""
+def serve_leg(args, dev, clocks=None):
+    """Continuous batching on a Poisson stream of requests (mean 20/s): grids
+    256 x 128 .. 2048 x 1024, sphere / torus / spheroid, 500-5000 steps, Re
+    log-uniform in [10, 500], 80% HBM budget; and the same requests run one
+    after another on the plain FP64 engine (per-size step time of one case
+    alone, times the steps asked)."""
     import torch
+
     from pyaxisymflow_gb300.engine import RigidEnsemble
     from pyaxisymflow_gb300.serving import SimulationServer, poisson_requests
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
     reqs = poisson_requests(args.requests, rate_per_s=20.0, seed=5)
     server = SimulationServer(precision=args.precision, device=dev, hbm_budget=0.8)
     server.prepare([r.case for r in reqs])
-    with ClockSampler(local) as clocks:
-        report = server.run(reqs)
+    report = server.run(reqs)
     summ = report.summary()
-    # plain sequential FP64 on the same GPU: per-size step time of one case
-    # alone, applied to the same request list
+    del server
+    torch.cuda.empty_cache()
     per_size = {}
     for r in reqs:
         key = (r.case.nz, r.case.nr)
@@ -744,21 +767,39 @@ def run_serve(args, world, rank, local):
         del e
     seq_s = sum(per_size[(r.case.nz, r.case.nr)] * r.steps for r in reqs)
     seq_cells = sum(r.case.nz * r.case.nr * r.steps for r in reqs)
-    line = {
-        "metric": METRIC, "value": summ["cell_updates_per_s"], "unit": UNIT, "n_gpus": world,
-        "steps": sum(len(report.step_latency_s) for _ in [0]), "warmup": 0,
-        "ms_per_step": summ["step_p50_ms"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": args.precision, "data": "synthetic",
-        "config": {"workload": "serve", "requests": len(reqs), "arrival_rate_per_s": 20.0,
+    return {
+        "config": {"requests": len(reqs), "arrival_rate_per_s": 20.0,
                    "grids": "nz in {256, 512, 1024, 2048}, nr = nz / 2",
                    "bodies": "sphere / torus / spheroid (aspect U[0.5, 2])",
-                   "steps_per_request": "U{500..5000}", "hbm_budget": 0.8, "seed": 5},
-        "serving": summ,
+                   "steps_per_request": "U{500..5000}", "hbm_budget": 0.8, "seed": 5,
+                   "precision": args.precision, "steps_in_flight": 2},
+        "summary": summ,
+        "steps": len(report.step_latency_s),
         "plain_fp64_sequential": {"value": seq_cells / seq_s, "wall_s_estimate": seq_s,
                                   "speedup_served_over_sequential_fp64":
                                       summ["cell_updates_per_s"] / (seq_cells / seq_s)},
+    }
+
+
+def run_serve(args, world, rank, local):
+    """The serving workload alone (config: Poisson arrivals, mixed grids and
+    bodies, HBM-budget admission)."""
+    import torch
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    with ClockSampler(local) as clocks:
+        leg = serve_leg(args, dev)
+    summ = leg["summary"]
+    line = {
+        "metric": METRIC, "value": summ["cell_updates_per_s"], "unit": UNIT, "n_gpus": world,
+        "steps": leg["steps"], "warmup": 0,
+        "ms_per_step": summ["step_p50_ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.precision, "data": "synthetic",
+        "config": dict(leg["config"], workload="serve"),
+        "serving": summ,
+        "plain_fp64_sequential": leg["plain_fp64_sequential"],
         "clocks": clocks.summary(),
-        "gpu_launches": 8 * len(report.step_latency_s),
+        "gpu_launches": 8 * leg["steps"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -874,6 +915,8 @@ def main():
     ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="skip the continuous-batching serving leg of the default line")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default launch choices (no autotuning)")
     ap.add_argument("--no-accuracy", action="store_true",

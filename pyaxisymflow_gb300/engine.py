@@ -381,6 +381,7 @@ class RigidEnsemble:
         self._free = list(range(capacity - 1, -1, -1))
         self._bases = {}
         self.members = []
+        self._omega_arena = None
         self.graph = None
         self.tuning = {}
         lib = N.lib()
@@ -408,10 +409,18 @@ class RigidEnsemble:
         self.members.append(m)
         return m
 
+    @property
+    def omega_arena(self):
+        """Every member's omega in one contiguous device buffer (members in
+        order, each (nr, nz) row-major); a plan made without packing is made
+        again with it on first use."""
+        if self._omega_arena is None and self.members:
+            self._replan(pack=True)
+        return self._omega_arena
+
     def _pack_vorticity(self):
-        """Place every member's omega in one contiguous device arena (members
-        in order, each (nr, nz) row-major), so host transfers of all cases'
-        vorticity are one copy each way (omega_arena)."""
+        """Place every member's omega in one contiguous device arena, so host
+        transfers of all cases' vorticity are one copy each way."""
         n = sum(m.case.nr * m.case.nz for m in self.members)
         arena = torch.empty(max(n, 1), dtype=self.dtype, device=self.device)
         off = 0
@@ -422,12 +431,19 @@ class RigidEnsemble:
             m.fields["omega"] = view
             m.struct.omega = view.data_ptr()
             off += c.nr * c.nz
-        self.omega_arena = arena[:n]
+        self._omega_arena = arena[:n]
 
-    def _replan(self):
+    def _replan(self, pack=True):
+        """Rebuild and upload the plan for the current members. pack=False
+        leaves each omega where it is (no copy of every case's vorticity; the
+        continuous-batching server re-plans at every admission and
+        retirement and never needs the arena)."""
         self.graph = None
         n = len(self.members)
-        self._pack_vorticity()
+        if pack:
+            self._pack_vorticity()
+        else:
+            self._omega_arena = None
         self.structs = (AxiCase * max(n, 1))()
         for k, m in enumerate(self.members):
             self.structs[k] = m.struct

@@ -256,10 +256,13 @@ def test_engine_f32_tensor_cores_error_vs_fp64_oracle():
     assert d < 1e-5, d
 
 
-@pytest.mark.parametrize("precision,tol", [("f64", 1e-11), ("f32", 1e-4)])
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-12), ("f32", 1e-4)])
 def test_engine_sedimenting_sphere_matches_oracle(precision, tol):
     """Freely sedimenting sphere (examples/SedimentingRigidSphere/falling_rigid_sphere.py):
-    moving mask, FP64 force integral and body ODE on the device."""
+    moving mask, FP64 force integral and body ODE on the device. The FP64
+    engine follows the oracle to 1e-12 (body position, velocity and
+    vorticity); one double ulp of noise in the oracle's own initial
+    vorticity moves its result by 1e-15 over these 40 steps."""
     from pyaxisymflow_gb300.engine import (ST_UBODY, ST_ZCM, RigidBodyCase, RigidEnsemble)
     nz, nr, steps = 128, 64, 40
     oc = sim.SedimentingCase(nz=nz, nr=nr, dx=1.0 / nz, r_sphere=0.08, z_cm=0.6, nu=0.01,
@@ -282,7 +285,7 @@ def test_engine_sedimenting_sphere_matches_oracle(precision, tol):
     assert abs(s[ST_ZCM] - st.part_Z_cm) <= tol * abs(st.part_Z_cm)
     assert abs(s[ST_UBODY] - st.U_z_cm_part) <= tol * abs(st.U_z_cm_part) + 1e-14
     err = rel_l2(e.fields[0]["omega"].double().cpu().numpy(), st.vorticity)
-    assert err < tol * 10, err
+    assert err < (tol if precision == "f64" else tol * 10), err
     chi_err = np.abs(e.fields[0]["chi"].double().cpu().numpy() - st.char_func).max()
     assert chi_err < (1e-12 if precision == "f64" else 1e-5), chi_err
 
