@@ -356,6 +356,18 @@ def run_reference(args, world, rank):
     of stepping."""
     if rank != 0:
         return
+    if args.workload == "soft1024":
+        rec = soft_cpu_record(soft_case(), seconds=120.0)
+        line = {"impl": "reference", "metric": "cell-updates/s, soft-sphere streaming loop (FP64)",
+                "value": rec["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "soft1024", "sample": rec["sample"]},
+                "cpu_baseline": rec,
+                "e2e": {"value": rec["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     cases = ensemble_cases(args.workload)
     cores = host_cores()
     rec = cpu_run(cases, cores, seconds=120.0, warmup=min(args.warmup, 1),
@@ -730,6 +742,146 @@ def run_poisson(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def soft_case():
+    """Config 2: a soft neo-Hookean sphere (radius 0.1, G = 1e-3, density
+    ratio 1) in oscillatory streaming, U(t) = 0.1 cos(2 pi t) on the
+    penalised forcing region, 1024 x 512 cells on z in [0, 1], r in [0, 0.5]
+    (the example's domain, dx = 1 / nz), the example's viscosity ratio and
+    Brinkman factor."""
+    from pyaxisymflow_gb300.simulation import SoftCase
+    omega = 2 * math.pi
+    e = 0.1 / (0.1 * omega)
+    return SoftCase(nz=1024, nr=512, dx=1.0 / 1024, z_cm=0.5, r_ball=0.1, freq=1.0, e=e,
+                    cauchy=e * (0.1 * omega) ** 2 / 1e-3)
+
+
+def run_soft(args, world, rank, local):
+    """Config 2 on the device: the soft-sphere loop with dt and t resident
+    on the GPU (SoftSphereEngine), one CUDA graph per step, FP64."""
+    import torch
+
+    from pyaxisymflow_gb300.simulation import SOFT_WORDS, SoftSphereEngine
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    case = soft_case()
+    cells = case.nr * case.nz
+    eng = SoftSphereEngine(case, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    eng.capture(1)
+    for _ in range(args.warmup):
+        eng.replay()
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+        ev[0].record(stream)
+        for k in range(args.steps):
+            eng.replay()
+            ev[k + 1].record(stream)
+        torch.cuda.synchronize(dev)
+        barrier(world)
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    ms = max_over_ranks(world, ev[0].elapsed_time(ev[-1])) / args.steps
+    status = eng.status()
+    # device time of each launch group of a step
+    nph = max(3, min(args.steps, 10))
+    pev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            for _ in eng.PARTS] for _ in range(nph)]
+    for q in range(nph):
+        for k in range(len(eng.PARTS)):
+            pev[q][k][0].record(stream)
+            eng.phase(k)
+            pev[q][k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    part_ms = {name: sum(pev[q][k][0].elapsed_time(pev[q][k][1]) for q in range(nph)) / nph
+               for k, name in enumerate(eng.PARTS)}
+    dom = max(part_ms, key=part_ms.get)
+    hbm, _, src = peaks()
+    if dom == "solve_velocity_dt":
+        # the four FP64 products of the spectral solve: 2 n m k flops each
+        flops = 4.0 * (case.nr * case.nz * case.nz + case.nr * case.nr * case.nz)
+        achieved = flops / (part_ms[dom] / 1e3) / 1e12
+        roof = {"bound": "fp64", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
+                "peak_source": "nominal GB300 FP64 (dense products; no FP64 tensor path)"}
+    else:
+        # FP64 fields read + written per cell by the group (algorithmic)
+        fields = {"advect_pin_mask": 23, "extrapolate": 12, "solid_stress": 17,
+                  "tether_penalise_diffuse": 19}[dom]
+        achieved = fields * 8.0 * cells / (part_ms[dom] / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "peak_source": f"{src} hbm"}
+    roof.update({"kernel": dom, "frac": roof["achieved"] / roof["peak"],
+                 "kernel_ms": part_ms[dom], "traffic": None})
+    # end to end: omega in from pinned host memory, one step, omega / eta1 /
+    # eta2 and the state block back, every step
+    host_w = torch.empty((case.nr, case.nz), dtype=torch.float64, pin_memory=True)
+    host_w.copy_(eng.vorticity)
+    host_out = torch.empty((3, case.nr, case.nz), dtype=torch.float64, pin_memory=True)
+    host_state = torch.empty(SOFT_WORDS, dtype=torch.float64, pin_memory=True)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.vorticity.copy_(host_w, non_blocking=True)
+        eng.replay()
+        host_out[0].copy_(eng.vorticity, non_blocking=True)
+        host_out[1].copy_(eng.eta1, non_blocking=True)
+        host_out[2].copy_(eng.eta2, non_blocking=True)
+        host_state.copy_(eng.state, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        host_w.copy_(host_out[0])
+    e2e_s = max_over_ranks(world, (time.perf_counter() - t0) / args.steps)
+    line = {
+        "metric": "cell-updates/s, soft-sphere streaming loop (FP64)", "value": cells * world
+        / (ms / 1e3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "soft1024", "grid": "nz 1024 x nr 512, dx = 1/1024",
+                   "body": "soft neo-Hookean sphere r 0.1, G 1e-3, density ratio 1",
+                   "forcing": "U(t) = 0.1 cos(2 pi t)", "nu": case.nu, "lam": case.lam,
+                   "dt": eng.dt, "l2": "each step touches > L2 (about 40 FP64 fields)"},
+        "roofline": roof,
+        "phase_ms": part_ms,
+        "step_latency_ms": {"p50": float(np.percentile(step_ms, 50)),
+                            "p99": float(np.percentile(step_ms, 99))},
+        "extrapolation_sweeps_max": float(eng.state[4]),
+        "e2e": {"value": cells * world / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": host_w.numel() * 8,
+                "d2h_bytes_per_step": host_out.numel() * 8 + SOFT_WORDS * 8},
+        "gpu_launches": eng.LAUNCHES_PER_STEP * args.steps,
+        "clocks": clocks.summary(),
+        "status_ok": status == 0,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = soft_cpu_record(case, seconds=12.0)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def soft_cpu_record(case, seconds):
+    """The numpy oracle's soft loop on the host (its least-squares sweeps and
+    ENO3 in numpy, slower than the reference's C++ and pystencils C), a
+    bounded sample of steps of the same case."""
+    from oracle import kernels as K
+    from oracle import simulation as osim
+    st, coords = osim.soft_sphere_init(case, K)
+    solver = K.FastDiagonalisationStokesSolver(case.nr, case.nz, case.dx)
+    aw = K.gen_advect_vorticity_via_eno3(case.dx, case.nr, case.nz)
+    ae = K.gen_advect_refmap_via_eno3(case.dx, case.nr, case.nz)
+    osim.soft_sphere_step(case, st, coords, solver, aw, ae, K)
+    n, t0 = 0, time.perf_counter()
+    while n < 1 or time.perf_counter() - t0 < seconds:
+        osim.soft_sphere_step(case, st, coords, solver, aw, ae, K)
+        n += 1
+    secs = time.perf_counter() - t0
+    return {"value": case.nr * case.nz * n / secs, "unit": UNIT, "cores": host_cores(),
+            "kind": "port",
+            "sample": f"{case.nz} x {case.nr}, {n} steps of the numpy oracle's soft loop "
+                      f"({secs:.1f} s; BLAS on all cores, elementwise work, ENO3 and the "
+                      "least-squares sweeps in numpy)"}
+
+
 def ctypes_stream(stream):
     import ctypes
     return ctypes.c_void_p(stream.cuda_stream)
@@ -910,7 +1062,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ensemble64",
-                    choices=["ensemble64", "sphere512", "poisson2048", "serve", "remesh"])
+                    choices=["ensemble64", "sphere512", "poisson2048", "serve", "remesh",
+                             "soft1024"])
     ap.add_argument("--requests", type=int, default=40)
     ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -936,6 +1089,8 @@ def main():
         run_serve(args, world, rank, local)
     elif args.workload == "remesh":
         run_remesh(args, world, rank, local)
+    elif args.workload == "soft1024":
+        run_soft(args, world, rank, local)
     else:
         run_gb300(args, world, rank, local)
 

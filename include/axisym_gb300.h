@@ -595,6 +595,80 @@ int axi_rigid_phase_f64(const axi_plan_info* info, const void* plan_dev, int pha
 int axi_rigid_phase_f32(const axi_plan_info* info, const void* plan_dev, int phase,
                         void* stream);
 
+/* ---------------------------------------------------------------------
+ * Soft-sphere streaming loop with the time step on the device
+ * (examples/SoftSphereStreaming/soft_sphere_streaming.py:129-272).
+ * The drop-in kernels above take dt and t as host scalars, so a host loop
+ * must read max |u| back each step. These entries keep dt and t in a state
+ * block of AXI_SOFT_WORDS doubles (zero it before the first step) and read
+ * them on the device; the arithmetic is that of the host-dt kernels, so a
+ * loop made of them (pyaxisymflow_gb300.simulation.SoftSphereEngine) runs
+ * without a host round trip and can be captured in a CUDA graph. FP64.
+ * ------------------------------------------------------------------ */
+enum {
+  AXI_SOFT_T = 0,       /* simulated time */
+  AXI_SOFT_DT = 1,      /* time step of the current step */
+  AXI_SOFT_STEPS = 2,   /* steps taken */
+  AXI_SOFT_STATUS = 3,  /* sticky status bits (uint64 view): 1 << AXI_ERR_* */
+  AXI_SOFT_SWEEPS = 4,  /* largest extrapolation sweep count seen */
+  AXI_SOFT_UMAX = 5,    /* scratch of axi_soft_dt (kept zero between calls) */
+  AXI_SOFT_COUNT = 6,   /* scratch of axi_soft_dt (kept zero between calls) */
+  AXI_SOFT_WORDS = 8
+};
+/* dt = min(dt_elastic, cfl_dx / (max(|u_z| + |u_r|) + eps), dt_diffusive) into
+ * state[AXI_SOFT_DT] (soft_sphere_streaming.py:168-172). */
+int axi_soft_dt_f64(const double* u_z, const double* u_r, int64_t n, double* state,
+                    double dt_elastic, double cfl_dx, double dt_diffusive, double eps,
+                    void* stream);
+/* ENO3 advection with dt from the state: refmap != 0 advects (eta1, eta2) as
+ * axi_advect_refmap_eno3_f64, else f0 = omega as axi_advect_vorticity_eno3_f64
+ * (scratch: 2 or 1 fields). */
+int axi_soft_advect_eno3_f64(double* f0, double* f1, int refmap, const double* u_z,
+                             const double* u_r, double* scratch, int nr, int nz, double dx,
+                             const double* state, void* stream);
+/* ball_phi = where(ball_phi > band, -sqrt((eta1 - z_cm)^2 + eta2^2) + r_ball, ball_phi)
+ * (soft_sphere_streaming.py:191-193; band = -3 dx). */
+int axi_soft_pin_level_set_f64(double* ball_phi, const double* eta1, const double* eta2,
+                               int64_t n, double z_cm, double r_ball, double band,
+                               void* stream);
+/* chi = smooth_Heaviside(phi, blend_w) and inside = chi > 0.5 (:205-206). */
+int axi_soft_mask_f64(double* chi, uint8_t* inside, const double* phi, int64_t n,
+                      double blend_w, void* stream);
+/* The extrapolation of axi_extrapolate_eta_with_least_squares_f64 without a
+ * host round trip: failures set state[AXI_SOFT_STATUS] bits, the sweep count
+ * goes to state[AXI_SOFT_SWEEPS]. */
+int axi_soft_extrapolate_eta_f64(const uint8_t* inside_solid, const double* ball_phi,
+                                 double* eta1, double* eta2, double* ball_phi_double,
+                                 double* eta1_double, double* eta2_double, int16_t* current_flag,
+                                 int16_t* target_flag, double extrap_zone, int nr, int nz,
+                                 const double* grid_x, const double* grid_y, int max_sweeps,
+                                 void* work, double* state, void* stream);
+/* sigma_ij *= chi (:236-238). */
+int axi_soft_stress_mask_f64(double* s11, double* s12, double* s22, const double* chi,
+                             int64_t n, void* stream);
+/* axi_update_vorticity_from_solid_stress_f64 with dt from the state (:239-241). */
+int axi_soft_update_vorticity_from_solid_stress_f64(double* vort, double* tau_z, double* tau_r,
+                                                    const double* t11, const double* t12,
+                                                    const double* t22, const double* R, int nr,
+                                                    int nz, double dx, const double* state,
+                                                    void* stream);
+/* Tether mask: smooth_Heaviside(-sqrt((Z - z_cm - e_r_ball sin(omega t))^2 + R^2)
+ * + zeta_r_ball, blend_w) with t from the state (:243-245). */
+int axi_soft_tether_f64(double* tether_chi, const double* Z, const double* R, int64_t n,
+                        const double* state, double z_cm, double e_r_ball, double omega,
+                        double zeta_r_ball, double blend_w, void* stream);
+/* Brinkman penalisation of (u_z, u_r) towards (U0 cos(omega_f t), 0) with
+ * lam dt chi, then omega += curl(u_pen - u) on the interior (:248-264);
+ * d_z, d_r: (nr, nz) scratch. */
+int axi_soft_penalise_f64(double* omega, double* u_z, double* u_r, const double* tether_chi,
+                          double* d_z, double* d_r, int nr, int nz, double dx, double lam,
+                          double U0, double omega_f, const double* state, void* stream);
+/* axi_diffusion_rk2_unb_f64 with dt from the state (:267). */
+int axi_soft_diffusion_rk2_f64(double* vort, double* tmp, const double* R, int nr, int nz,
+                               double nu, double dx, const double* state, void* stream);
+/* t += dt, steps += 1 (:270-272). */
+int axi_soft_advance_f64(double* state, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,20 @@ def _signatures():
         "axi_rigid_step_f32": (I, [P, P, I, P]),
         "axi_rigid_phase_f64": (I, [P, P, I, P]),
         "axi_rigid_phase_f32": (I, [P, P, I, P]),
+        # the soft-sphere loop with dt and t on the device
+        "axi_soft_dt_f64": (I, [P, P, I64, P, D, D, D, D, P]),
+        "axi_soft_advect_eno3_f64": (I, [P, P, I, P, P, P, I, I, D, P, P]),
+        "axi_soft_pin_level_set_f64": (I, [P, P, P, I64, D, D, D, P]),
+        "axi_soft_mask_f64": (I, [P, P, P, I64, D, P]),
+        "axi_soft_extrapolate_eta_f64": (
+            I, [P, P, P, P, P, P, P, P, P, D, I, I, P, P, I, P, P, P]),
+        "axi_soft_stress_mask_f64": (I, [P, P, P, P, I64, P]),
+        "axi_soft_update_vorticity_from_solid_stress_f64": (
+            I, [P, P, P, P, P, P, P, I, I, D, P, P]),
+        "axi_soft_tether_f64": (I, [P, P, P, I64, P, D, D, D, D, D, P]),
+        "axi_soft_penalise_f64": (I, [P, P, P, P, P, P, I, I, D, D, D, D, P, P]),
+        "axi_soft_diffusion_rk2_f64": (I, [P, P, P, I, I, D, D, P, P]),
+        "axi_soft_advance_f64": (I, [P, P]),
     }
     for s in ("f64", "f32"):
         T = _real(s)

@@ -56,10 +56,13 @@ template <typename T, int NF, bool CONS>
 __global__ void eno3_step_kernel(T* __restrict__ dst0, T* __restrict__ dst1,
                                  const T* __restrict__ src0, const T* __restrict__ src1,
                                  T par0, T par1, const T* __restrict__ uz,
-                                 const T* __restrict__ ur, int nr, int nz, T a) {
+                                 const T* __restrict__ ur, int nr, int nz, T a,
+                                 const double* __restrict__ dt_dev, T dx) {
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   if (i >= nr || j >= nz) return;
+  // a device-resident time step (the soft-sphere loop): a = -(dt / dx)
+  if (dt_dev) a = -rn_div(static_cast<T>(dt_dev[0]), dx);
   const long long c = (long long)i * nz + j;
   const bool interior = (i < nr - 2) && (j >= 2) && (j < nz - 2);
 #pragma unroll
@@ -106,7 +109,8 @@ __global__ void eno3_step_kernel(T* __restrict__ dst0, T* __restrict__ dst1,
 
 template <typename T, int NF, bool CONS>
 int eno3_launch(T* f0, T* f1, T par0, T par1, const T* uz, const T* ur, T* scratch, int nr,
-                int nz, T dt_by_dx, cudaStream_t s, const char* what) {
+                int nz, T dt_by_dx, cudaStream_t s, const char* what,
+                const double* dt_dev = nullptr, T dx = T(0)) {
   if (nr < 3 || nz < 5) {
     axi::set_error("%s: grid %d x %d too small for ENO3 (needs nr >= 3, nz >= 5)", what, nr, nz);
     return AXI_ERR_INVALID;
@@ -123,7 +127,8 @@ int eno3_launch(T* f0, T* f1, T par0, T par1, const T* uz, const T* ur, T* scrat
   }
   dim3 grid(axi::ceil_div(nz, BX), axi::ceil_div(nr, BY));
   eno3_step_kernel<T, NF, CONS><<<grid, dim3(BX, BY), 0, s>>>(f0, f1, scratch, s1, par0, par1,
-                                                              uz, ur, nr, nz, -dt_by_dx);
+                                                              uz, ur, nr, nz, -dt_by_dx,
+                                                              dt_dev, dx);
   return axi::launch_status(what);
 }
 
@@ -171,3 +176,23 @@ int eno3_launch(T* f0, T* f1, T par0, T par1, const T* uz, const T* ur, T* scrat
 
 AXI_DEFINE_ENO3(f64, double)
 AXI_DEFINE_ENO3(f32, float)
+
+// The soft-sphere loop's two advections with the time step read on the device
+// (state[AXI_SOFT_DT]): eta (non-conservative, eta1 even and eta2 odd about the
+// axis, elasto_kernels/advect_refmap_via_eno3.py:8-44) or omega (conservative,
+// odd), the arithmetic of the host-dt entries above.
+extern "C" int axi_soft_advect_eno3_f64(double* f0, double* f1, int refmap, const double* u_z,
+                                        const double* u_r, double* scratch, int nr, int nz,
+                                        double dx, const double* state, void* stream) {
+  axi::clear_error();
+  AXI_TRY(axi::check_ptr("soft_advect_eno3", state, "state"));
+  if (refmap) {
+    AXI_TRY(axi::check_ptr("soft_advect_eno3", f1, "eta2"));
+    return eno3_launch<double, 2, false>(f0, f1, 1.0, -1.0, u_z, u_r, scratch, nr, nz, 0.0,
+                                         axi::as_stream(stream), "soft_advect_eno3",
+                                         state + AXI_SOFT_DT, dx);
+  }
+  return eno3_launch<double, 1, true>(f0, nullptr, -1.0, 0.0, u_z, u_r, scratch, nr, nz, 0.0,
+                                      axi::as_stream(stream), "soft_advect_eno3",
+                                      state + AXI_SOFT_DT, dx);
+}

@@ -181,10 +181,12 @@ __device__ __forceinline__ T rk2_operator(const T* __restrict__ w, const T* __re
 template <typename T>
 __global__ void rk2_stage1_kernel(const T* __restrict__ w, T* __restrict__ tmp,
                                   const T* __restrict__ R, int nr, int nz, T coef, T dx2,
-                                  T two_dx) {
+                                  T two_dx, const double* __restrict__ dt_dev = nullptr) {
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   if (i >= nr || j >= nz) return;
+  // device-resident time step: coef holds the factor of dt ((0.5 nu) or nu)
+  if (dt_dev) coef = rn_mul(coef, static_cast<T>(dt_dev[0]));
   const long long c = (long long)i * nz + j;
   T v = w[c];
   if (i > 0 && j > 0 && i < nr - 1 && j < nz - 1)
@@ -196,10 +198,11 @@ __global__ void rk2_stage1_kernel(const T* __restrict__ w, T* __restrict__ tmp,
 template <typename T>
 __global__ void rk2_stage2_kernel(T* __restrict__ w, const T* __restrict__ tmp,
                                   const T* __restrict__ R, int nr, int nz, T coef, T dx2,
-                                  T two_dx) {
+                                  T two_dx, const double* __restrict__ dt_dev = nullptr) {
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   if (i < 1 || j < 1 || i >= nr - 1 || j >= nz - 1) return;
+  if (dt_dev) coef = rn_mul(coef, static_cast<T>(dt_dev[0]));
   const long long c = (long long)i * nz + j;
   w[c] = rn_add(w[c], rn_mul(coef, rk2_operator(tmp, R, c, nz, dx2, two_dx)));
 }
@@ -276,10 +279,12 @@ __global__ void div_tau_kernel(T* __restrict__ tz, T* __restrict__ tr, const T* 
 // elasto_kernels/div_tau.py:30-34: vort[1:-1,1:-1] += dt (dtau_r/dz - dtau_z/dr) / (2 dx)
 template <typename T>
 __global__ void curl_tau_kernel(T* __restrict__ w, const T* __restrict__ tz,
-                                const T* __restrict__ tr, int nr, int nz, T dt, T dx) {
+                                const T* __restrict__ tr, int nr, int nz, T dt, T dx,
+                                const double* __restrict__ dt_dev = nullptr) {
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   if (i < 1 || j < 1 || i >= nr - 1 || j >= nz - 1) return;
+  if (dt_dev) dt = static_cast<T>(dt_dev[0]);
   const long long c = (long long)i * nz + j;
   T a = rn_sub(rn_sub(tr[c + 1], tr[c - 1]), tz[c + nz]);
   a = rn_add(a, tz[c - nz]);
@@ -453,3 +458,36 @@ AXI_DEFINE_VORTICITY(f64, double)
 AXI_DEFINE_VORTICITY(f32, float)
 AXI_DEFINE_POINTWISE(f64, double)
 AXI_DEFINE_POINTWISE(f32, float)
+
+// The soft-sphere loop's dt-dependent kernels with the time step read on the
+// device (state[AXI_SOFT_DT]); the arithmetic of the host-dt entries above.
+extern "C" int axi_soft_update_vorticity_from_solid_stress_f64(
+    double* vort, double* tau_z, double* tau_r, const double* t11, const double* t12,
+    const double* t22, const double* R, int nr, int nz, double dx, const double* state,
+    void* stream) {
+  axi::clear_error();
+  AXI_TRY(axi::check_grid("soft_update_vorticity_from_solid_stress", nr, nz));
+  AXI_TRY(axi::check_ptr("soft_update_vorticity_from_solid_stress", state, "state"));
+  cudaStream_t s = axi::as_stream(stream);
+  div_tau_kernel<double><<<grid2d(nr, nz), dim3(BX, BY), 0, s>>>(tau_z, tau_r, t11, t12, t22, R,
+                                                                  nr, nz, dx);
+  curl_tau_kernel<double><<<grid2d(nr, nz), dim3(BX, BY), 0, s>>>(vort, tau_z, tau_r, nr, nz,
+                                                                   0.0, dx, state + AXI_SOFT_DT);
+  return axi::launch_status("soft_update_vorticity_from_solid_stress");
+}
+
+extern "C" int axi_soft_diffusion_rk2_f64(double* vort, double* tmp, const double* R, int nr,
+                                          int nz, double nu, double dx, const double* state,
+                                          void* stream) {
+  axi::clear_error();
+  AXI_TRY(axi::check_grid("soft_diffusion_rk2", nr, nz));
+  AXI_TRY(axi::check_ptr("soft_diffusion_rk2", state, "state"));
+  cudaStream_t s = axi::as_stream(stream);
+  const double dx2 = rn_host_mul(dx, dx), two_dx = rn_host_mul(2.0, dx);
+  const double half_nu = rn_host_mul(0.5, nu);
+  rk2_stage1_kernel<double><<<grid2d(nr, nz), dim3(BX, BY), 0, s>>>(
+      vort, tmp, R, nr, nz, half_nu, dx2, two_dx, state + AXI_SOFT_DT);
+  rk2_stage2_kernel<double><<<grid2d(nr, nz), dim3(BX, BY), 0, s>>>(
+      vort, tmp, R, nr, nz, nu, dx2, two_dx, state + AXI_SOFT_DT);
+  return axi::launch_status("soft_diffusion_rk2");
+}

@@ -4,9 +4,13 @@ RigidSphereSimulation runs the loop body of
 examples/FlowPastSphere/flow_past_sphere.py:107-188 (kill boundary vorticity,
 stream-function solve, velocity, free stream, CFL time step, Brinkman
 penalisation and its vorticity, drag, ENO3 advection, RK2 diffusion) with all
-fields resident on one GPU.
+fields resident on one GPU. SoftSphereSimulation runs the soft-sphere
+streaming loop through the drop-in kernels (dt formed on the host each
+step); SoftSphereEngine runs the same loop with dt and t on the device.
 """
+import ctypes
 import math
+from dataclasses import dataclass
 
 import numpy as np
 import torch
@@ -22,6 +26,53 @@ from .kernels.kill_boundary_vorticity_sine import (kill_boundary_vorticity_sine_
 from .kernels.smooth_Heaviside import smooth_Heaviside
 
 EPS = float(np.finfo(float).eps)
+
+
+@dataclass
+class SoftCase:
+    """Parameters of the soft-sphere streaming loop, named as in
+    examples/SoftSphereStreaming/soft_sphere_streaming.py:31-63 (defaults:
+    that example on its 256 x 128 grid); derived quantities follow its
+    formulas."""
+    nz: int = 256
+    nr: int = 128
+    dx: float = 1.0 / 256
+    z_cm: float = 0.5
+    r_ball: float = 0.15
+    rho_f: float = 1.0
+    freq: float = 16.0
+    nond_AC: float = 0.125
+    e: float = 0.1
+    cauchy: float = 0.1
+    zeta: float = 0.25
+    lam: float = 1e8
+    cfl: float = 0.1
+    kill_width: int = 3
+
+    @property
+    def omega(self):
+        return 2 * np.pi * self.freq
+
+    @property
+    def U0(self):
+        return self.e * self.r_ball * self.omega
+
+    @property
+    def nu(self):
+        Rs = (self.e / self.nond_AC) ** 2
+        return self.e * self.U0 * self.r_ball / Rs
+
+    @property
+    def G(self):
+        return self.e * self.rho_f * (self.r_ball * self.omega) ** 2 / self.cauchy
+
+    @property
+    def moll_zone(self):
+        return self.dx * 2
+
+    @property
+    def extrap_zone(self):
+        return self.moll_zone + 4 * self.dx
 
 
 def grid(nz, nr, dx):
@@ -204,3 +255,156 @@ class SoftSphereSimulation:
     def run(self, n):
         for _ in range(n):
             self.step()
+
+
+# state words of the device-resident soft loop (include/axisym_gb300.h AXI_SOFT_*)
+SOFT_T, SOFT_DT, SOFT_STEPS, SOFT_STATUS, SOFT_SWEEPS, SOFT_WORDS = 0, 1, 2, 3, 4, 8
+
+
+class SoftSphereEngine:
+    """The soft-sphere loop of SoftSphereSimulation with the time step and
+    the simulated time resident on the device: a kernel reduces
+    max(|u_z| + |u_r|) into dt, the dt- and t-dependent kernels read it
+    there, and no step reads anything back to the host, so a run of steps can
+    be captured in a CUDA graph (capture / replay). The arithmetic is that of
+    the drop-in kernels, with sin and cos of omega t taken on the device.
+    Extrapolation failures set bits of status() instead of raising."""
+
+    def __init__(self, case, device="cuda"):
+        from . import _native as N
+        from .core.extrapolate_using_least_squares import MAX_SWEEPS
+        self._N = N
+        self.max_sweeps = MAX_SWEEPS
+        self.sim = s = SoftSphereSimulation(case, device=device)
+        self.case = c = case
+        self.device = torch.device(device)
+        nr, nz = c.nr, c.nz
+        f64 = dict(dtype=torch.float64, device=self.device)
+        self.state = torch.zeros(SOFT_WORDS, **f64)
+        self.inside = torch.zeros((nr, nz), dtype=torch.uint8, device=self.device)
+        self.flags = torch.zeros((2, 2 * nr, nz), dtype=torch.int16, device=self.device)
+        self.lsq_work = torch.zeros(int(N.lib().axi_lsq_work_bytes(2 * nr, nz)),
+                                    dtype=torch.uint8, device=self.device)
+        self.scratch2 = torch.zeros(2 * nr * nz, **f64)
+        dx = c.dx
+        self.dt_elastic = c.cfl * dx / math.sqrt(c.G / c.rho_f)
+        self.cfl_dx = c.cfl * dx
+        self.dt_diffusive = 0.9 * dx ** 2 / 4 / c.nu
+        self.graph = None
+
+    # the launch groups of one step, in order (timed one at a time by phase())
+    PARTS = ("solve_velocity_dt", "advect_pin_mask", "extrapolate", "solid_stress",
+             "tether_penalise_diffuse")
+
+    def _part(self, k, st):
+        N, s, c = self._N, self.sim, self.case
+        p = N.ptr
+        nr, nz, dx = c.nr, c.nz, c.dx
+        n = nr * nz
+        w = s.vorticity
+        if k == 0:
+            N.call("axi_kill_boundary_vorticity_sine_z_f64", p(w), p(s.Z), nr, nz, c.kill_width,
+                   dx, st)
+            N.call("axi_kill_boundary_vorticity_sine_r_f64", p(w), p(s.R), nr, nz, c.kill_width,
+                   dx, st)
+            s.solver.solve(s.psi, w)
+            N.call("axi_velocity_from_psi_unb_f64", p(s.u_z), p(s.u_r), p(s.psi), p(s.R), nr, nz,
+                   dx, st)
+            N.call("axi_soft_dt_f64", p(s.u_z), p(s.u_r), n, p(self.state), self.dt_elastic,
+                   self.cfl_dx, self.dt_diffusive, EPS, st)
+        elif k == 1:
+            N.call("axi_soft_advect_eno3_f64", p(s.eta1), p(s.eta2), 1, p(s.u_z), p(s.u_r),
+                   p(self.scratch2), nr, nz, dx, p(self.state), st)
+            N.call("axi_soft_pin_level_set_f64", p(s.ball_phi), p(s.eta1), p(s.eta2), n, c.z_cm,
+                   c.r_ball, -3 * dx, st)
+            N.call("axi_soft_advect_eno3_f64", p(w), None, 0, p(s.u_z), p(s.u_r),
+                   p(self.scratch2), nr, nz, dx, p(self.state), st)
+            N.call("axi_soft_mask_f64", p(s.ball_char_func), p(self.inside), p(s.ball_phi), n,
+                   c.moll_zone, st)
+        elif k == 2:
+            N.call("axi_soft_extrapolate_eta_f64", p(self.inside), p(s.ball_phi), p(s.eta1),
+                   p(s.eta2), p(s.phi_d), p(s.e1_d), p(s.e2_d), p(self.flags[0]),
+                   p(self.flags[1]), float(c.extrap_zone), nr, nz, p(s.z), p(s.z),
+                   self.max_sweeps, p(self.lsq_work), p(self.state), st)
+        elif k == 3:
+            N.call("axi_solid_sigma_f64", p(s.s11), p(s.s12), p(s.s22), c.G, dx, p(s.eta1),
+                   p(s.eta2), p(s.e1z), p(s.e1r), p(s.e2z), p(s.e2r), nr, nz, st)
+            N.call("axi_soft_stress_mask_f64", p(s.s11), p(s.s12), p(s.s22),
+                   p(s.ball_char_func), n, st)
+            N.call("axi_soft_update_vorticity_from_solid_stress_f64", p(w), p(s.tau_z),
+                   p(s.tau_r), p(s.s11), p(s.s12), p(s.s22), p(s.R), nr, nz, dx, p(self.state),
+                   st)
+        else:
+            N.call("axi_soft_tether_f64", p(s.tether_char_func), p(s.Z), p(s.R), n,
+                   p(self.state), c.z_cm, c.e * c.r_ball, c.omega, c.zeta * c.r_ball,
+                   c.moll_zone, st)
+            N.call("axi_soft_penalise_f64", p(w), p(s.u_z), p(s.u_r), p(s.tether_char_func),
+                   p(s.u_z_upen), p(s.u_r_upen), nr, nz, dx, c.lam, c.U0, c.omega,
+                   p(self.state), st)
+            N.call("axi_soft_diffusion_rk2_f64", p(w), p(s.tmp), p(s.R), nr, nz, c.nu, dx,
+                   p(self.state), st)
+            N.call("axi_soft_advance_f64", p(self.state), st)
+
+    def _launch(self, stream):
+        st = ctypes.c_void_p(stream.cuda_stream)
+        for k in range(len(self.PARTS)):
+            self._part(k, st)
+
+    def phase(self, k, stream=None):
+        """Run launch group k of a step (PARTS); all groups in order = one step."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(s):
+            self._part(k, ctypes.c_void_p(s.cuda_stream))
+
+    # kernel launches of one step: kill (2), solve (4 products), velocity,
+    # dt, eta advection, pin, omega advection, mask, extrapolation (prepare,
+    # collect, 8 multi-block sweeps of 3 launches, the single-block finisher,
+    # fold, copy back), stress, stress mask, div tau + curl (2), tether,
+    # penalise (2), diffusion (2), advance
+    LAUNCHES_PER_STEP = (2 + 4 + 1 + 1 + 1 + 1 + 1 + 1 + (2 + 3 * 8 + 3) + 1 + 1 + 2 + 1 + 2
+                         + 2 + 1)
+
+    def step(self, n=1, stream=None):
+        """Advance n steps (asynchronous on `stream`, default torch's current)."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(s):
+            for _ in range(n):
+                self._launch(s)
+
+    def capture(self, steps_per_replay=1):
+        """Capture `steps_per_replay` steps into a CUDA graph (replay with replay())."""
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.step(steps_per_replay, stream=s)
+        torch.cuda.synchronize(self.device)
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()
+
+    @property
+    def t(self):
+        return float(self.state[SOFT_T])
+
+    @property
+    def dt(self):
+        return float(self.state[SOFT_DT])
+
+    @property
+    def steps(self):
+        return int(self.state[SOFT_STEPS])
+
+    def status(self):
+        """Sticky status bits (1 << AXI_ERR_*; 0 = healthy)."""
+        return int(self.state[SOFT_STATUS:SOFT_STATUS + 1].cpu().numpy().view(np.uint64)[0])
+
+    # the fields, as SoftSphereSimulation names them
+    def __getattr__(self, name):
+        sim = self.__dict__.get("sim")
+        if sim is not None and hasattr(sim, name):
+            return getattr(sim, name)
+        raise AttributeError(name)
