@@ -51,17 +51,17 @@ PHASE_FIELDS = {"vel_max": 1, "penalise": 6, "advect_diffuse": 4}
 PHASE_FIELDS_F64 = {"vel_max": 1, "penalise": 6, "advect_diffuse": 5}
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum per launch of a phase, from the
-# ncu captures summarised in profiles/ (transform: sum over its four products).
-# DRAM bytes (read + write) per launch of each step kernel, ensemble64 FP32
-# engine, from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum,
-# averaged over the launches of three steps)
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of each step
+# kernel's launches in one step (the z transforms and the radial products: both
+# launches together), ensemble64 FP32 engine, from the ncu capture summarised
+# in profiles/dram_traffic_ensemble64.md
 NCU_TRAFFIC = {
-    ("ensemble64", "f32", "r_products"): 193.4e6,
-    ("ensemble64", "f32", "z_transforms"): 178.7e6,
-    ("ensemble64", "f32", "advect_diffuse"): 325.6e6,
-    ("ensemble64", "f32", "penalise"): 389.4e6,
+    ("ensemble64", "f32", "kill"): 5.9e6,
+    ("ensemble64", "f32", "z_transforms"): 641.7e6,
+    ("ensemble64", "f32", "r_products"): 586.4e6,
     ("ensemble64", "f32", "vel_max"): 74.0e6,
+    ("ensemble64", "f32", "penalise"): 482.4e6,
+    ("ensemble64", "f32", "advect_diffuse"): 335.0e6,
 }
 # remeshing (2048 x 1024 cells, 4.19 M particles): FP64 instructions per
 # particle of the two kernels together (80 + 48) and their DRAM bytes per call
@@ -581,7 +581,7 @@ def run_gb300(args, world, rank, local):
     # DRAM bytes (read + write) of the dominant kernel's launches in one step,
     # from the ncu capture summarised in profiles/ (same workload and kernels)
     roof["traffic"] = NCU_TRAFFIC.get((args.workload, args.precision, dom))
-    roof["traffic_unit"] = "bytes per launch (ncu dram read + write)"
+    roof["traffic_unit"] = "bytes per step of the kernel's launches (ncu dram read + write)"
     stencil_bytes = sum(sum(PHASE_FIELDS.values()) * esize * c.nr * c.nz for c in cases)
     stencil_ms = sum(ph_ms[p] for p in PHASE_FIELDS)
     line = {
