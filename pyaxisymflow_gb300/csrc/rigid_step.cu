@@ -865,6 +865,71 @@ __device__ __forceinline__ T face_flux(T fm1, T f0, T f1, T f2, T um1, T u0, T u
   }
 }
 
+// FP32 engine: the ENO3 flux divergence F(i+1/2) - F(i-1/2) of one direction
+// formed from differences of neighbouring flux values instead of the two face
+// values. Each face value is its upwind cell's flux value g = f u plus a
+// small correction, (1/3)(g1 - g0) - (1/6)(gm1 - g0) for the branch u0 > -u1
+// and (1/3)(g0 - g1) - (1/6)(g2 - g1) otherwise (the same weights 1/3, 5/6,
+// -1/6), so the divergence is a combination of the four differences
+// d_k = g(k+1) - g(k) around the cell. With g an exact product pair and each
+// difference taken pairwise, the rounding of the result scales with the
+// differences, not with |g|: the face values of a smooth field no longer
+// cancel in float.
+struct GPair {
+  float h, l;
+};
+__device__ __forceinline__ GPair gprod(float f, float u) {
+  GPair g;
+  g.h = __fmul_rn(f, u);
+  g.l = fmaf(f, u, -g.h);
+  return g;
+}
+// g(b) - g(a)
+__device__ __forceinline__ float gdiff(GPair a, GPair b) {
+  return __fadd_rn(__fsub_rn(b.h, a.h), __fsub_rn(b.l, a.l));
+}
+// d0 = g(i-1) - g(i-2), d1 = g(i) - g(i-1), d2 = g(i+1) - g(i), d3 = g(i+2) - g(i+1);
+// af, ab: the upwind tests of the faces i+1/2 (u_i > -u_{i+1}) and i-1/2
+__device__ __forceinline__ float eno3_div(float d0, float d1, float d2, float d3, bool af,
+                                          bool ab) {
+  const float third = 1.0f / 3.0f, sixth = 1.0f / 6.0f;
+  const float cf = af ? fmaf(third, d2, __fmul_rn(sixth, d1))
+                      : -fmaf(third, d2, __fmul_rn(sixth, d3));
+  const float cb = ab ? fmaf(third, d1, __fmul_rn(sixth, d0))
+                      : -fmaf(third, d1, __fmul_rn(sixth, d2));
+  // upwind cells of the two faces: (i, i-1) -> d1, (i, i) -> 0,
+  // (i+1, i-1) -> d1 + d2, (i+1, i) -> d2
+  const float base = af ? (ab ? d1 : 0.0f) : (ab ? __fadd_rn(d1, d2) : d2);
+  return __fsub_rn(__fadd_rn(base, cf), cb);
+}
+// divergence along a line of five values f, u at stride `st` around c
+__device__ __forceinline__ float eno3_div_at(const float* f, const float* u, int c, int st) {
+  const GPair gm2 = gprod(f[c - 2 * st], u[c - 2 * st]), gm1 = gprod(f[c - st], u[c - st]);
+  const GPair g0 = gprod(f[c], u[c]), g1 = gprod(f[c + st], u[c + st]);
+  const GPair g2 = gprod(f[c + 2 * st], u[c + 2 * st]);
+  return eno3_div(gdiff(gm2, gm1), gdiff(gm1, g0), gdiff(g0, g1), gdiff(g1, g2),
+                  u[c] > -u[c + st], u[c - st] > -u[c]);
+}
+// the advected value f0 + a (Dx + Dy)
+__device__ __forceinline__ float eno3_update(float f0, float a, float dxv, float dyv) {
+  return __fadd_rn(f0, __fadd_rn(__fmul_rn(a, dxv), __fmul_rn(a, dyv)));
+}
+
+// RK2 operator at one cell (kernels/diffusion_RK2.py:15-25). The FP64 engine
+// keeps the reference's expression; the FP32 engine sums the four neighbour
+// differences (exact for neighbouring values within a factor 2) instead of
+// n + s + e + w - 4 c, whose float rounding scales with |c|.
+template <typename T>
+__device__ __forceinline__ T rk2_lap(T n, T s, T e, T w, T c, T inv_dx2, T k1, T k2) {
+  if constexpr (sizeof(T) == 4) {
+    const T ns = __fadd_rn(__fsub_rn(n, c), __fsub_rn(s, c));
+    const T ew = __fadd_rn(__fsub_rn(e, c), __fsub_rn(w, c));
+    return __fmul_rn(__fadd_rn(ns, ew), inv_dx2) + (n - s) * k1 - c * k2;
+  } else {
+    return (n + s + e + w - T(4) * c) * inv_dx2 + (n - s) * k1 - c * k2;
+  }
+}
+
 // Smoothed Heaviside of a sphere level set (kernels/smooth_Heaviside.py:10-14,
 // level set of falling_rigid_sphere.py:156).
 template <typename T>
@@ -952,6 +1017,11 @@ __device__ __forceinline__ T advect_point(const T* sw, const T* sz, const T* sr,
   if (!(gi >= 0 && gi < nr && gj >= 0 && gj < nz)) return T(0);
   const int c = ad_box(p, q);
   const T f0 = sw[c];
+  if constexpr (sizeof(T) == 4) {
+    if (gi < nr - 2 && gj >= 2 && gj < nz - 2)
+      return eno3_update(f0, a, eno3_div_at(sw, sz, c, 1), eno3_div_at(sw, sr, c, BOXW));
+    return f0;
+  }
   T flux = T(0);
   if (gi < nr - 2 && gj >= 2 && gj < nz - 2) {
     const int L = BOXW;
@@ -1053,7 +1123,53 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) advect_diffuse_ker
     const int gjm = j0 + qm;
     constexpr int L = BOXW;
     // ---- advected omega on the tile + halo 2: rows -2..TY+1, columns -2..TX+1
-    {
+    if constexpr (sizeof(T) == 4) {
+      // FP32: the r-direction flux values of the window rows ride along as
+      // exact pairs with their differences (one new product and one new
+      // difference per row)
+      const bool jin = gjm < nz, jflux = gjm >= 2 && gjm < nz - 2;
+      const int p0 = -2 + AD_RA * grp;
+      int c = ad_box(p0, qm);
+      const GPair gm2 = gprod(sw[c - 2 * L], sr[c - 2 * L]);
+      const GPair gm1 = gprod(sw[c - L], sr[c - L]);
+      const GPair g0 = gprod(sw[c], sr[c]);
+      GPair g1 = gprod(sw[c + L], sr[c + L]);
+      float d0 = gdiff(gm2, gm1), d1 = gdiff(gm1, g0), d2 = gdiff(g0, g1);
+      float f0 = sw[c], f1 = sw[c + L], u0 = sr[c], u1 = sr[c + L];
+      bool ab = sr[c - L] > -u0;
+#pragma unroll 1
+      for (int m = 0; m < AD_RA; ++m, c += L) {
+        const int pr = p0 + m, gi = i0 + pr;
+        const float f2 = sw[c + 2 * L], u2 = sr[c + 2 * L];
+        const GPair g2 = gprod(f2, u2);
+        const float d3 = gdiff(g1, g2);
+        const bool af = u0 > -u1;
+        float val = 0.0f;
+        if (jin && gi >= 0 && gi < nr) {
+          val = f0;
+          // pystencils ghost layers: no flux in the last two rows and the
+          // first and last two columns
+          if (jflux && gi < nr - 2)
+            val = eno3_update(f0, a, eno3_div_at(sw, sz, c, 1), eno3_div(d0, d1, d2, d3, af, ab));
+        }
+        wa[ad_wa(pr, qm)] = val;
+        d0 = d1;
+        d1 = d2;
+        d2 = d3;
+        g1 = g2;
+        ab = af;
+        f0 = f1;
+        f1 = f2;
+        u0 = u1;
+        u1 = u2;
+      }
+      // halo columns -2, -1, TX, TX + 1
+      if (threadIdx.x < 4 * AD_AH) {
+        const int pr = -2 + (int)threadIdx.x / 4, s4 = threadIdx.x % 4;
+        const int qe = s4 < 2 ? s4 - 2 : TX + s4 - 2;
+        wa[ad_wa(pr, qe)] = advect_point<T>(sw, sz, sr, pr, qe, i0 + pr, j0 + qe, nr, nz, a);
+      }
+    } else {
       const bool jin = gjm < nz, jflux = gjm >= 2 && gjm < nz - 2;
       const int p0 = -2 + AD_RA * grp;
       int c = ad_box(p0, qm);
@@ -1061,23 +1177,11 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) advect_diffuse_ker
       T fm2 = sw[c - 2 * L], fm1 = sw[c - L], f0 = sw[c], f1 = sw[c + L];
       T um2 = sr[c - 2 * L], um1 = sr[c - L], u0 = sr[c], u1 = sr[c + L];
       T yb = face_flux(fm2, fm1, f0, f1, um2, um1, u0, u1);
-      // FP32: the flux values of the window rows carried along (one new
-      // product per row); unused, and removed, in the FP64 engine
-      T gm1 = fm1 * um1, g0 = f0 * u0, g1 = f1 * u1;
 #pragma unroll 1
       for (int m = 0; m < AD_RA; ++m, c += L) {
         const int pr = p0 + m, gi = i0 + pr;
         const T f2 = sw[c + 2 * L], u2 = sr[c + 2 * L];
-        T yf;
-        if constexpr (sizeof(T) == 4) {
-          const T g2 = f2 * u2;
-          yf = face_flux_g(gm1, g0, g1, g2, u0, u1);
-          gm1 = g0;
-          g0 = g1;
-          g1 = g2;
-        } else {
-          yf = face_flux(fm1, f0, f1, f2, um1, u0, u1, u2);
-        }
+        const T yf = face_flux(fm1, f0, f1, f2, um1, u0, u1, u2);
         T val = T(0);
         if (jin && gi >= 0 && gi < nr) {
           T flux = T(0);
@@ -1131,8 +1235,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) advect_diffuse_ker
           tmpv = c_;
           if (jint && gi >= 1 && gi < nr - 1) {
             const T ee = wa[d + 1], ww = wa[d - 1];
-            const T lap = (n_ + s_ + ee + ww - T(4) * c_) * inv_dx2 +
-                          (n_ - s_) * rowf[0][pr + 1] - c_ * rowf[1][pr + 1];
+            const T lap = rk2_lap<T>(n_, s_, ee, ww, c_, inv_dx2, rowf[0][pr + 1],
+                                     rowf[1][pr + 1]);
             tmpv = c_ + c1 * lap;
           }
         }
@@ -1151,8 +1255,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) advect_diffuse_ker
           tmpv = c0;
           if (gi >= 1 && gi < nr - 1 && gj >= 1 && gj < nz - 1) {
             const T n = wa[e + AD_AW], s = wa[e - AD_AW], ee = wa[e + 1], ww = wa[e - 1];
-            const T lap = (n + s + ee + ww - T(4) * c0) * inv_dx2 + (n - s) * rowf[0][pr + 1] -
-                          c0 * rowf[1][pr + 1];
+            const T lap = rk2_lap<T>(n, s, ee, ww, c0, inv_dx2, rowf[0][pr + 1],
+                                     rowf[1][pr + 1]);
             tmpv = c0 + c1 * lap;
           }
         }
@@ -1210,8 +1314,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) advect_diffuse_ker
           T v = wa[ad_wa(pr, qm)];
           if (jint && gi >= 1 && gi < nr - 1) {
             const T ee = tp[d + 1], ww = tp[d - 1];
-            const T lap = (n_ + s_ + ee + ww - T(4) * c_) * inv_dx2 +
-                          (n_ - s_) * rowf[0][pr + 1] - c_ * rowf[1][pr + 1];
+            const T lap = rk2_lap<T>(n_, s_, ee, ww, c_, inv_dx2, rowf[0][pr + 1],
+                                     rowf[1][pr + 1]);
             v = v + c2 * lap;
           }
           wout[c] = v;
