@@ -380,16 +380,16 @@ int axi_add_f32_to_f64(double* y, const float* x, int64_t n, void* stream);
 int axi_widen_f32_to_f64(double* y, const float* x, int64_t n, void* stream);
 
 /* Allocation-free form of axi_fd_transform_f64 (no counterpart in the
- * reference). For callers that cannot call cudaMalloc: code that captures its
- * time loop into a CUDA graph, or a host whose device memory is owned by
- * another allocator. The two intermediate products live in a device array
- * inside this library, sized for nr * nz <= axi_fd_transform_static_max_cells()
- * (512 x 1024 cells, 8 MiB, resident on every GPU that loads the library until
- * the process exits); larger grids are rejected with AXI_ERR_INVALID. The
- * first call on each device looks up the array's device address (with that
- * device current): make that first call before any stream capture. All calls
+ * reference). For callers that cannot call cudaMalloc: a host whose device
+ * memory is owned by another allocator. The two intermediate products live in
+ * a device array inside this library, sized for
+ * nr * nz <= axi_fd_transform_static_max_cells() (512 x 1024 cells, 8 MiB,
+ * resident on every GPU that loads the library until the process exits);
+ * larger grids are rejected with AXI_ERR_INVALID. The first call in a context
+ * looks up the array's device address (with that device current). All calls
  * share the array, so calls that overlap on the GPU (other streams, other
- * host threads) race; serialise them on one stream. Nothing is allocated. */
+ * host threads) race; serialise them on one stream. Nothing is allocated or
+ * freed. */
 int64_t axi_fd_transform_static_max_cells(void);
 int axi_fd_transform_static_f64(double* out, int ld_out, const double* in, int ld_in,
                                 const double* Er_inv_w, const double* EzinvT,

@@ -35,10 +35,9 @@ extern "C" int axi_fd_transform_f64(double* out, int ld_out, const double* in, i
 // ---------------------------------------------------------------------------
 // Allocation-free variant of axi_fd_transform_f64.
 //
-// Some callers cannot call cudaMalloc: a host that captures its whole time
-// loop into a CUDA graph (allocation is not allowed while a stream is being
-// captured), or a host whose device memory belongs to another allocator that
-// has already reserved it, so this library may not ask the driver for more.
+// Some callers cannot call cudaMalloc: a host whose device memory belongs to
+// another allocator that has already reserved it, so this library may not ask
+// the driver for more.
 // For them the two intermediate (nr, nz) products live in this file-scope
 // device array instead of caller-provided scratch. It holds
 // AXI_FD_STATIC_MAX_CELLS cells per product and stays resident on every GPU

@@ -1,9 +1,8 @@
 """The allocation-free spectral transform against the scratch-taking one.
 
-axi_fd_transform_static_f64 serves callers that may not call cudaMalloc
-(a time loop captured into a CUDA graph, or a host whose device memory is
-owned by another allocator): its intermediate products live in a fixed device
-array inside the library. Both entry points are called through the C ABI on
+axi_fd_transform_static_f64 serves callers that may not call cudaMalloc (a
+host whose device memory is owned by another allocator): its intermediate
+products live in a fixed device array inside the library. Both entry points are called through the C ABI on
 the same operands; the results must agree to the spectral-solve tolerance of
 the other GPU tests, on two calls in a row (the second call reuses the array
 the first one left behind). Named so that pytest collects it last.
@@ -41,11 +40,17 @@ def test_static_scratch_transform_matches_scratch_taking_transform():
         N.check(lib.axi_fd_transform_f64(N.ptr(ref), nz, N.ptr(rhs), nz, N.ptr(d["Er_inv_w"]),
                                          N.ptr(d["EzinvT"]), N.ptr(d["inv_eig"]), N.ptr(d["Er"]),
                                          N.ptr(d["EzT"]), N.ptr(work), nr, nz, s))
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         N.check(lib.axi_fd_transform_static_f64(N.ptr(out), nz, N.ptr(rhs), nz,
                                                 N.ptr(d["Er_inv_w"]), N.ptr(d["EzinvT"]),
                                                 N.ptr(d["inv_eig"]), N.ptr(d["Er"]),
                                                 N.ptr(d["EzT"]), nr, nz, s))
         torch.cuda.synchronize()
+        if call == 1:
+            # the second call (the module is loaded by the first): no device
+            # memory taken or given back
+            assert torch.cuda.mem_get_info()[0] == free_before
         assert torch.isfinite(out).all()
         assert rel_l2(out, ref) < SOLVE_RTOL, (call, rel_l2(out, ref))
 
