@@ -103,43 +103,62 @@ class ClockSampler:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, interval_ms=50):
         self.gpu = gpu_index
+        self.interval_ms = interval_ms
         self.samples = []
-        self._stop = threading.Event()
+        self._proc = None
+        self.t0 = self.t1 = 0.0
         self._thread = threading.Thread(target=self._run, daemon=True)
 
     def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", f"--id={self.gpu}",
-                                      f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits"],
-                                     capture_output=True, text=True, timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([x.strip() for x in out.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        # one nvidia-smi process sampling every interval_ms (a new process per
+        # sample takes longer than the interval)
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", f"-lms={self.interval_ms}"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            for line in self._proc.stdout:
+                line = line.strip()
+                if line:
+                    self.samples.append((time.perf_counter(), [x.strip() for x in line.split(",")]))
+        except Exception:
+            pass
 
     def __enter__(self):
         self._thread.start()
+        time.sleep(0.2)  # let the sampler start before the timed region
+        self.t0 = time.perf_counter()
         return self
 
     def __exit__(self, *exc):
-        self._stop.set()
+        self.t1 = time.perf_counter()
+        time.sleep(2 * self.interval_ms / 1000.0)
+        if self._proc is not None:
+            self._proc.terminate()  # the process this sampler started
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
         self._thread.join(timeout=10)
 
     def summary(self):
-        if not self.samples:
+        """Median SM clock and the throttle reasons of the samples taken while
+        the timed region ran (all samples when none fell inside it)."""
+        inside = [f for t, f in self.samples
+                  if self.t0 <= t <= self.t1 + self.interval_ms / 1000.0]
+        picked = inside or [f for _, f in self.samples]
+        if not picked:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        sm = [float(s[1]) for s in picked if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in picked if s[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for s in self.samples for k in range(4)
+        reasons = sorted({names[k] for s in picked for k in range(4)
                           if len(s) > 5 + k and s[5 + k].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(self.samples)}
+                "samples": len(picked), "interval_ms": self.interval_ms}
 
 
 def dist_setup(args):
@@ -853,6 +872,26 @@ def run_soft(args, world, rank, local):
         "clocks": clocks.summary(),
         "status_ok": status == 0,
     }
+    # the same loop with the z products of the solve as FP64 DCTs (psi within
+    # ~1e-11 of the dense eigenvector products)
+    del eng
+    torch.cuda.empty_cache()
+    eng2 = SoftSphereEngine(case, device=dev, dct=True)
+    eng2.capture(1)
+    for _ in range(args.warmup):
+        eng2.replay()
+    torch.cuda.synchronize(dev)
+    d0 = torch.cuda.Event(enable_timing=True)
+    d1 = torch.cuda.Event(enable_timing=True)
+    d0.record(stream)
+    for _ in range(args.steps):
+        eng2.replay()
+    d1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms2 = d0.elapsed_time(d1) / args.steps
+    line["dct_variant"] = {"value": cells * world / (ms2 / 1e3), "ms_per_step": ms2,
+                           "speedup_over_dense": ms / ms2, "status_ok": eng2.status() == 0,
+                           "z_transform": "FP64 DCT-II / DCT-III rows, dense radial products"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = soft_cpu_record(case, seconds=12.0)
     if rank == 0:

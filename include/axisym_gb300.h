@@ -669,6 +669,23 @@ int axi_soft_diffusion_rk2_f64(double* vort, double* tmp, const double* R, int n
 /* t += dt, steps += 1 (:270-272). */
 int axi_soft_advance_f64(double* state, void* stream);
 
+/* ---------------------------------------------------------------------
+ * Orthonormal FP64 DCT-II / DCT-III along the rows of a (rows, N) array, for
+ * a spectral solve outside the rigid engine whose z operator is the Neumann
+ * Laplacian (kernels/FastDiagonalisationStokesSolver.py:41-97): E_z^-1 x is
+ * the DCT-II of each row, E_z y the DCT-III (no counterpart in the
+ * reference, which multiplies by the dense eigenvector matrices). N even with
+ * factors 2 and 3 only, N <= 2048. table: the double tables of the z
+ * transform as axi_case.dct_table describes them (6 N doubles).
+ * axi_dct64_plan_f64 fills a caller-allocated device plan
+ * (axi_dct64_plan_bytes) for fixed in / out arrays and synchronises the
+ * stream; axi_dct64_run_f64 transforms with it (no host data: capturable).
+ * ------------------------------------------------------------------ */
+int64_t axi_dct64_plan_bytes(int rows, int N);
+int axi_dct64_plan_f64(const double* in, double* out, int rows, int N, const double* table,
+                       int forward, void* plan_dev, void* stream);
+int axi_dct64_run_f64(const void* plan_dev, int rows, int N, int forward, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -91,6 +91,9 @@ def _signatures():
         "axi_soft_penalise_f64": (I, [P, P, P, P, P, P, I, I, D, D, D, D, P, P]),
         "axi_soft_diffusion_rk2_f64": (I, [P, P, P, I, I, D, D, P, P]),
         "axi_soft_advance_f64": (I, [P, P]),
+        "axi_dct64_plan_bytes": (I64, [I, I]),
+        "axi_dct64_plan_f64": (I, [P, P, I, I, P, I, P, P]),
+        "axi_dct64_run_f64": (I, [P, I, I, I, P]),
     }
     for s in ("f64", "f32"):
         T = _real(s)

@@ -1,5 +1,7 @@
 // Grouped orthonormal DCT-II / DCT-III along rows in double (see dct64.cuh).
+#include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "dct64.cuh"
 
@@ -175,3 +177,74 @@ int launch(const Job* jobs_dev, const int4* items_dev, int n_items, bool forward
 }
 
 }  // namespace axi_dct64
+
+// ---------------------------------------------------------------------------
+// Standalone FP64 row transforms for callers outside the rigid engine's plan
+// (the soft-sphere engine's spectral solve). A plan is one device buffer: the
+// Job record, then one work item per group of rows; it fixes the input and
+// output arrays, so a step can launch it with no host data (and inside a CUDA
+// graph). Tables: the double layout of the engine's dct_table (twiddles,
+// rotations, c_k, 1 / c_k).
+// ---------------------------------------------------------------------------
+namespace {
+constexpr size_t JOB_BYTES = (sizeof(axi_dct64::Job) + 15) & ~size_t(15);
+inline int items_of(int rows, int N) {
+  const int r = axi_dct64::rows_per_item(N);
+  return (rows + r - 1) / r;
+}
+}  // namespace
+
+extern "C" int64_t axi_dct64_plan_bytes(int rows, int N) {
+  if (rows < 1 || N < 2) return 0;
+  return (int64_t)(JOB_BYTES + (size_t)items_of(rows, N) * sizeof(int4));
+}
+
+extern "C" int axi_dct64_plan_f64(const double* in, double* out, int rows, int N,
+                                  const double* table, int forward, void* plan_dev,
+                                  void* stream) {
+  axi::clear_error();
+  const char* what = "dct64_plan";
+  AXI_TRY(axi::check_ptr(what, in, "in"));
+  AXI_TRY(axi::check_ptr(what, out, "out"));
+  AXI_TRY(axi::check_ptr(what, table, "table"));
+  AXI_TRY(axi::check_ptr(what, plan_dev, "plan"));
+  axi_dct64::Job j;
+  memset(&j, 0, sizeof(j));
+  if (rows < 1 || !axi_dct64::plan_radices(N, j.radix, &j.nstages)) {
+    axi::set_error("%s: %d rows of length %d have no double DCT plan (N even, factors 2 and 3 "
+                   "only, <= %d)", what, rows, N, axi_dct64::ELEMS);
+    return AXI_ERR_INVALID;
+  }
+  j.N = N;
+  j.rows = rows;
+  j.in = in;
+  j.out = out;
+  j.twiddle = reinterpret_cast<const double2*>(table);
+  j.rot = reinterpret_cast<const double2*>(table + (size_t)2 * N);
+  j.scale = table + (size_t)(forward ? 4 : 5) * N;
+  const int n_items = items_of(rows, N);
+  std::vector<unsigned char> buf(JOB_BYTES + (size_t)n_items * sizeof(int4), 0);
+  memcpy(buf.data(), &j, sizeof(j));
+  int4* items = reinterpret_cast<int4*>(buf.data() + JOB_BYTES);
+  const int r = axi_dct64::rows_per_item(N);
+  for (int q = 0; q < n_items; ++q) items[q] = make_int4(0, q * r, 0, 0);
+  cudaStream_t s = axi::as_stream(stream);
+  if (cudaMemcpyAsync(plan_dev, buf.data(), buf.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return axi::launch_status(what);
+  return AXI_OK;
+}
+
+extern "C" int axi_dct64_run_f64(const void* plan_dev, int rows, int N, int forward,
+                                 void* stream) {
+  axi::clear_error();
+  AXI_TRY(axi::check_ptr("dct64_run", plan_dev, "plan"));
+  if (rows < 1 || N < 2) {
+    axi::set_error("dct64_run: invalid size %d x %d", rows, N);
+    return AXI_ERR_INVALID;
+  }
+  const unsigned char* base = static_cast<const unsigned char*>(plan_dev);
+  return axi_dct64::launch(reinterpret_cast<const axi_dct64::Job*>(base),
+                           reinterpret_cast<const int4*>(base + JOB_BYTES), items_of(rows, N),
+                           forward != 0, axi::as_stream(stream));
+}

@@ -270,7 +270,7 @@ class SoftSphereEngine:
     the drop-in kernels, with sin and cos of omega t taken on the device.
     Extrapolation failures set bits of status() instead of raising."""
 
-    def __init__(self, case, device="cuda"):
+    def __init__(self, case, device="cuda", dct=False):
         from . import _native as N
         from .core.extrapolate_using_least_squares import MAX_SWEEPS
         self._N = N
@@ -278,6 +278,7 @@ class SoftSphereEngine:
         self.sim = s = SoftSphereSimulation(case, device=device)
         self.case = c = case
         self.device = torch.device(device)
+        self.dct = bool(dct)
         nr, nz = c.nr, c.nz
         f64 = dict(dtype=torch.float64, device=self.device)
         self.state = torch.zeros(SOFT_WORDS, **f64)
@@ -286,11 +287,57 @@ class SoftSphereEngine:
         self.lsq_work = torch.zeros(int(N.lib().axi_lsq_work_bytes(2 * nr, nz)),
                                     dtype=torch.uint8, device=self.device)
         self.scratch2 = torch.zeros(2 * nr * nz, **f64)
+        if self.dct:
+            self._setup_dct()
         dx = c.dx
         self.dt_elastic = c.cfl * dx / math.sqrt(c.G / c.rho_f)
         self.cfl_dx = c.cfl * dx
         self.dt_diffusive = 0.9 * dx ** 2 / 4 / c.nu
         self.graph = None
+
+    def _setup_dct(self):
+        """The spectral solve with the z products as FP64 DCT-II / DCT-III row
+        transforms (the Neumann z operator is diagonal in the cosine basis;
+        psi does not depend on which eigenbasis diagonalises it): E_z^-1 and
+        E_z become O(nz log nz) per row, the radial products stay dense. psi
+        differs from the dense eigenvector products by ~1e-12 of a solve."""
+        from .engine import dct_ok, dct_table
+        N, s, c = self._N, self.sim, self.case
+        nr, nz, dx = c.nr, c.nz, c.dx
+        if not dct_ok(nz, "f64"):
+            raise ValueError(f"nz = {nz} has no FP64 DCT plan (even, factors 2 and 3 only, "
+                             "<= 2048)")
+        eng = s.solver.engine
+        f64 = dict(dtype=torch.float64, device=self.device)
+        lam_z = (2.0 - 2.0 * np.cos(np.pi * np.arange(nz) / nz)) / (dx * dx)
+        self.inv_eig_dct = torch.tensor(1.0 / (eng.eig_vals_r.reshape(nr, 1)
+                                               + lam_z.reshape(1, nz)), **f64)
+        self.dct_tab = torch.tensor(dct_table(nz, np.float64), **f64)
+        self.w1 = torch.zeros((nr, nz), **f64)
+        self.w2 = torch.zeros((nr, nz), **f64)
+        nb = int(N.lib().axi_dct64_plan_bytes(nr, nz))
+        self.plan_fwd = torch.zeros(nb, dtype=torch.uint8, device=self.device)
+        self.plan_inv = torch.zeros(nb, dtype=torch.uint8, device=self.device)
+        st = N.stream_of(self.w1)
+        N.call("axi_dct64_plan_f64", N.ptr(s.vorticity), N.ptr(self.w1), nr, nz,
+               N.ptr(self.dct_tab), 1, N.ptr(self.plan_fwd), st)
+        N.call("axi_dct64_plan_f64", N.ptr(self.w2), N.ptr(self.w1), nr, nz,
+               N.ptr(self.dct_tab), 0, N.ptr(self.plan_inv), st)
+
+    def _solve(self, st):
+        N, s, c = self._N, self.sim, self.case
+        if not self.dct:
+            s.solver.solve(s.psi, s.vorticity)
+            return
+        p = N.ptr
+        nr, nz = c.nr, c.nz
+        d = s.solver.engine.dev
+        N.call("axi_dct64_run_f64", p(self.plan_fwd), nr, nz, 1, st)
+        N.call("axi_dgemm_f64", p(self.w2), nz, p(d["Er_inv_w"]), nr, p(self.w1), nz,
+               p(self.inv_eig_dct), nr, nz, nr, st)
+        N.call("axi_dct64_run_f64", p(self.plan_inv), nr, nz, 0, st)
+        N.call("axi_dgemm_f64", p(s.psi), nz, p(d["Er"]), nr, p(self.w1), nz, None, nr, nz,
+               nr, st)
 
     # the launch groups of one step, in order (timed one at a time by phase())
     PARTS = ("solve_velocity_dt", "advect_pin_mask", "extrapolate", "solid_stress",
@@ -307,7 +354,7 @@ class SoftSphereEngine:
                    dx, st)
             N.call("axi_kill_boundary_vorticity_sine_r_f64", p(w), p(s.R), nr, nz, c.kill_width,
                    dx, st)
-            s.solver.solve(s.psi, w)
+            self._solve(st)
             N.call("axi_velocity_from_psi_unb_f64", p(s.u_z), p(s.u_r), p(s.psi), p(s.R), nr, nz,
                    dx, st)
             N.call("axi_soft_dt_f64", p(s.u_z), p(s.u_r), n, p(self.state), self.dt_elastic,

@@ -157,6 +157,18 @@ def test_config2_soft_sphere_1024x512_50_steps():
         assert abs(s.t - st.t) <= 1e-13 * st.t
     print("config 2, rel L2 vs oracle (GPU, oracle one-ulp control):", report)
     assert runs["engine"].status() == 0
+    # the engine with the z products of the solve as FP64 DCTs (exact cosine
+    # basis instead of LAPACK's eigenvectors): 2e-11, as the rigid FP64 DCT
+    # engine (measured: omega 5.1e-13, eta 3.0e-13, psi 9.4e-12)
+    e = SoftSphereEngine(case, device="cuda", dct=True)
+    e.step(steps)
+    torch.cuda.synchronize()
+    for f, t, ref in (("omega", e.vorticity, st.vorticity), ("eta1", e.eta1, st.eta1),
+                      ("eta2", e.eta2, st.eta2), ("phi", e.ball_phi, st.ball_phi),
+                      ("psi", e.psi, st.psi)):
+        err = rel_l2(t.cpu().numpy(), ref)
+        assert err < 2e-11, ("dct", f, err)
+    assert e.status() == 0
 
 
 def test_config3_periodic_poisson_2048x1024():

@@ -67,3 +67,20 @@ def test_graph_replay_is_bit_identical():
         assert torch.equal(getattr(a, f), getattr(b, f)), f
     assert torch.equal(a.state, b.state)
     assert b.steps == 6 and b.status() == 0 and float(b.state[4]) >= 1
+
+
+def test_engine_fp64_dct_solve():
+    """The z products of the solve as FP64 DCTs: the cosine basis
+    diagonalises the Neumann z operator exactly, LAPACK's eigenvectors to
+    ~1e-12, so the two solves differ at that level (psi most)."""
+    from pyaxisymflow_gb300.simulation import SoftSphereEngine
+    case = golden_case()
+    dense = SoftSphereEngine(case, device="cuda")
+    dct = SoftSphereEngine(case, device="cuda", dct=True)
+    dense.step(12)
+    dct.step(12)
+    torch.cuda.synchronize()
+    for f in FIELDS:
+        err = rel_l2(getattr(dct, f).cpu().numpy(), getattr(dense, f).cpu().numpy())
+        assert err < 2e-11, (f, err)
+    assert dct.status() == 0 and dct.steps == 12
