@@ -1041,8 +1041,10 @@ __device__ __forceinline__ T advect_point(const T* sw, const T* sz, const T* sr,
   return f0 + flux;
 }
 
+// FP32: 4 resident blocks per SM (up to 64 registers; at 5 blocks the
+// pairwise flux divergence spilled and ran 5 % slower)
 template <typename T>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) advect_diffuse_kernel(const axi_case* __restrict__ cases,
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) advect_diffuse_kernel(const axi_case* __restrict__ cases,
                                                             const int4* __restrict__ tiles,
                                                             int n_tiles,
                                                             const CUtensorMap* __restrict__ maps,
