@@ -554,7 +554,10 @@ __device__ __forceinline__ void residual_pair_to_buf(const DctJob& job, int ga, 
   const float k2a = has_a ? job.inv_2dx * job.rinv2[ga] : 0.0f;
   const float k1b = has_b ? job.two_over_dx * job.rinv2dx[gb] : 0.0f;
   const float k2b = (has_b && gb + 1 < nr) ? job.inv_2dx * job.rinv2[gb] : 0.0f;
-#pragma unroll 1
+  // two float4 groups per iteration: the loads of the second are in flight
+  // while the first is formed (0.247 -> 0.239 ms for the two transforms;
+  // four groups were no faster)
+#pragma unroll 2
   for (int m = 0; m < NV; ++m) {
     const int p = 4 * (lane + 32 * m);
     float4 xa = zero, xb = zero;
