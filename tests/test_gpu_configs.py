@@ -62,12 +62,13 @@ def test_config1_rigid_sphere_512x256_1000_steps():
         assert abs(e.state[0, 2].item() - st.Cd) <= 1e-10 * abs(st.Cd)
 
 
-@pytest.mark.parametrize("index", [14, 49])
+@pytest.mark.parametrize("index", [14, 9, 37, 49])
 def test_config4_sedimenting_sphere_200_steps(index):
-    """Config 4: a freely sedimenting sphere of the seeded 64-case ensemble
-    (case 14: 256 x 128, Re 301, radius 0.043; case 49: 1024 x 512, Re 871,
-    radius 0.093), 200 steps, FP64 engine against the oracle: fields, body
-    position and velocity."""
+    """Config 4: freely sedimenting spheres of the seeded 64-case ensemble, one
+    per grid size (case 14: 256 x 128, Re 301, radius 0.043; case 9: 512 x 256,
+    Re 755, radius 0.087; case 37: 768 x 384, Re 622, radius 0.118; case 49:
+    1024 x 512, Re 871, radius 0.093), 200 steps, FP64 engine against the
+    oracle: fields, body position and velocity."""
     import bench
     from pyaxisymflow_gb300.engine import ST_UBODY, ST_ZCM, RigidEnsemble
     c = bench.ensemble_cases("ensemble64")[index]
