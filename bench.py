@@ -57,11 +57,11 @@ PHASE_FIELDS_F64 = {"vel_max": 1, "penalise": 6, "advect_diffuse": 5}
 # in profiles/dram_traffic_ensemble64.md
 NCU_TRAFFIC = {
     ("ensemble64", "f32", "kill"): 5.9e6,
-    ("ensemble64", "f32", "z_transforms"): 641.7e6,
+    ("ensemble64", "f32", "z_transforms"): 641.2e6,
     ("ensemble64", "f32", "r_products"): 586.4e6,
     ("ensemble64", "f32", "vel_max"): 74.0e6,
-    ("ensemble64", "f32", "penalise"): 482.4e6,
-    ("ensemble64", "f32", "advect_diffuse"): 335.0e6,
+    ("ensemble64", "f32", "penalise"): 482.9e6,
+    ("ensemble64", "f32", "advect_diffuse"): 333.0e6,
 }
 # remeshing (2048 x 1024 cells, 4.19 M particles): FP64 instructions per
 # particle of the two kernels together (80 + 48) and their DRAM bytes per call
