@@ -1,7 +1,7 @@
 """FP32 spectral solves on the tcgen05 tensor cores (3xTF32) with one step of
 iterative refinement (FP64 residual), against the FP64 oracle.
 
-The survey's isolated-Poisson configuration: periodic z, Neumann r, a seeded
+The isolated Poisson configuration: periodic z, Neumann r, a seeded
 sum of 32 axisymmetric Gaussian vortex rings as right-hand side; errors of psi
 and of the velocity derived from it are relative L2 against FP64.
 """
