@@ -325,3 +325,35 @@ def test_engine_refined_solve_matches_fp64_solve():
     print("psi rel L2 vs the FP64 solve of the same vorticity:", errs)
     assert errs[True] < 1e-7, errs
     assert errs[True] < errs[False], errs
+
+
+def test_engine_f32_drift_after_2000_steps_on_the_hardest_cases():
+    """The FP32 engine (DCT z transforms, tcgen05 radial products, one
+    refinement step per solve) against the FP64 engine (within 1e-12 of the
+    oracle) after config 4's 2000 steps, on the two ensemble cases with the
+    largest vorticity drift (case 9: 512 x 256, Re 755; case 14: 256 x 128,
+    Re 301): psi and velocity within 1e-5, vorticity within 2e-5 (measured
+    1.15e-5 and 9.5e-6; a float-sized change of the sphere radius moves the
+    FP64 vorticity by 5e-6 over the same steps)."""
+    import bench
+    from pyaxisymflow_gb300.engine import RigidEnsemble
+    cases = bench.ensemble_cases("ensemble64")
+    sel = [cases[9], cases[14]]
+    w0 = [c.noise * np.random.default_rng(c.seed).standard_normal((c.nr, c.nz)) for c in sel]
+    a = RigidEnsemble(sel, precision="f64", initial_vorticity=w0)
+    b = RigidEnsemble(sel, precision="f32", initial_vorticity=w0)
+    assert b.refine and b.dct and b.tensor_cores
+    a.step(2000)
+    b.step(2000)
+    torch.cuda.synchronize()
+    assert not a.status().any() and not b.status().any()
+    for k in range(len(sel)):
+        fa, fb = a.fields[k], b.fields[k]
+        errs = {}
+        for n in ("omega", "psi", "u_z", "u_r"):
+            ref = fa[n].double()
+            got = fb[n].double()
+            if n == "psi":
+                got = got + fb["psi_lo"].double()
+            errs[n] = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+        assert errs["omega"] < 2e-5 and max(errs["psi"], errs["u_z"], errs["u_r"]) < 1e-5, errs
