@@ -294,14 +294,10 @@ constexpr int MB_SWEEPS = 8;
 void issue_sweeps(int16_t* cf, const int16_t* tf, double* ex, double* ey, const double* gx,
                   const double* gy, int n0, int n1, int max_sweeps, LsqHeader* hdr,
                   const int* list, int4* front, cudaStream_t s) {
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
-  const int blocks = 2 * sms;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = 2 * (sms > 0 ? sms : 1);
   for (int k = 0; k < MB_SWEEPS; ++k) {
     const int parity = k & 1;
     lsq_scan_mb_kernel<<<blocks, 256, 0, s>>>(cf, tf, n0, n1, hdr, list, front, parity);
