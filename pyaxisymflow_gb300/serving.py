@@ -100,6 +100,14 @@ class SimulationServer:
         self.budget = hbm_budget * total
         self.keep_vorticity = keep_vorticity
         self.depth = max(1, int(depth))
+        # pinned rows for the state blocks of retiring cases, used round robin:
+        # a row is read back within `depth` steps, and at most `capacity` cases
+        # retire per step, so (depth + 2) * capacity rows are never overwritten
+        # before they are read
+        self._rows = torch.empty(((self.depth + 2) * capacity,
+                                  self.ens.state_arena.shape[1]), dtype=torch.float64,
+                                 pin_memory=True)
+        self._next_row = 0
 
     def prepare(self, cases):
         """Build the spectral bases of every grid size in `cases` ahead of time
@@ -204,8 +212,8 @@ class SimulationServer:
                     done.append(m)
             for m in done:
                 req, steps, admitted_at = active.pop(m)
-                state_host = torch.empty(ens.state_arena.shape[1], dtype=torch.float64,
-                                         pin_memory=True)
+                state_host = self._rows[self._next_row]
+                self._next_row = (self._next_row + 1) % self._rows.shape[0]
                 state_host.copy_(ens.state_arena[m.slot], non_blocking=True)
                 vort = m.fields["omega"].detach().clone() if self.keep_vorticity else None
                 fin.append((req, admitted_at, state_host, vort))
