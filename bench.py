@@ -363,8 +363,19 @@ def fp32_accuracy(cases, dev, steps):
     last = str(steps)
     summary = {name: {n: max(r[name][last][n] for r in per_case) for n in fields}
                for name in runs}
+    # the same error over all cells of the selected cases together
+    agg = {}
+    for name, sn in runs.items():
+        a, _ = sn[steps]
+        b, _ = ref[steps]
+        agg[name] = {n: float(np.sqrt(sum(float(torch.linalg.norm(a[q][n] - b[q][n])) ** 2
+                                          for q in range(len(sel)))
+                                      / sum(float(torch.linalg.norm(b[q][n])) ** 2
+                                            for q in range(len(sel)))))
+                     for n in fields}
     return {"steps": steps, "checkpoints": checkpoints, "cases": idx,
-            "max_rel_l2_at_end": summary, "per_case": per_case}
+            "max_rel_l2_at_end": summary, "rel_l2_over_all_selected_cells_at_end": agg,
+            "per_case": per_case}
 
 
 def run_reference(args, world, rank):
