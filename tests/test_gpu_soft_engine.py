@@ -84,3 +84,22 @@ def test_engine_fp64_dct_solve():
         err = rel_l2(getattr(dct, f).cpu().numpy(), getattr(dense, f).cpu().numpy())
         assert err < 2e-11, (f, err)
     assert dct.status() == 0 and dct.steps == 12
+
+
+def test_extrapolation_failure_sets_a_status_bit():
+    """An extrapolation that needs more sweeps than allowed fails with
+    AXI_ERR_NOT_CONVERGED; the device loop records it in its status word
+    instead of raising (it never reads back mid-step), and the sweep count
+    reaches the cap plus one, as the single-block loop counts it."""
+    from pyaxisymflow_gb300 import _native as N
+    from pyaxisymflow_gb300.simulation import SOFT_SWEEPS, SoftSphereEngine
+    case = golden_case()
+    ok = SoftSphereEngine(case, device="cuda")
+    capped = SoftSphereEngine(case, device="cuda")
+    capped.max_sweeps = 2
+    ok.step(2)
+    capped.step(2)
+    torch.cuda.synchronize()
+    assert ok.status() == 0 and float(ok.state[SOFT_SWEEPS]) > 3
+    assert capped.status() & (1 << N.AXI_ERR_NOT_CONVERGED)
+    assert float(capped.state[SOFT_SWEEPS]) == 3
