@@ -496,31 +496,40 @@ def run_gb300(args, world, rank, local):
     uses_refine = ens.refine
     # ---- end to end through the public API with host buffers ------------------
     # every case's vorticity in pinned host memory; each step copies it in,
-    # advances every case and copies it and the state blocks (dt, Cd) back,
-    # with the transfers of 4 case groups overlapped with their computation
-    pipe = HostPipeline(cases, groups=4, precision=args.precision, device=dev, **zopt)
+    # advances every case and copies it and the state blocks (dt, Cd) back.
+    # The cases run as groups (--e2e-groups), each step of a group one CUDA graph on the
+    # group's stream (its H2D copy, its launches, its D2H copies), so the
+    # transfers of one group overlap the computation of the others, within a
+    # step and across steps; the host reads each step's state blocks (two
+    # pinned buffers in turn) while the next step runs.
+    pipe = HostPipeline(cases, groups=args.e2e_groups, precision=args.precision, device=dev,
+                        **zopt)
     if not args.no_tune:
         for sub in pipe.ensembles:
             tuner.tune(sub)
     host_w = pipe.host_buffer()
-    host_state = torch.empty((len(cases), ST_WORDS), dtype=torch.float64, pin_memory=True)
+    host_states = [torch.empty((len(cases), ST_WORDS), dtype=torch.float64, pin_memory=True)
+                   for _ in range(2)]
     for _ in range(2):
-        pipe.step(host_w, host_state)
+        pipe.step(host_w, host_states[0])
         pipe.synchronize()
-    # every group's copies and launches of one step issued as one CUDA graph
-    pipe.capture(host_w, host_state)
-    for _ in range(2):
-        pipe.replay()
-        pipe.synchronize()
+    pipe.capture_pipelined(host_w, host_states)
+    for k in range(2):
+        pipe.replay_step(k)
+        pipe.wait_step(k)
     field_bytes = host_w.numel() * host_w.element_size()
     h2d = field_bytes
-    d2h = field_bytes + host_state.numel() * 8
+    d2h = field_bytes + host_states[0].numel() * 8
     barrier(world)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        pipe.replay()
-        pipe.synchronize()
-        _ = float(host_state[0, ST_CD]) + float(host_state[0, ST_DT])
+    for k in range(args.steps):
+        pipe.replay_step(k)
+        if k:
+            hs = host_states[pipe.wait_step(k - 1)]
+            _ = float(hs[0, ST_CD]) + float(hs[0, ST_DT])
+    hs = host_states[pipe.wait_step(args.steps - 1)]
+    _ = float(hs[0, ST_CD]) + float(hs[0, ST_DT])
+    pipe.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_s = max_over_ranks(world, e2e_s)
     e2e_value = cells * world / e2e_s
@@ -636,7 +645,8 @@ def run_gb300(args, world, rank, local):
         "tuning": tuning,
         "stencil_hbm_gbs": stencil_bytes / (stencil_ms / 1000.0) / 1e9,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h, "groups": len(pipe.ensembles),
+                "pipelined": "per-group step graphs, state read one step behind"},
         "gpu_launches": None,
         "clocks": clocks.summary(),
         "status_ok": bool(np.all(status == 0)),
@@ -1136,6 +1146,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the FP32-vs-FP64 comparison over --accuracy-steps steps")
     ap.add_argument("--accuracy-steps", type=int, default=2000)
+    ap.add_argument("--e2e-groups", type=int, default=2,
+                    help="case groups of the end-to-end host pipeline")
     ap.add_argument("--z-transform", default="default", choices=["default", "dense", "dct"],
                     help="FP32 engine: z products as dense tensor-core GEMMs or as DCTs")
     args = ap.parse_args()

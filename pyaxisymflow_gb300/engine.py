@@ -647,23 +647,28 @@ class HostPipeline:
             h[a:b].copy_(e.omega_arena)
         return h
 
+    def _group_step(self, g, host, state_out, s):
+        """Group g's step on stream s: its vorticity in, one step, vorticity
+        and state blocks out."""
+        e = self.ensembles[g]
+        a, b = self.offsets[g], self.offsets[g + 1]
+        with torch.cuda.stream(s):
+            e.load_vorticity(host[a:b], stream=s)
+            e.step(1, stream=s)
+            e.store_vorticity(host[a:b], stream=s)
+            if state_out is not None:
+                row = sum(len(idx) for idx in self.index[:g])
+                state_out[row:row + e.n_cases].copy_(e.state, non_blocking=True)
+
     def step(self, host, state_out=None):
         """One step of every case: host vorticity in, step, host vorticity out.
         Asynchronous; call synchronize() before reading `host`. state_out
         (pinned, one row of AXI_ST_WORDS per case, groups in order) receives
         each case's state block."""
         cur = torch.cuda.current_stream(self.device)
-        row = 0
-        for e, s, a, b in zip(self.ensembles, self.streams, self.offsets, self.offsets[1:]):
+        for g, s in enumerate(self.streams):
             s.wait_stream(cur)
-            with torch.cuda.stream(s):
-                e.load_vorticity(host[a:b], stream=s)
-                e.step(1, stream=s)
-                e.store_vorticity(host[a:b], stream=s)
-                if state_out is not None:
-                    n = e.n_cases
-                    state_out[row:row + n].copy_(e.state, non_blocking=True)
-                    row += n
+            self._group_step(g, host, state_out, s)
         for s in self.streams:
             cur.wait_stream(s)
 
@@ -686,6 +691,51 @@ class HostPipeline:
     def replay(self):
         """One captured step (asynchronous on the current stream)."""
         self.graph.replay()
+
+    def capture_pipelined(self, host, state_outs):
+        """Record each group's step as a CUDA graph of its own, once per host
+        state buffer in `state_outs` (steps take the buffers in turn), for
+        replay_step / wait_step. A group's step then follows only its own
+        previous step on its stream: while the last groups of step k still
+        compute, the first groups already copy in and advance step k + 1, so
+        the copies and the steps of successive steps overlap. The graphs hold
+        the buffers' addresses: host and state_outs must stay alive and in
+        place while they are used."""
+        torch.cuda.synchronize(self.device)
+        graphs = []
+        for st in state_outs:
+            row = []
+            for g, s in enumerate(self.streams):
+                gr = torch.cuda.CUDAGraph()
+                with torch.cuda.stream(s):
+                    with torch.cuda.graph(gr, stream=s):
+                        self._group_step(g, host, st, s)
+                row.append(gr)
+            graphs.append(row)
+        torch.cuda.synchronize(self.device)
+        self.step_graphs = graphs
+        self.step_done = [[torch.cuda.Event() for _ in self.streams] for _ in state_outs]
+        self._pipelined_buffers = (host, list(state_outs))
+
+    def replay_step(self, k):
+        """Issue step k (asynchronous): every group's graph on its own stream.
+        Its state blocks go to state_outs[k % len(state_outs)]; before step
+        k + len(state_outs) is issued, wait_step(k) must have returned and the
+        caller must be done reading that buffer."""
+        p = k % len(self.step_graphs)
+        for gr, s, ev in zip(self.step_graphs[p], self.streams, self.step_done[p]):
+            with torch.cuda.stream(s):
+                gr.replay()
+                ev.record(s)
+        return p
+
+    def wait_step(self, k):
+        """Block until step k's copies to the host are complete; returns the
+        index of the state buffer that holds its state blocks."""
+        p = k % len(self.step_graphs)
+        for ev in self.step_done[p]:
+            ev.synchronize()
+        return p
 
     def synchronize(self):
         for s in self.streams:

@@ -171,6 +171,46 @@ def test_host_pipeline_matches_single_ensemble(precision):
             row += 1
 
 
+def test_host_pipeline_pipelined_steps_match_single_ensemble():
+    """Per-group step graphs replayed without a barrier between steps (a
+    group's next step follows only its own previous one), the host reading
+    each step's state blocks one step behind: every case ends where one
+    ensemble does, and each step's state blocks are that step's."""
+    from pyaxisymflow_gb300.engine import ST_T, ST_WORDS, HostPipeline, RigidBodyCase, \
+        RigidEnsemble
+    cases = [RigidBodyCase(nz=64 * (1 + k % 3), nr=32 * (1 + k % 3), dx=2.0 / (64 * (1 + k % 3)),
+                           r_sphere=0.125, seed=20 + k) for k in range(7)]
+    pipe = HostPipeline(cases, groups=3, precision="f32")
+    ref = RigidEnsemble(cases, precision="f32")
+    host = pipe.host_buffer()
+    states = [torch.empty((len(cases), ST_WORDS), dtype=torch.float64, pin_memory=True)
+              for _ in range(2)]
+    pipe.capture_pipelined(host, states)
+    order = [k for idx in pipe.index for k in idx]
+    steps = 6
+    seen = []
+    for k in range(steps):
+        pipe.replay_step(k)
+        if k:
+            seen.append(states[pipe.wait_step(k - 1)].clone())
+    seen.append(states[pipe.wait_step(steps - 1)].clone())
+    pipe.synchronize()
+    for k in range(steps):
+        ref.step(1)
+        want = ref.state.cpu()
+        for row, c in enumerate(order):
+            assert torch.equal(seen[k][row], want[c]), (k, c)
+    row = 0
+    for g, idx in enumerate(pipe.index):
+        a = pipe.offsets[g]
+        for c in idx:
+            n = cases[c].nr * cases[c].nz
+            assert torch.equal(host[a:a + n].view(cases[c].nr, cases[c].nz),
+                               ref.fields[c]["omega"].cpu()), c
+            a += n
+    assert float(seen[-1][0, ST_T]) > float(seen[0][0, ST_T])
+
+
 def test_engine_dct_z_transform_tracks_fp64():
     """The FP32 engine with the z products as DCTs (dct=True) against the
     FP64 engine, and no worse than the dense tensor-core form."""
