@@ -52,16 +52,16 @@ PHASE_FIELDS_F64 = {"vel_max": 1, "penalise": 6, "advect_diffuse": 5}
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of each step
-# kernel's launches in one step (the z transforms and the radial products: both
-# launches together), ensemble64 FP32 engine, from the ncu capture summarised
-# in profiles/dram_traffic_ensemble64.md
+# kernel's launches in one step (both plan groups; the z transforms and the
+# radial products: both launches of each group together), ensemble64 FP32
+# engine, from the ncu capture summarised in profiles/dram_traffic_ensemble64.md
 NCU_TRAFFIC = {
     ("ensemble64", "f32", "kill"): 5.9e6,
-    ("ensemble64", "f32", "z_transforms"): 641.2e6,
-    ("ensemble64", "f32", "r_products"): 586.4e6,
+    ("ensemble64", "f32", "z_transforms"): 461.1e6,
+    ("ensemble64", "f32", "r_products"): 523.9e6,
     ("ensemble64", "f32", "vel_max"): 74.0e6,
-    ("ensemble64", "f32", "penalise"): 482.9e6,
-    ("ensemble64", "f32", "advect_diffuse"): 333.0e6,
+    ("ensemble64", "f32", "penalise"): 444.4e6,
+    ("ensemble64", "f32", "advect_diffuse"): 295.7e6,
 }
 # remeshing (2048 x 1024 cells, 4.19 M particles): FP64 instructions per
 # particle of the two kernels together (80 + 48) and their DRAM bytes per call
@@ -268,24 +268,6 @@ def cpu_baseline_record(cases):
     }
 
 
-def phase_times(ens, stream, n):
-    """Mean device time (ms) of each phase of a step, CUDA events on `stream`."""
-    import torch
-    out = {p: 0.0 for p in PHASES}
-    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-            for _ in PHASES] for _ in range(n)]
-    for s in range(n):
-        for k, _ in enumerate(PHASES):
-            evs[s][k][0].record(stream)
-            ens.phase(k)
-            evs[s][k][1].record(stream)
-    torch.cuda.synchronize()
-    for s in range(n):
-        for k, p in enumerate(PHASES):
-            out[p] += evs[s][k][0].elapsed_time(evs[s][k][1]) / n
-    return out
-
-
 def accuracy_cases(cases):
     """Indices of the hardest cases of the seeded ensemble per grid size: the
     highest Reynolds number and the smallest sphere."""
@@ -422,6 +404,42 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def phase_times(ens, ids, rounds, stream):
+    """Device time (ms) of each phase in `ids` over all cases, as it runs in a
+    step: each phase captured as a CUDA graph of its own (the plan groups'
+    launches on forked streams, as in the step graph), `rounds` rounds of the
+    phases in order replayed behind a backlog of whole steps, so the host
+    never leaves the device idle between the events. Runs the phases (the
+    cases advance)."""
+    import torch
+    dev = ens.device
+    graphs = []
+    torch.cuda.synchronize(dev)
+    for ph in ids:
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(dev)
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                ens.phase(ph, stream=s)
+        graphs.append(g)
+    torch.cuda.synchronize(dev)
+    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            for _ in ids] for _ in range(rounds)]
+    if ens.graph is not None:
+        for _ in range(5):
+            ens.replay()
+    else:
+        ens.step(1)
+    for r in range(rounds):
+        for q, g in enumerate(graphs):
+            evs[r][q][0].record(stream)
+            g.replay()
+            evs[r][q][1].record(stream)
+    torch.cuda.synchronize(dev)
+    return [sum(evs[r][q][0].elapsed_time(evs[r][q][1]) for r in range(rounds)) / rounds
+            for q in range(len(ids))]
+
+
 def run_gb300(args, world, rank, local):
     import torch
     from pyaxisymflow_gb300 import _native
@@ -464,34 +482,16 @@ def run_gb300(args, world, rank, local):
     ms_per_step = ms / args.steps
     value = cells * world / (ms_per_step / 1000.0)
     status = ens.status()
+    n_plans = ens.n_plans
     uses_tc = ens.tensor_cores
     # ---- per-phase device times (same stream, same step sequence) -------------
     ph_ms = {p: 0.0 for p in PHASES}
     nph = max(3, min(args.steps, 10))
-    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-            for _ in PHASES] for _ in range(nph)]
-    for s in range(nph):
-        for k, p in enumerate(PHASES):
-            evs[s][k][0].record(stream)
-            ens.phase(k)
-            evs[s][k][1].record(stream)
-    torch.cuda.synchronize(dev)
-    for s in range(nph):
-        for k, p in enumerate(PHASES):
-            ph_ms[p] += evs[s][k][0].elapsed_time(evs[s][k][1]) / nph
+    ph_list = phase_times(ens, list(range(len(PHASES))), nph, stream)
+    for k, p in enumerate(PHASES):
+        ph_ms[p] = ph_list[k]
     # the four launches of the transform one at a time (phase ids 5..8)
-    part_ms = [0.0] * 4
-    pev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-            for _ in range(4)] for _ in range(nph)]
-    for s in range(nph):
-        for q in range(4):
-            pev[s][q][0].record(stream)
-            ens.phase(5 + q)
-            pev[s][q][1].record(stream)
-    torch.cuda.synchronize(dev)
-    for s in range(nph):
-        for q in range(4):
-            part_ms[q] += pev[s][q][0].elapsed_time(pev[s][q][1]) / nph
+    part_ms = phase_times(ens, [5, 6, 7, 8], nph, stream)
     uses_dct = ens.dct
     uses_refine = ens.refine
     # ---- end to end through the public API with host buffers ------------------
@@ -557,7 +557,7 @@ def run_gb300(args, world, rank, local):
             if dct:
                 # per-phase device times of the FP64 step, and its stencil passes'
                 # algorithmic bytes (FP64 fields) over their time
-                p64 = phase_times(e64, stream, 3)
+                p64 = dict(zip(PHASES, phase_times(e64, list(range(len(PHASES))), 3, stream)))
                 entry["phase_ms"] = p64
                 b64 = sum(sum(PHASE_FIELDS_F64.values()) * 8 * c.nr * c.nz for c in cases)
                 entry["stencil_hbm_gbs"] = b64 / (sum(p64[p] for p in PHASE_FIELDS_F64)
@@ -652,9 +652,11 @@ def run_gb300(args, world, rank, local):
         "status_ok": bool(np.all(status == 0)),
     }
     # kill_reset, 4 spectral products (2 transforms + 2 products on the DCT
-    # path), vel_max (which also computes dt), penalise, advect_diffuse
-    n_launch = 1 + 4 + 3
+    # path), vel_max (which also computes dt), penalise, advect_diffuse; per
+    # plan group
+    n_launch = (1 + 4 + 3) * n_plans
     line["gpu_launches"] = n_launch * args.steps
+    line["config"]["plan_groups"] = n_plans
     # ---- continuous-batching serving leg (config 5) ----------------------------
     # (a failure of a secondary leg is recorded in the line, not allowed to
     # lose the measurement above)

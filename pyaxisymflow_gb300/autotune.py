@@ -3,7 +3,8 @@
 The reference specialises its pystencils kernels per grid at generation time
 (pyst_kernels/advection_flux.py:9-21: fixed_grid_size, num_threads); here the
 kernels are compiled once, and what depends on the mix of grid sizes in an
-ensemble is how the work is scheduled: how many blocks of each stencil kernel
+ensemble is how the work is scheduled: into how many plans the cases are
+split (each stepped on a stream of its own), how many blocks of each stencil kernel
 stay resident per SM, how far ahead they prefetch their tiles into L2, how
 many persistent CTAs run the tensor-core products and in which order they
 take their tiles, and in which order the z-transform items run. Every choice
@@ -30,6 +31,7 @@ CANDIDATES = {
     "vel_max_blocks": (0, 2, 4),
     "penalise_blocks": (0, 2, 3),
     "advect_blocks": (0, 2, 3),
+    "plan_groups": (0, 1, 2, 3),
 }
 
 
@@ -47,6 +49,8 @@ def mix_key(ens):
 def applicable(ens, name):
     if name in ("tc_ctas_percent", "tc_tile_order"):
         return ens.tensor_cores
+    if name == "plan_groups":
+        return ens.n_cases > 1
     if name == "dct_item_order":
         return ens.dct and ens.tensor_cores
     return True

@@ -142,9 +142,12 @@ class AxiTuning(ctypes.Structure):
                 ("reserved", ctypes.c_int32)]
 
 
-# names of the launch choices (keys of RigidEnsemble.tuning)
+# names of the launch choices (keys of RigidEnsemble.tuning); plan_groups is
+# the host's (how many plans the cases are split into, each stepped on a
+# stream of its own: 0 automatic, see RigidEnsemble.plan_group_count), the
+# others go to the plan (axi_tuning)
 TUNING_KEYS = ("vel_max_blocks", "penalise_blocks", "advect_blocks", "prefetch_waves",
-               "tc_ctas_percent", "tc_tile_order", "dct_item_order")
+               "tc_ctas_percent", "tc_tile_order", "dct_item_order", "plan_groups")
 
 
 def fill_tuning(tune, choices):
@@ -340,9 +343,34 @@ class CaseState:
         return n
 
 
+def split_by_cells(cases, groups):
+    """Indices of `cases` in `groups` parts of about equal cell count (greedy,
+    largest case first), each part in input order; empty parts dropped."""
+    groups = max(1, min(groups, len(cases)))
+    order = sorted(range(len(cases)), key=lambda k: -cases[k].nr * cases[k].nz)
+    load = [0] * groups
+    parts = [[] for _ in range(groups)]
+    for k in order:
+        g = load.index(min(load))
+        parts[g].append(k)
+        load[g] += cases[k].nr * cases[k].nz
+    return [sorted(p) for p in parts if p]
+
+
 class RigidEnsemble:
     """Cases resident on one GPU, advanced together by one launch sequence per
-    step. Cases may join (add_case) and leave (remove_case) between steps."""
+    step. Cases may join (add_case) and leave (remove_case) between steps.
+
+    The cases may be split into plan groups (launch choice plan_groups), each
+    with a plan of its own; a step then forks one stream per group from the
+    caller's stream and joins them again, so the kernels of one group fill
+    the other's drain and fill bubbles between kernels (the 64-case bench
+    workload: 0.808 ms per step as one plan, 0.769 ms as two, 0.788 as
+    three). Each case's arithmetic does not depend on the grouping."""
+
+    # plan groups of the automatic choice, and the fewest cases it splits
+    AUTO_PLAN_GROUPS = 2
+    AUTO_SPLIT_MIN_CASES = 8
 
     def __init__(self, cases, precision="f64", device="cuda", history_steps=0,
                  initial_vorticity=None, tensor_cores=None, capacity=None, dct=None,
@@ -384,6 +412,8 @@ class RigidEnsemble:
         self._omega_arena = None
         self.graph = None
         self.tuning = {}
+        self.plans = []
+        self._streams = []
         lib = N.lib()
         self._step_fn = getattr(lib, f"axi_rigid_step_{precision}")
         self._phase_fn = getattr(lib, f"axi_rigid_phase_{precision}")
@@ -444,9 +474,7 @@ class RigidEnsemble:
             self._pack_vorticity()
         else:
             self._omega_arena = None
-        self.structs = (AxiCase * max(n, 1))()
-        for k, m in enumerate(self.members):
-            self.structs[k] = m.struct
+        self.plans = []
         self.info = AxiPlanInfo()
         fill_tuning(self.info.tune, self.tuning)
         if n == 0:
@@ -457,14 +485,40 @@ class RigidEnsemble:
         esize = 8 if self.precision == "f64" else 4
         flags = ((PLAN_TENSOR_CORES if self.tensor_cores else 0) | (PLAN_DCT_Z if self.dct else 0)
                  | (PLAN_REFINE if self.refine else 0))
-        N.check(lib.axi_plan_init(ctypes.addressof(self.structs), n, esize, flags,
-                                  ctypes.byref(self.info)), "plan_init")
-        self.n_tiles = self.info.n_stencil_tiles
-        self.plan = torch.empty(int(self.info.bytes), dtype=torch.uint8, device=self.device)
-        N.check(lib.axi_plan_upload(ctypes.addressof(self.structs), ctypes.byref(self.info),
-                                    ctypes.c_void_p(self.plan.data_ptr()),
-                                    ctypes.c_void_p(torch.cuda.current_stream(
-                                        self.device).cuda_stream)), "plan_upload")
+        stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        for idx in split_by_cells(self.cases, self.plan_group_count(n)):
+            structs = (AxiCase * len(idx))()
+            for q, k in enumerate(idx):
+                structs[q] = self.members[k].struct
+            info = AxiPlanInfo()
+            fill_tuning(info.tune, self.tuning)
+            N.check(lib.axi_plan_init(ctypes.addressof(structs), len(idx), esize, flags,
+                                      ctypes.byref(info)), "plan_init")
+            plan = torch.empty(int(info.bytes), dtype=torch.uint8, device=self.device)
+            N.check(lib.axi_plan_upload(ctypes.addressof(structs), ctypes.byref(info),
+                                        ctypes.c_void_p(plan.data_ptr()), stream), "plan_upload")
+            self.plans.append((info, plan, structs, idx))
+        self.info, self.plan = self.plans[0][0], self.plans[0][1]
+        self.n_tiles = sum(p[0].n_stencil_tiles for p in self.plans)
+
+    def plan_group_count(self, n=None):
+        """Plan groups for n cases (default: the members): the plan_groups
+        launch choice, or when it is 0 (automatic) AUTO_PLAN_GROUPS once there
+        are AUTO_SPLIT_MIN_CASES cases, else one."""
+        n = len(self.members) if n is None else n
+        g = int(self.tuning.get("plan_groups", 0))
+        if g <= 0:
+            g = self.AUTO_PLAN_GROUPS if n >= self.AUTO_SPLIT_MIN_CASES else 1
+        return max(1, min(g, n))
+
+    @property
+    def n_plans(self):
+        return len(self.plans)
+
+    def _group_streams(self):
+        while len(self._streams) < len(self.plans):
+            self._streams.append(torch.cuda.Stream(self.device))
+        return self._streams[:len(self.plans)]
 
     def set_tuning(self, choices):
         """Use the launch choices `choices` (a dict over TUNING_KEYS; missing
@@ -516,21 +570,36 @@ class RigidEnsemble:
     def cells(self):
         return sum(c.nr * c.nz for c in self.cases)
 
-    def step(self, n=1, stream=None):
-        """Advance every case by n steps (asynchronous on torch's current stream)."""
+    def _forked(self, fn, arg, what, stream):
+        """fn(info, plan, arg, stream) for every plan group: on `stream` for
+        one group, else on streams forked from it and joined back."""
         s = stream if stream is not None else torch.cuda.current_stream(self.device)
-        N.check(self._step_fn(ctypes.byref(self.info), ctypes.c_void_p(self.plan.data_ptr()),
-                              int(n), ctypes.c_void_p(s.cuda_stream)), "rigid_step")
+        if len(self.plans) == 1:
+            N.check(fn(ctypes.byref(self.info), ctypes.c_void_p(self.plan.data_ptr()), int(arg),
+                       ctypes.c_void_p(s.cuda_stream)), what)
+            return
+        streams = self._group_streams()
+        for (info, plan, _, _), gs in zip(self.plans, streams):
+            gs.wait_stream(s)
+            N.check(fn(ctypes.byref(info), ctypes.c_void_p(plan.data_ptr()), int(arg),
+                       ctypes.c_void_p(gs.cuda_stream)), what)
+        for gs in streams:
+            s.wait_stream(gs)
+
+    def step(self, n=1, stream=None):
+        """Advance every case by n steps (asynchronous on torch's current
+        stream, or `stream`). With several plan groups each group's steps run
+        on a stream forked from it and joined back before the call returns."""
+        self._forked(self._step_fn, n, "rigid_step", stream)
 
     PHASES = ("kill", "transform", "vel_max", "penalise", "advect_diffuse")
     # the four launches of "transform" (phase ids 5..8), for timing
     TRANSFORM_PARTS = ("z_forward", "r_product", "z_inverse", "r_product_2")
 
     def phase(self, ph, stream=None):
-        """Run one phase of a step (see PHASES); all six in order = one step."""
-        s = stream if stream is not None else torch.cuda.current_stream(self.device)
-        N.check(self._phase_fn(ctypes.byref(self.info), ctypes.c_void_p(self.plan.data_ptr()),
-                               int(ph), ctypes.c_void_p(s.cuda_stream)), "rigid_phase")
+        """Run one phase of a step (see PHASES); all six in order = one step.
+        The plan groups run it concurrently, as in a step (forked streams)."""
+        self._forked(self._phase_fn, ph, "rigid_phase", stream)
 
     def capture(self, steps_per_replay=1):
         """Capture `steps_per_replay` steps into a CUDA graph (replay with replay())."""
@@ -554,10 +623,10 @@ class RigidEnsemble:
         1 << AXI_ERR_CUDA."""
         st = self.state[:, ST_STATUS].cpu().numpy().view(np.uint64)
         out = (st & 0xFFFFFFFF).astype(np.int64)
-        if self.plan is not None:
+        for info, plan, _, _ in self.plans:
             err = ctypes.c_int(0)
             N.check(N.lib().axi_plan_tc_status(
-                ctypes.byref(self.info), ctypes.c_void_p(self.plan.data_ptr()),
+                ctypes.byref(info), ctypes.c_void_p(plan.data_ptr()),
                 ctypes.byref(err), ctypes.c_void_p(
                     torch.cuda.current_stream(self.device).cuda_stream)), "plan_tc_status")
             if err.value:
@@ -569,9 +638,10 @@ class RigidEnsemble:
         operand copy of omega (one launch for all cases)."""
         if self.tensor_cores:
             s = stream if stream is not None else torch.cuda.current_stream(self.device)
-            N.check(N.lib().axi_rigid_refresh_operands(
-                ctypes.byref(self.info), ctypes.c_void_p(self.plan.data_ptr()),
-                ctypes.c_void_p(s.cuda_stream)), "rigid_refresh_operands")
+            for info, plan, _, _ in self.plans:
+                N.check(N.lib().axi_rigid_refresh_operands(
+                    ctypes.byref(info), ctypes.c_void_p(plan.data_ptr()),
+                    ctypes.c_void_p(s.cuda_stream)), "rigid_refresh_operands")
 
     def load_vorticity(self, src, stream=None):
         """Replace the vorticity of every case from one flat buffer laid out like
@@ -615,16 +685,8 @@ class HostPipeline:
 
     def __init__(self, cases, groups=4, precision="f32", device="cuda", **kw):
         cases = list(cases)
-        groups = max(1, min(groups, len(cases)))
         # greedy balance by cells, keeping each group's cases in input order
-        order = sorted(range(len(cases)), key=lambda k: -cases[k].nr * cases[k].nz)
-        load = [0] * groups
-        parts = [[] for _ in range(groups)]
-        for k in order:
-            g = load.index(min(load))
-            parts[g].append(k)
-            load[g] += cases[k].nr * cases[k].nz
-        self.index = [sorted(p) for p in parts if p]
+        self.index = split_by_cells(cases, groups)
         self.device = torch.device(device)
         self.ensembles = [RigidEnsemble([cases[k] for k in idx], precision=precision,
                                         device=self.device, **kw) for idx in self.index]
