@@ -175,13 +175,17 @@ def test_host_pipeline_pipelined_steps_match_single_ensemble():
     """Per-group step graphs replayed without a barrier between steps (a
     group's next step follows only its own previous one), the host reading
     each step's state blocks one step behind: every case ends where one
-    ensemble does, and each step's state blocks are that step's."""
+    ensemble (one plan) does, and each step's state blocks are that step's."""
     from pyaxisymflow_gb300.engine import ST_T, ST_WORDS, HostPipeline, RigidBodyCase, \
         RigidEnsemble
     cases = [RigidBodyCase(nz=64 * (1 + k % 3), nr=32 * (1 + k % 3), dx=2.0 / (64 * (1 + k % 3)),
-                           r_sphere=0.125, seed=20 + k) for k in range(7)]
-    pipe = HostPipeline(cases, groups=3, precision="f32")
+                           r_sphere=0.125, seed=20 + k) for k in range(18)]
+    pipe = HostPipeline(cases, groups=2, precision="f32")
+    # each host group of 9 cases steps as two plan groups of its own: the
+    # captured group graphs hold the nested fork
+    assert all(e.n_plans == 2 for e in pipe.ensembles)
     ref = RigidEnsemble(cases, precision="f32")
+    ref.set_tuning({"plan_groups": 1})
     host = pipe.host_buffer()
     states = [torch.empty((len(cases), ST_WORDS), dtype=torch.float64, pin_memory=True)
               for _ in range(2)]
