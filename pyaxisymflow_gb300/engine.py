@@ -680,10 +680,10 @@ class HostPipeline:
     group's vorticity (load_vorticity), one step, and the D2H copy back
     (store_vorticity). Groups run concurrently, so while one group computes
     the copy engines move the next group's input and the previous group's
-    output; with capture_pipelined the steps themselves overlap as well (two
-    groups measured best on the 64-case workload, 2.27e10 cell-updates/s
-    against 2.03e10 with four). Every case's result is the same as in a
-    single RigidEnsemble.
+    output; with capture_pipelined the steps themselves overlap as well (on
+    the 64-case workload, each group one plan: 2.09e10 cell-updates/s with
+    two groups, 2.03e10 with four, 1.87e10 with eight). Every case's result
+    is the same as in a single RigidEnsemble.
     """
 
     def __init__(self, cases, groups=2, precision="f32", device="cuda", **kw):
