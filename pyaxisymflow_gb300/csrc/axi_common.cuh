@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <initializer_list>
 #include <string>
 
 #include "../../include/axisym_gb300.h"
@@ -40,6 +41,20 @@ inline int check_ptr(const char* what, const void* p, const char* name) {
   if (p == nullptr) {
     set_error("%s: %s is null", what, name);
     return AXI_ERR_INVALID;
+  }
+  return AXI_OK;
+}
+
+// Every pointer in `ptrs` non-null; `names` names them in the same order.
+inline int check_ptrs(const char* what, std::initializer_list<const void*> ptrs,
+                      std::initializer_list<const char*> names) {
+  const char* const* n = names.begin();
+  for (const void* p : ptrs) {
+    const char* name = n != names.end() ? *n++ : "pointer";
+    if (p == nullptr) {
+      set_error("%s: %s is null", what, name);
+      return AXI_ERR_INVALID;
+    }
   }
   return AXI_OK;
 }

@@ -185,7 +185,8 @@ extern "C" int axi_soft_advect_eno3_f64(double* f0, double* f1, int refmap, cons
                                         const double* u_r, double* scratch, int nr, int nz,
                                         double dx, const double* state, void* stream) {
   axi::clear_error();
-  AXI_TRY(axi::check_ptr("soft_advect_eno3", state, "state"));
+  AXI_TRY(axi::check_ptrs("soft_advect_eno3", {f0, u_z, u_r, scratch, state},
+                          {refmap ? "eta1" : "omega", "u_z", "u_r", "scratch", "state"}));
   if (refmap) {
     AXI_TRY(axi::check_ptr("soft_advect_eno3", f1, "eta2"));
     return eno3_launch<double, 2, false>(f0, f1, 1.0, -1.0, u_z, u_r, scratch, nr, nz, 0.0,

@@ -442,8 +442,12 @@ extern "C" int axi_soft_extrapolate_eta_f64(
     axi::set_error("%s: invalid grid %d x %d", what, nr, nz);
     return AXI_ERR_INVALID;
   }
-  AXI_TRY(axi::check_ptr(what, work, "work"));
-  AXI_TRY(axi::check_ptr(what, state, "state"));
+  AXI_TRY(axi::check_ptrs(what,
+                          {inside_solid, ball_phi, eta1, eta2, ball_phi_double, eta1_double,
+                           eta2_double, current_flag, target_flag, grid_x, grid_y, work, state},
+                          {"inside_solid", "ball_phi", "eta1", "eta2", "ball_phi_double",
+                           "eta1_double", "eta2_double", "current_flag", "target_flag", "grid_x",
+                           "grid_y", "work", "state"}));
   cudaStream_t s = axi::as_stream(stream);
   dim3 g2(axi::ceil_div(nz, 128), 2 * nr);
   lsq_prepare_kernel<<<g2, 128, 0, s>>>(inside_solid, ball_phi, eta1, eta2, ball_phi_double,

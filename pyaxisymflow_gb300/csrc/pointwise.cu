@@ -467,7 +467,10 @@ extern "C" int axi_soft_update_vorticity_from_solid_stress_f64(
     void* stream) {
   axi::clear_error();
   AXI_TRY(axi::check_grid("soft_update_vorticity_from_solid_stress", nr, nz));
-  AXI_TRY(axi::check_ptr("soft_update_vorticity_from_solid_stress", state, "state"));
+  AXI_TRY(axi::check_ptrs("soft_update_vorticity_from_solid_stress",
+                          {vort, tau_z, tau_r, t11, t12, t22, R, state},
+                          {"vorticity", "tau_z", "tau_r", "sigma_11", "sigma_12", "sigma_22", "R",
+                           "state"}));
   cudaStream_t s = axi::as_stream(stream);
   div_tau_kernel<double><<<grid2d(nr, nz), dim3(BX, BY), 0, s>>>(tau_z, tau_r, t11, t12, t22, R,
                                                                   nr, nz, dx);
@@ -481,7 +484,8 @@ extern "C" int axi_soft_diffusion_rk2_f64(double* vort, double* tmp, const doubl
                                           void* stream) {
   axi::clear_error();
   AXI_TRY(axi::check_grid("soft_diffusion_rk2", nr, nz));
-  AXI_TRY(axi::check_ptr("soft_diffusion_rk2", state, "state"));
+  AXI_TRY(axi::check_ptrs("soft_diffusion_rk2", {vort, tmp, R, state},
+                          {"vorticity", "temp_vorticity", "R", "state"}));
   cudaStream_t s = axi::as_stream(stream);
   const double dx2 = rn_host_mul(dx, dx), two_dx = rn_host_mul(2.0, dx);
   const double half_nu = rn_host_mul(0.5, nu);

@@ -204,7 +204,7 @@ extern "C" int axi_soft_dt_f64(const double* u_z, const double* u_r, int64_t n, 
                                void* stream) {
   axi::clear_error();
   AXI_TRY(check_n("soft_dt", n));
-  AXI_TRY(axi::check_ptr("soft_dt", state, "state"));
+  AXI_TRY(axi::check_ptrs("soft_dt", {u_z, u_r, state}, {"u_z", "u_r", "state"}));
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -219,6 +219,8 @@ extern "C" int axi_soft_pin_level_set_f64(double* ball_phi, const double* eta1,
                                           double r_ball, double band, void* stream) {
   axi::clear_error();
   AXI_TRY(check_n("soft_pin_level_set", n));
+  AXI_TRY(axi::check_ptrs("soft_pin_level_set", {ball_phi, eta1, eta2},
+                          {"ball_phi", "eta1", "eta2"}));
   pin_kernel<<<blocks_for(n), NT, 0, axi::as_stream(stream)>>>(ball_phi, eta1, eta2, n, z_cm,
                                                               r_ball, band);
   return axi::launch_status("soft_pin_level_set");
@@ -228,6 +230,7 @@ extern "C" int axi_soft_mask_f64(double* chi, uint8_t* inside, const double* phi
                                  double blend_w, void* stream) {
   axi::clear_error();
   AXI_TRY(check_n("soft_mask", n));
+  AXI_TRY(axi::check_ptrs("soft_mask", {chi, inside, phi}, {"chi", "inside", "phi"}));
   mask_kernel<<<blocks_for(n), NT, 0, axi::as_stream(stream)>>>(chi, inside, phi, n, blend_w);
   return axi::launch_status("soft_mask");
 }
@@ -236,6 +239,7 @@ extern "C" int axi_soft_stress_mask_f64(double* s11, double* s12, double* s22, c
                                         int64_t n, void* stream) {
   axi::clear_error();
   AXI_TRY(check_n("soft_stress_mask", n));
+  AXI_TRY(axi::check_ptrs("soft_stress_mask", {s11, s12, s22, chi}, {"s11", "s12", "s22", "chi"}));
   stress_mask_kernel<<<blocks_for(n), NT, 0, axi::as_stream(stream)>>>(s11, s12, s22, chi, n);
   return axi::launch_status("soft_stress_mask");
 }
@@ -246,7 +250,8 @@ extern "C" int axi_soft_tether_f64(double* tether_chi, const double* Z, const do
                                    void* stream) {
   axi::clear_error();
   AXI_TRY(check_n("soft_tether", n));
-  AXI_TRY(axi::check_ptr("soft_tether", state, "state"));
+  AXI_TRY(axi::check_ptrs("soft_tether", {tether_chi, Z, R, state},
+                          {"tether_chi", "Z", "R", "state"}));
   tether_kernel<<<blocks_for(n), NT, 0, axi::as_stream(stream)>>>(
       tether_chi, Z, R, n, state, z_cm, e_r_ball, omega, zeta_r_ball, blend_w);
   return axi::launch_status("soft_tether");
@@ -258,7 +263,8 @@ extern "C" int axi_soft_penalise_f64(double* omega, double* u_z, double* u_r,
                                      const double* state, void* stream) {
   axi::clear_error();
   AXI_TRY(axi::check_grid("soft_penalise", nr, nz));
-  AXI_TRY(axi::check_ptr("soft_penalise", state, "state"));
+  AXI_TRY(axi::check_ptrs("soft_penalise", {omega, u_z, u_r, tether_chi, d_z, d_r, state},
+                          {"omega", "u_z", "u_r", "tether_chi", "d_z", "d_r", "state"}));
   const long long n = (long long)nr * nz;
   cudaStream_t s = axi::as_stream(stream);
   brinkman_kernel<<<blocks_for(n), NT, 0, s>>>(u_z, u_r, tether_chi, d_z, d_r, n, state, lam, U0,

@@ -93,3 +93,44 @@ def test_spectral_transforms_reject_null_fields():
         st = lib.axi_fd_transform_static_f64(out, 8, inp, 8, fake, fake, fake, fake, fake, 8, 8,
                                              null)
         assert st == N.AXI_ERR_INVALID and b"fd_transform_static" in lib.axi_last_error()
+
+
+def test_soft_loop_entries_reject_null_pointers():
+    """Every pointer argument of the device-resident soft-loop entries is
+    checked on the host: a null one comes back as AXI_ERR_INVALID naming the
+    argument, before any launch (the stream argument, last, may be null)."""
+    import ctypes as c
+
+    from pyaxisymflow_gb300 import _native as N
+    lib = N.lib()
+    F = 4096  # fake non-null device address, never dereferenced
+    n, nr, nz = 64, 8, 8
+    # (entry, arguments with fake pointers as "P", positions of the pointers checked)
+    calls = {
+        "axi_soft_dt_f64": ["P", "P", n, "P", 1.0, 0.1, 1.0, 1e-10, None],
+        "axi_soft_advect_eno3_f64": ["P", "P", 1, "P", "P", "P", nr, nz, 0.1, "P", None],
+        "axi_soft_pin_level_set_f64": ["P", "P", "P", n, 0.5, 0.1, 0.05, None],
+        "axi_soft_mask_f64": ["P", "P", "P", n, 0.01, None],
+        "axi_soft_extrapolate_eta_f64": ["P", "P", "P", "P", "P", "P", "P", "P", "P", 0.1, nr, nz,
+                                         "P", "P", 10, "P", "P", None],
+        "axi_soft_stress_mask_f64": ["P", "P", "P", "P", n, None],
+        "axi_soft_update_vorticity_from_solid_stress_f64": ["P", "P", "P", "P", "P", "P", "P", nr,
+                                                            nz, 0.1, "P", None],
+        "axi_soft_tether_f64": ["P", "P", "P", n, "P", 0.5, 0.1, 6.28, 0.1, 0.01, None],
+        "axi_soft_penalise_f64": ["P", "P", "P", "P", "P", "P", nr, nz, 0.1, 1e6, 0.1, 6.28, "P",
+                                  None],
+        "axi_soft_diffusion_rk2_f64": ["P", "P", "P", nr, nz, 0.01, 0.1, "P", None],
+        "axi_soft_advance_f64": ["P", None],
+    }
+    for name, proto in calls.items():
+        fn = getattr(lib, name)
+        ptrs = [q for q, a in enumerate(proto) if a == "P"]
+        assert ptrs, name
+        for q in ptrs:
+            args = [c.c_void_p(F) if a == "P" else (c.c_void_p(None) if a is None else a)
+                    for a in proto]
+            args[q] = c.c_void_p(None)
+            st = fn(*args)
+            assert st == N.AXI_ERR_INVALID, (name, q, st)
+            msg = lib.axi_last_error()
+            assert b"null" in msg and name[4:-4].encode() in msg, (name, q, msg)
