@@ -115,7 +115,9 @@ int eno3_launch(T* f0, T* f1, T par0, T par1, const T* uz, const T* ur, T* scrat
     axi::set_error("%s: grid %d x %d too small for ENO3 (needs nr >= 3, nz >= 5)", what, nr, nz);
     return AXI_ERR_INVALID;
   }
-  AXI_TRY(axi::check_ptr(what, scratch, "scratch"));
+  AXI_TRY(axi::check_ptrs(what, {f0, uz, ur, scratch},
+                          {NF == 2 ? "eta1" : "vorticity", "u_z", "u_r", "scratch"}));
+  if (NF == 2) AXI_TRY(axi::check_ptr(what, f1, "eta2"));
   const size_t bytes = (size_t)nr * nz * sizeof(T);
   if (cudaMemcpyAsync(scratch, f0, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
     return axi::launch_status(what);

@@ -317,7 +317,9 @@ int lsq_run(int16_t* cf, const int16_t* tf, double* ex, double* ey, const double
     axi::set_error("%s: invalid size %d x %d", what, n0, n1);
     return AXI_ERR_INVALID;
   }
-  AXI_TRY(axi::check_ptr(what, work, "work"));
+  AXI_TRY(axi::check_ptrs(what, {cf, tf, ex, ey, gx, gy, work},
+                          {"current_flag", "target_flag", "eta_x", "eta_y", "grid_x", "grid_y",
+                           "work"}));
   const long long n = (long long)n0 * n1;
   char* base = static_cast<char*>(work);
   LsqHeader* hdr = reinterpret_cast<LsqHeader*>(base);
@@ -414,6 +416,12 @@ extern "C" int axi_extrapolate_eta_with_least_squares_f64(
     axi::set_error("%s: invalid grid %d x %d", what, nr, nz);
     return AXI_ERR_INVALID;
   }
+  AXI_TRY(axi::check_ptrs(what,
+                          {inside_solid, ball_phi, eta1, eta2, ball_phi_double, eta1_double,
+                           eta2_double, current_flag, target_flag, grid_x, grid_y, work},
+                          {"inside_solid", "ball_phi", "eta1", "eta2", "ball_phi_double",
+                           "eta1_double", "eta2_double", "current_flag", "target_flag", "grid_x",
+                           "grid_y", "work"}));
   cudaStream_t s = axi::as_stream(stream);
   dim3 g2(axi::ceil_div(nz, 128), 2 * nr);
   lsq_prepare_kernel<<<g2, 128, 0, s>>>(inside_solid, ball_phi, eta1, eta2, ball_phi_double,

@@ -297,6 +297,7 @@ int ghost_comm(T* f, int nr, int nz, int g, bool eta, T z_max, T dx, cudaStream_
     axi::set_error("periodic_ghost_comm: invalid ghost size %d for nz = %d", g, nz);
     return AXI_ERR_INVALID;
   }
+  AXI_TRY(axi::check_ptr("periodic_ghost_comm", f, "field"));
   const int threads = 2 * g <= 256 ? 2 * g : 256;
   dim3 grid(axi::ceil_div(2 * g, threads), nr);
   ghost_comm_kernel<T><<<grid, threads, 0, s>>>(f, nr, nz, g, eta, z_max,
@@ -315,6 +316,8 @@ int ghost_comm(T* f, int nr, int nz, int g, bool eta, T z_max, T dx, cudaStream_
                                                  int nr, int nz, T dx, void* stream) {        \
     axi::clear_error();                                                                       \
     AXI_TRY(axi::check_grid("velocity_from_psi", nr, nz));                                    \
+    AXI_TRY(axi::check_ptrs("velocity_from_psi", {u_z, u_r, psi, R},                           \
+                            {"u_z", "u_r", "psi", "R"}));                                      \
     velocity_from_psi_kernel<T><<<grid2d(nr, nz), dim3(BX, BY), 0, axi::as_stream(stream)>>>( \
         u_z, u_r, psi, R, nr, nz, dx);                                                        \
     return axi::launch_status("velocity_from_psi");                                           \
@@ -324,6 +327,8 @@ int ghost_comm(T* f, int nr, int nz, int g, bool eta, T z_max, T dx, cudaStream_
                                                       void* stream) {                         \
     axi::clear_error();                                                                       \
     AXI_TRY(axi::check_grid("velocity_from_psi_periodic", nr, nz));                           \
+    AXI_TRY(axi::check_ptrs("velocity_from_psi_periodic", {u_z, u_r, psi, R},                  \
+                            {"u_z", "u_r", "psi", "R"}));                                      \
     AXI_TRY(ghost_comm<T>(psi, nr, nz, ghost, false, T(0), dx, axi::as_stream(stream)));      \
     velocity_from_psi_kernel<T><<<grid2d(nr, nz), dim3(BX, BY), 0, axi::as_stream(stream)>>>( \
         u_z, u_r, psi, R, nr, nz, dx);                                                        \
@@ -335,6 +340,8 @@ int ghost_comm(T* f, int nr, int nz, int g, bool eta, T z_max, T dx, cudaStream_
                                                        int nr, int nz, T dx, void* stream) {  \
     axi::clear_error();                                                                       \
     AXI_TRY(axi::check_grid("vorticity_from_velocity", nr, nz));                              \
+    AXI_TRY(axi::check_ptrs("vorticity_from_velocity", {vort, u_z, u_r},                       \
+                            {"vort", "u_z", "u_r"}));                                          \
     vorticity_from_velocity_kernel<T>                                                         \
         <<<grid2d(nr, nz), dim3(BX, BY), 0, axi::as_stream(stream)>>>(vort, u_z, u_r, nr, nz,  \
                                                                       dx);                    \
@@ -345,6 +352,8 @@ int ghost_comm(T* f, int nr, int nz, int g, bool eta, T z_max, T dx, cudaStream_
                                                             void* stream) {                   \
     axi::clear_error();                                                                       \
     AXI_TRY(axi::check_grid("vorticity_from_velocity_periodic", nr, nz));                     \
+    AXI_TRY(axi::check_ptrs("vorticity_from_velocity_periodic", {vort, u_z, u_r},              \
+                            {"vort", "u_z", "u_r"}));                                          \
     AXI_TRY(ghost_comm<T>(u_r, nr, nz, ghost, false, T(0), dx, axi::as_stream(stream)));      \
     AXI_TRY(ghost_comm<T>(u_z, nr, nz, ghost, false, T(0), dx, axi::as_stream(stream)));      \
     vorticity_from_velocity_kernel<T>                                                         \
@@ -360,6 +369,9 @@ int ghost_comm(T* f, int nr, int nz, int g, bool eta, T z_max, T dx, cudaStream_
     axi::clear_error();                                                                        \
     if (n < 0) { axi::set_error("brinkmann_penalize: negative size"); return AXI_ERR_INVALID; } \
     if (n == 0) return AXI_OK;                                                                 \
+    AXI_TRY(axi::check_ptrs("brinkmann_penalize", {chi, gz, gr, pz, pr},                       \
+                            {"char_func", "grid_u_z", "grid_u_r", "penalized_u_z",             \
+                             "penalized_u_r"}));                                               \
     brinkman_kernel<T><<<axi::ceil_div(n, 256), 256, 0, axi::as_stream(stream)>>>(            \
         lam, dt, chi, U_z, U_r, gz, gr, pz, pr, n);                                            \
     return axi::launch_status("brinkmann_penalize");                                          \
@@ -368,6 +380,7 @@ int ghost_comm(T* f, int nr, int nz, int g, bool eta, T z_max, T dx, cudaStream_
     axi::clear_error();                                                                        \
     if (n < 0) { axi::set_error("smooth_heaviside: negative size"); return AXI_ERR_INVALID; }  \
     if (n == 0) return AXI_OK;                                                                 \
+    AXI_TRY(axi::check_ptrs("smooth_heaviside", {H, phi}, {"H", "phi"}));                      \
     heaviside_kernel<T><<<axi::ceil_div(n, 256), 256, 0, axi::as_stream(stream)>>>(H, phi, w, n); \
     return axi::launch_status("smooth_heaviside");                                             \
   }                                                                                            \
@@ -378,6 +391,7 @@ int ghost_comm(T* f, int nr, int nz, int g, bool eta, T z_max, T dx, cudaStream_
       axi::set_error("kill_boundary_vorticity_sine_z: width %d unsupported for nz = %d", width, nz); \
       return AXI_ERR_INVALID;                                                                  \
     }                                                                                          \
+    AXI_TRY(axi::check_ptrs("kill_boundary_vorticity_sine_z", {vort, Z}, {"vorticity", "Z"})); \
     kill_z_kernel<T><<<axi::ceil_div(nr, 128), 128, 0, axi::as_stream(stream)>>>(vort, Z, nr, nz, \
                                                                                  width, dx);   \
     return axi::launch_status("kill_boundary_vorticity_sine_z");                               \
@@ -389,6 +403,7 @@ int ghost_comm(T* f, int nr, int nz, int g, bool eta, T z_max, T dx, cudaStream_
       axi::set_error("kill_boundary_vorticity_sine_r: width %d unsupported for nr = %d", width, nr); \
       return AXI_ERR_INVALID;                                                                  \
     }                                                                                          \
+    AXI_TRY(axi::check_ptrs("kill_boundary_vorticity_sine_r", {vort, R}, {"vorticity", "R"})); \
     kill_r_kernel<T><<<axi::ceil_div(nz, 128), 128, 0, axi::as_stream(stream)>>>(vort, R, nr, nz, \
                                                                                  width, dx);   \
     return axi::launch_status("kill_boundary_vorticity_sine_r");                               \
@@ -397,6 +412,8 @@ int ghost_comm(T* f, int nr, int nz, int g, bool eta, T z_max, T dx, cudaStream_
                                              T dt, T dx, void* stream) {                       \
     axi::clear_error();                                                                        \
     AXI_TRY(axi::check_grid("diffusion_rk2", nr, nz));                                         \
+    AXI_TRY(axi::check_ptrs("diffusion_rk2", {vort, tmp, R},                                   \
+                            {"vorticity", "temp_vorticity", "R"}));                            \
     cudaStream_t s = axi::as_stream(stream);                                                   \
     const T dx2 = rn_host_mul(dx, dx), two_dx = rn_host_mul(T(2), dx);                         \
     const T c1 = rn_host_mul(rn_host_mul(T(0.5), nu), dt), c2 = rn_host_mul(nu, dt);           \
@@ -410,6 +427,8 @@ int ghost_comm(T* f, int nr, int nz, int g, bool eta, T z_max, T dx, cudaStream_
                                                   T nu, T dt, T dx, int ghost, void* stream) { \
     axi::clear_error();                                                                        \
     AXI_TRY(axi::check_grid("diffusion_rk2_periodic", nr, nz));                                \
+    AXI_TRY(axi::check_ptrs("diffusion_rk2_periodic", {vort, tmp, R},                          \
+                            {"vorticity", "temp_vorticity", "R"}));                            \
     cudaStream_t s = axi::as_stream(stream);                                                   \
     const T dx2 = rn_host_mul(dx, dx), two_dx = rn_host_mul(T(2), dx);                         \
     const T c1 = rn_host_mul(rn_host_mul(T(0.5), nu), dt), c2 = rn_host_mul(nu, dt);           \
@@ -435,6 +454,9 @@ int ghost_comm(T* f, int nr, int nz, int g, bool eta, T z_max, T dx, cudaStream_
                                        int nz, void* stream) {                                 \
     axi::clear_error();                                                                        \
     AXI_TRY(axi::check_grid("solid_sigma", nr, nz));                                           \
+    AXI_TRY(axi::check_ptrs("solid_sigma", {s11, s12, s22, e1, e2, e1z, e1r, e2z, e2r},        \
+                            {"sigma_11", "sigma_12", "sigma_22", "eta1", "eta2", "eta1_z",     \
+                             "eta1_r", "eta2_z", "eta2_r"}));                                  \
     solid_sigma_kernel<T><<<grid2d(nr, nz), dim3(BX, BY), 0, axi::as_stream(stream)>>>(        \
         s11, s12, s22, G, dx, e1, e2, e1z, e1r, e2z, e2r, nr, nz);                             \
     return axi::launch_status("solid_sigma");                                                  \
@@ -444,6 +466,10 @@ int ghost_comm(T* f, int nr, int nz, int g, bool eta, T z_max, T dx, cudaStream_
       int nr, int nz, T dt, T dx, void* stream) {                                              \
     axi::clear_error();                                                                        \
     AXI_TRY(axi::check_grid("update_vorticity_from_solid_stress", nr, nz));                    \
+    AXI_TRY(axi::check_ptrs("update_vorticity_from_solid_stress",                              \
+                            {vort, tau_z, tau_r, t11, t12, t22, R},                            \
+                            {"vorticity", "tau_z", "tau_r", "sigma_11", "sigma_12",            \
+                             "sigma_22", "R"}));                                               \
     cudaStream_t s = axi::as_stream(stream);                                                   \
     div_tau_kernel<T><<<grid2d(nr, nz), dim3(BX, BY), 0, s>>>(tau_z, tau_r, t11, t12, t22, R,  \
                                                                nr, nz, dx);                    \

@@ -106,8 +106,8 @@ int force_on_body(const T* R, const T* chi, double rho_f, double lam, const T* u
     axi::set_error("compute_force_on_body: empty field");
     return AXI_ERR_INVALID;
   }
-  AXI_TRY(axi::check_ptr("compute_force_on_body", partials, "partials"));
-  AXI_TRY(axi::check_ptr("compute_force_on_body", out, "out"));
+  AXI_TRY(axi::check_ptrs("compute_force_on_body", {R, chi, uz, partials, out},
+                          {"R", "char_func", "u_z", "partials", "out"}));
   const int nb = red_blocks(n);
   force_partials_kernel<T><<<nb, RED_THREADS, 0, s>>>(R, chi, uz, U, n, partials);
   finish_kernel<<<1, RED_THREADS, 0, s>>>(partials, nb, 1, 0, rho_f * lam, (diff * vol) / dt, out);
@@ -121,8 +121,8 @@ int projection(double rho, const T* chi, const T* uz, const T* ur, const T* R, l
     axi::set_error("force_projection: empty field");
     return AXI_ERR_INVALID;
   }
-  AXI_TRY(axi::check_ptr("force_projection", partials, "partials"));
-  AXI_TRY(axi::check_ptr("force_projection", out, "out"));
+  AXI_TRY(axi::check_ptrs("force_projection", {chi, uz, ur, R, partials, out},
+                          {"char_func", "u_z", "u_r", "R", "partials", "out"}));
   const int nb = red_blocks(n);
   projection_partials_kernel<T><<<nb, RED_THREADS, 0, s>>>(rho, chi, uz, ur, R, n, partials);
   finish_kernel<<<1, RED_THREADS, 0, s>>>(partials, nb, 3, 1, 0.0, 0.0, out);

@@ -134,3 +134,54 @@ def test_soft_loop_entries_reject_null_pointers():
             assert st == N.AXI_ERR_INVALID, (name, q, st)
             msg = lib.axi_last_error()
             assert b"null" in msg and name[4:-4].encode() in msg, (name, q, msg)
+
+
+def test_drop_in_entries_reject_null_pointers():
+    """The drop-in kernel entries (both precisions) check their field pointers
+    on the host too: with any one of them null the call returns
+    AXI_ERR_INVALID naming it, before any launch."""
+    import ctypes as c
+
+    from pyaxisymflow_gb300 import _native as N
+    lib = N.lib()
+    F = 4096  # fake non-null device address, never dereferenced
+    nr = nz = 16
+    n = nr * nz
+    for s in ("f64", "f32"):
+        calls = {
+            f"axi_velocity_from_psi_unb_{s}": ["P", "P", "P", "P", nr, nz, 0.1, None],
+            f"axi_velocity_from_psi_periodic_{s}": ["P", "P", "P", "P", nr, nz, 0.1, 1, None],
+            f"axi_vorticity_from_velocity_unb_{s}": ["P", "P", "P", nr, nz, 0.1, None],
+            f"axi_vorticity_from_velocity_periodic_{s}": ["P", "P", "P", nr, nz, 0.1, 1, None],
+            f"axi_brinkmann_penalize_{s}": [1e4, 0.01, "P", 0.0, 0.0, "P", "P", "P", "P", n, None],
+            f"axi_smooth_heaviside_{s}": ["P", "P", 0.1, n, None],
+            f"axi_kill_boundary_vorticity_sine_z_{s}": ["P", "P", nr, nz, 3, 0.1, None],
+            f"axi_kill_boundary_vorticity_sine_r_{s}": ["P", "P", nr, nz, 3, 0.1, None],
+            f"axi_diffusion_rk2_unb_{s}": ["P", "P", "P", nr, nz, 0.01, 0.01, 0.1, None],
+            f"axi_diffusion_rk2_periodic_{s}": ["P", "P", "P", nr, nz, 0.01, 0.01, 0.1, 1, None],
+            f"axi_periodic_ghost_comm_{s}": ["P", nr, nz, 1, None],
+            f"axi_compute_force_on_body_{s}": ["P", "P", 1.0, 1e4, "P", 0.0, 1.0, 0.01, 0.0, n,
+                                               "P", "P", None],
+            f"axi_force_projection_{s}": [1.0, "P", "P", "P", "P", n, "P", "P", None],
+            f"axi_advect_vorticity_eno3_{s}": ["P", "P", "P", "P", nr, nz, 0.1, None],
+            f"axi_advect_refmap_eno3_{s}": ["P", "P", "P", "P", "P", nr, nz, 0.1, None],
+            f"axi_solid_sigma_{s}": ["P", "P", "P", 1e-3, 0.1, "P", "P", "P", "P", "P", "P", nr,
+                                     nz, None],
+            f"axi_update_vorticity_from_solid_stress_{s}": ["P", "P", "P", "P", "P", "P", "P", nr,
+                                                            nz, 0.01, 0.1, None],
+        }
+        if s == "f64":
+            calls["axi_extrapolate_lsq_first_order_f64"] = ["P", "P", "P", "P", "P", "P", nr, nz,
+                                                            10, "P", None, None]
+            calls["axi_extrapolate_eta_with_least_squares_f64"] = [
+                "P", "P", "P", "P", "P", "P", "P", "P", "P", 0.1, nr, nz, "P", "P", 10, "P", None,
+                None]
+        for name, proto in calls.items():
+            fn = getattr(lib, name)
+            for q in [q for q, a in enumerate(proto) if a == "P"]:
+                args = [c.c_void_p(F) if a == "P" else (c.c_void_p(None) if a is None else a)
+                        for a in proto]
+                args[q] = c.c_void_p(None)
+                st = fn(*args)
+                assert st == N.AXI_ERR_INVALID, (name, q, st)
+                assert b"null" in lib.axi_last_error(), (name, q, lib.axi_last_error())
