@@ -231,6 +231,7 @@ extern "C" int axi_tc_transform_status(const axi_tc_plan_info* info, const void*
 extern "C" int axi_tc_split_f32(float* hi, float* lo, const float* x, int64_t n, void* stream) {
   axi::clear_error();
   if (n <= 0) return AXI_OK;
+  AXI_TRY(axi::check_ptrs("tc_split_f32", {hi, lo, x}, {"hi", "lo", "x"}));
   split_f32_kernel<<<axi::ceil_div(n, 256), 256, 0, axi::as_stream(stream)>>>(x, hi, lo, n);
   return axi::launch_status("tc_split_f32");
 }
@@ -238,6 +239,7 @@ extern "C" int axi_tc_split_f32(float* hi, float* lo, const float* x, int64_t n,
 extern "C" int axi_tc_split_f64(float* hi, float* lo, const double* x, int64_t n, void* stream) {
   axi::clear_error();
   if (n <= 0) return AXI_OK;
+  AXI_TRY(axi::check_ptrs("tc_split_f64", {hi, lo, x}, {"hi", "lo", "x"}));
   split_f64_kernel<<<axi::ceil_div(n, 256), 256, 0, axi::as_stream(stream)>>>(x, hi, lo, n);
   return axi::launch_status("tc_split_f64");
 }
@@ -251,6 +253,9 @@ extern "C" int axi_fd_residual_f64(double* res, const double* rhs, const double*
     axi::set_error("fd_residual: nr %d too large", nr);
     return AXI_ERR_INVALID;
   }
+  // row_weight may be null (no weight)
+  AXI_TRY(axi::check_ptrs("fd_residual", {res, rhs, psi, ar, az},
+                          {"residual", "rhs", "psi", "op_r", "op_z"}));
   dim3 grid(axi::ceil_div(nz, 256), nr);
   residual_kernel<<<grid, 256, 0, axi::as_stream(stream)>>>(res, rhs, psi, row_weight, ar, az, nr,
                                                             nz, wrap0, wrap1);
@@ -260,6 +265,7 @@ extern "C" int axi_fd_residual_f64(double* res, const double* rhs, const double*
 extern "C" int axi_add_f32_to_f64(double* y, const float* x, int64_t n, void* stream) {
   axi::clear_error();
   if (n <= 0) return AXI_OK;
+  AXI_TRY(axi::check_ptrs("add_f32_to_f64", {y, x}, {"y", "x"}));
   add_kernel<<<axi::ceil_div(n, 256), 256, 0, axi::as_stream(stream)>>>(y, x, n);
   return axi::launch_status("add_f32_to_f64");
 }
@@ -267,6 +273,7 @@ extern "C" int axi_add_f32_to_f64(double* y, const float* x, int64_t n, void* st
 extern "C" int axi_widen_f32_to_f64(double* y, const float* x, int64_t n, void* stream) {
   axi::clear_error();
   if (n <= 0) return AXI_OK;
+  AXI_TRY(axi::check_ptrs("widen_f32_to_f64", {y, x}, {"y", "x"}));
   widen_kernel<<<axi::ceil_div(n, 256), 256, 0, axi::as_stream(stream)>>>(y, x, n);
   return axi::launch_status("widen_f32_to_f64");
 }
